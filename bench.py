@@ -1,0 +1,342 @@
+#!/usr/bin/env python3
+"""Throughput benchmark of the GB300 Orthotope Machine kernels.
+
+Default workload: Conway's Life (examples/Life) on a 16384x16384 cyclic grid,
+int32 cells Bernoulli(0.3) from seed 1; one step = 100 generations with the
+population reduce after every generation.  Metric: Gcell-updates/s.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload life16k|life128|hydro4k|ensemble|adjoint]
+
+Prints one JSON line (rank 0).  Under torchrun (N > 1) every rank advances
+its own independent replica (no data-path collective; weak scaling).
+`--impl reference` times the CPU restatement of the reference's algorithm
+(oracle/) on all host cores, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+# ---------------------------------------------------------------------------
+# process group (replicas only: barrier + max-over-ranks timing)
+# ---------------------------------------------------------------------------
+
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# measurement helpers
+# ---------------------------------------------------------------------------
+
+def peaks() -> tuple[float, str]:
+    try:
+        with open(MEASURED_PEAKS) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows: list[list[str]] = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+        time.sleep(0.25)
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self) -> dict:
+        if self.proc:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm = []
+        mx = None
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_cores() -> int:
+    return os.cpu_count() or 1
+
+
+# ---------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------
+
+def life_workload(args, dist: Dist) -> dict:
+    import paraiso_gb300 as pg
+    from paraiso_gb300 import build as pgbuild
+    pgbuild.build()
+    n = args.size or (128 if args.workload == "life128" else 16384)
+    gens = args.generations or (1000 if args.workload == "life128" else 100)
+    cells = n * n
+    life = pg.Life((n, n), device=dist.local_rank, depth=args.depth, tile_x=args.tile_x,
+                   tile_y=args.tile_y)
+    life.fill_random(1 + dist.rank, 0.3)
+    kid = life.kernel_id("proceed")
+    # warm-up
+    for _ in range(args.warmup):
+        life.run("proceed", gens)
+    # timed region: K steps of `gens` generations, device time (CUDA events on
+    # the handle's stream), barrier + synchronize on both sides
+    clocks = ClockSampler(dist.local_rank)
+    clocks.start()
+    dist.barrier()
+    ms = life.time_run("proceed", gens * args.steps)
+    launches = life.last_launch_count()
+    dist.barrier()
+    clk = clocks.stop()
+    ms = dist.max(ms)
+    updates = cells * gens * args.steps * dist.world
+    value = updates / (ms * 1e-3) / 1e9
+
+    # dominant kernel: per-launch device time with events around each launch
+    life.profile(True)
+    life.time_run("proceed", gens * min(args.steps, 4))
+    kname = "life_smallgrid_kernel" if n * n // 32 <= 4096 else "life_tb_kernel"
+    nl, kms, kunits = life.profile_query(kname)
+    life.profile(False)
+    peak, peak_kind = peaks()
+    bytes_per_update = 8.0           # int32 read + int32 write per cell-update
+    per_launch_units = kunits / max(nl, 1)
+    per_launch_ms = kms / max(nl, 1)
+    achieved = bytes_per_update * per_launch_units / (per_launch_ms * 1e-3) / 1e9
+    traffic = profile_traffic(kname, n)
+    roofline = {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1),
+                "peak": peak, "peak_source": f"{peak_kind} MEASURED_PEAKS.json hbm_gbs"
+                if peak_kind == "measured" else "fallback 6.8 TB/s",
+                "unit": "GB/s", "frac": round(achieved / peak, 3),
+                "traffic": traffic["bytes_per_launch"] if traffic else None,
+                "algorithmic_bytes_per_launch": bytes_per_update * per_launch_units,
+                "launch_ms": round(per_launch_ms, 4), "launches_profiled": nl,
+                "note": "algorithmic 8 B per cell-update; temporal blocking re-uses each "
+                        "loaded cell for several generations, so frac may exceed 1"}
+    if traffic:
+        roofline["dram_gbs"] = round(traffic["bytes_per_launch"] / (per_launch_ms * 1e-3) / 1e9, 1)
+        roofline["dram_frac"] = round(roofline["dram_gbs"] / peak, 3)
+
+    # end to end through the public API with host buffers: per step, upload
+    # the cells from pinned host memory, run `gens` generations, read the
+    # cells and the population back
+    import torch
+    host_in = torch.empty(cells, dtype=torch.int32).pin_memory()
+    host_out = torch.empty(cells, dtype=torch.int32).pin_memory()
+    life.read_to_pointer("cell", host_in.data_ptr(), cells * 4)
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    dist.barrier()
+    t0 = time.perf_counter()
+    pops = []
+    for _ in range(e2e_steps):
+        life.write_from_pointer("cell", host_in.data_ptr(), cells * 4)
+        life.run("proceed", gens)
+        life.read_to_pointer("cell", host_out.data_ptr(), cells * 4)
+        pops.append(life.population)
+    t1 = time.perf_counter()
+    dist.barrier()
+    e2e_s = dist.max(t1 - t0)
+    e2e = {"value": round(cells * gens * e2e_steps * dist.world / e2e_s / 1e9, 3),
+           "unit": "Gcell-updates/s", "h2d_bytes_per_step": cells * 4,
+           "d2h_bytes_per_step": cells * 4 + 4, "steps": e2e_steps,
+           "api": "om_array_write + om_run_n(proceed) + om_array_read + population scalar"}
+    life.close()
+
+    out = {
+        "metric": "Life cell-updates/s (Gcell-updates/s), bit-exact vs the oracle",
+        "value": round(value, 3), "unit": "Gcell-updates/s", "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": f"life {n}x{n} cyclic, Bernoulli(0.3) seed 1+rank, "
+                               f"{gens} generations per step, population reduce every generation",
+                   "n0": n, "n1": n, "generations_per_step": gens,
+                   "parallelism": f"replicas x{dist.world}",
+                   "l2": "inputs larger than L2 (2 x 1 GiB int32 buffers)" if n >= 8192
+                   else "grid resident in shared memory (launch-bound case)"},
+        "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+    }
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = life_cpu_baseline(n, args)
+    return out
+
+
+def profile_traffic(kernel: str, n: int):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        if d.get("n") == n:
+            return d
+    except Exception:
+        pass
+    return None
+
+
+def life_cpu_baseline(n: int, args) -> dict:
+    from oracle import pyoracle as O
+    O.build()
+    gens = 3 if n >= 8192 else 200
+    a = O.life_bernoulli(n, n, 1, 0.3)
+    t0 = time.perf_counter()
+    O.life_run(a, gens, cyclic=True)
+    dt = time.perf_counter() - t0
+    return {"value": round(n * n * gens / dt / 1e9, 4), "unit": "Gcell-updates/s",
+            "cores": O.lib().oracle_num_threads(), "kind": "port",
+            "sample": f"{n}x{n} cyclic Bernoulli(0.3), {gens} generations, oracle/om_oracle.cpp "
+                      f"(OpenMP), {dt:.2f} s"}
+
+
+def reference_arm(args, dist: Dist) -> dict | None:
+    if dist.rank != 0:
+        return None
+    from oracle import pyoracle as O
+    O.build()
+    n = args.size or (128 if args.workload == "life128" else 16384)
+    gens_full = args.generations or (1000 if args.workload == "life128" else 100)
+    sample_gens = 2 if n >= 8192 else gens_full
+    a = O.life_bernoulli(n, n, 1, 0.3)
+    for _ in range(min(args.warmup, 1)):
+        a, _ = O.life_run(a, 1, cyclic=True)
+    times = []
+    for _ in range(args.steps if n < 8192 else min(args.steps, 5)):
+        t0 = time.perf_counter()
+        a, _ = O.life_run(a, sample_gens, cyclic=True)
+        times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    value = n * n * sample_gens * len(times) / tot / 1e9
+    cores = O.lib().oracle_num_threads()
+    return {
+        "impl": "reference", "metric": "Life cell-updates/s (Gcell-updates/s), bit-exact vs the oracle",
+        "value": round(value, 4), "unit": "Gcell-updates/s", "n_gpus": dist.world,
+        "steps": len(times), "warmup": args.warmup,
+        "ms_per_step": round(tot / len(times) * 1e3 * gens_full / sample_gens, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic",
+        "config": {"workload": f"life {n}x{n} cyclic, Bernoulli(0.3) seed 1, {gens_full} "
+                               f"generations per step", "n0": n, "n1": n},
+        "cpu_baseline": {"value": round(value, 4), "unit": "Gcell-updates/s", "cores": cores,
+                         "kind": "port",
+                         "sample": f"{sample_gens} of {gens_full} generations per step on {n}x{n}; "
+                                   "CPU restatement (oracle/om_oracle.cpp, OpenMP) of the "
+                                   "generated Life loop, pinned bit-exact to the reference's "
+                                   "pre-generated Life.cpp"},
+        "e2e": {"value": round(value, 4), "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="life16k",
+                    choices=["life16k", "life128"])
+    ap.add_argument("--size", type=int, default=0)
+    ap.add_argument("--generations", type=int, default=0)
+    ap.add_argument("--depth", type=int, default=0)
+    ap.add_argument("--tile-x", type=int, default=0)
+    ap.add_argument("--tile-y", type=int, default=0)
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            out = reference_arm(args, dist)
+        else:
+            out = life_workload(args, dist)
+        if out is not None and dist.rank == 0:
+            print(json.dumps(out), flush=True)
+    finally:
+        dist.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,172 @@
+/*
+ * om_gb300.h -- C ABI of the GB300 (sm_103a) Orthotope Machine runtime.
+ *
+ * Paraiso's generator (Language/Paraiso/Generator/PlanTrans.hs) prints one
+ * C++ class per Orthotope Machine.  Its members -- constructor, size and
+ * margin accessors, scalar/array accessors, named kernels such as
+ * init/proceed -- are what drivers such as examples/Life/main.cpp and
+ * examples/Hydro/main-kh.cpp call.  This header exposes the same members
+ * as plain C functions over an opaque handle, so the header-only shims
+ * include/Life.hpp and include/Hydro.hpp rebuild the generated class on
+ * top of it, and any FFI (ctypes, cgo, JNI) can bind it.
+ *
+ * Conventions
+ *  - Every entry point returns om_status; OM_OK is 0.  On failure,
+ *    om_last_error() returns a thread-local description.  (The generated
+ *    class has no runtime error reporting at all.)
+ *  - Arrays are stored x-fastest with margins:
+ *      addr = (lower_margin_0 + i0) + memory_size_0 * (lower_margin_1 + i1)
+ *    (PlanTrans.hs:136-151).  Cyclic boundary has zero margins
+ *    (Language/Paraiso/Generator/OMTrans.hs:103-116).
+ *  - Host/device mirror semantics follow the generated CUDA container
+ *    (PlanTrans.hs:724-728): om_array_host marks the host copy newer and
+ *    the next kernel uploads it; om_array_host_const only refreshes it.
+ *  - A handle is not thread-safe; use one handle per host thread, as with
+ *    the generated class.  All work is queued on the handle's stream and
+ *    every om_run returns with that stream synchronised.
+ */
+#ifndef OM_GB300_H
+#define OM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  OM_OK = 0,
+  OM_ERR_ARG = 1,          /* bad argument, unknown name, size out of range */
+  OM_ERR_CUDA = 2,         /* CUDA runtime error (text in om_last_error) */
+  OM_ERR_UNSUPPORTED = 3,  /* configuration not implemented */
+  OM_ERR_NOMEM = 4,        /* device or pinned host allocation failed */
+  OM_ERR_NONFINITE = 5,    /* a NaN/Inf was detected in a reduction */
+  OM_ERR_TIMEOUT = 6,      /* a bounded device-side wait gave up */
+  OM_ERR_STATE = 7         /* call not valid in the handle's current state */
+} om_status;
+
+typedef enum { OM_KIND_LIFE = 1, OM_KIND_HYDRO = 2 } om_kind;
+typedef enum { OM_BOUNDARY_CYCLIC = 0, OM_BOUNDARY_OPEN = 1 } om_boundary;
+typedef enum { OM_SCALAR_INT = 0, OM_SCALAR_DOUBLE = 1 } om_scalar_type;
+
+typedef struct om_handle_s *om_handle;
+
+/* Runtime counterpart of Native.Setup (Language/Paraiso/Generator/Native.hs:16-24):
+ * boundary per OM, plus the knobs the GB300 kernels expose to the tuner. */
+typedef struct {
+  int boundary;     /* om_boundary; applies to every axis */
+  int precision;    /* Hydro: 32 = FP32 bulk with FP64 dt and totals; 64 = FP64 */
+  double gamma;     /* Hydro: ratio of specific heats (kGamma, examples/Hydro/Hydro.hs:53-54) */
+  int device;       /* CUDA device ordinal */
+  int depth;        /* Life: generations per temporally blocked launch (0 = tuned) */
+  int tile_x;       /* Life: tile width in 32-cell words; Hydro: tile width in cells (0 = tuned) */
+  int tile_y;       /* tile height in cells (0 = tuned) */
+  int use_graph;    /* capture om_run_n in a CUDA graph (default 1) */
+  int variant;      /* 0 = fastest path.  Life 1: integer one-cell-per-thread kernel only.
+                       Hydro 1: plain unfused FP64-structured grid-stride kernels */
+  int reserved[7];
+} om_config;
+
+/* Fill `cfg` with defaults: cyclic, FP32, gamma 5/3, device 0, tuned tiles. */
+void om_config_default(om_config *cfg);
+
+/* Text of the last error raised on this host thread ("" if none). */
+const char *om_last_error(void);
+
+/* Library version string. */
+const char *om_version(void);
+
+/* ---- construction ----------------------------------------------------- */
+
+/* Replaces the generated class constructor (PlanTrans.hs:75-86), with the
+ * mesh size (Native.localSize) given at run time.  kind: om_kind; ndim: 2;
+ * sizes[ndim]: interior extent per axis.  Allocates every array with
+ * om_memory_size elements, zero-filled, as the generated constructor does. */
+om_status om_create(int kind, int ndim, const int *sizes, const om_config *cfg,
+                    om_handle *out);
+
+/* Releases the handle and all its device and host memory. */
+om_status om_destroy(om_handle h);
+
+/* ---- sizes (PlanTrans.hs:167-215) -------------------------------------
+ * axis = -1 gives the product over axes (om_size / om_memory_size). */
+om_status om_size(om_handle h, int axis, int *out);
+om_status om_memory_size(om_handle h, int axis, int *out);
+om_status om_lower_margin(om_handle h, int axis, int *out);
+om_status om_upper_margin(om_handle h, int axis, int *out);
+
+/* ---- kernels (PlanTrans.hs:225-277) ------------------------------------ */
+
+/* Kernel index by name ("init", "proceed", ...). */
+om_status om_kernel_id(om_handle h, const char *name, int *id);
+/* Runs one kernel: `void init()` / `void proceed()` of the generated class. */
+om_status om_run(om_handle h, int kernel_id);
+/* Runs a kernel n times back to back (a driver's step loop), captured in a
+ * CUDA graph when cfg.use_graph is set.  Scalars are synced once at the end. */
+om_status om_run_n(om_handle h, int kernel_id, int n);
+
+/* ---- static variable accessors (PlanTrans.hs:117-157) ------------------ */
+
+/* Host pointer to a Scalar static (`T& name()`); valid for the handle's
+ * lifetime.  Writes take effect at the next om_run; om_run refreshes it. */
+om_status om_scalar_ptr(om_handle h, const char *name, void **ptr, int *type);
+
+/* Host mirror of an Array static (`container<T>& name()`, `T& name(i0,i1)`),
+ * memory-sized.  Downloads if the device copy is newer, then marks the host
+ * copy newer so the next kernel uploads it (thrust_vector::operator[]). */
+om_status om_array_host(om_handle h, const char *name, void **ptr,
+                        size_t *count, int *elem_size);
+/* Same, read-only: refreshes the host copy without marking it newer. */
+om_status om_array_host_const(om_handle h, const char *name, const void **ptr,
+                              size_t *count, int *elem_size);
+/* Device pointer of an Array static (thrust_vector::raw()): uploads if the
+ * host copy is newer, then marks the device copy newer.  Valid until the
+ * next kernel (statics are double-buffered and swap on every step). */
+om_status om_array_device(om_handle h, const char *name, void **dptr);
+/* Copy an array out of / into caller memory (host or device pointer;
+ * cudaMemcpyDefault), memory-sized. */
+om_status om_array_read(om_handle h, const char *name, void *dst, size_t bytes);
+om_status om_array_write(om_handle h, const char *name, const void *src, size_t bytes);
+
+/* ---- synthetic inputs and extra results (no counterpart in the generated
+ * class: benchmark inputs and multi-step reduce results) ---------------- */
+
+/* Life: every interior cell i = x + n0*y alive iff
+ * (splitmix-style hash(seed, i) >> 11) < floor(p * 2^53); margins 0. */
+om_status om_life_fill_random(om_handle h, uint64_t seed, double p);
+/* Life: populations after each generation of the last om_run / om_run_n
+ * (the `reduce Sum` of examples/Life/Generator.hs:110).  Copies min(n, kept). */
+om_status om_life_population_history(om_handle h, int32_t *out, int n, int *written);
+
+/* Hydro: Kelvin-Helmholtz state on cell centres of the unit square (periodic):
+ * rho 2 in |y-0.5|<0.25 else 1, vx +0.5/-0.5, vy = 0.01 sin(4 pi x) +
+ * 0.01 (2u-1), u = (hash(seed,i) >> 11) 2^-53, p 2.5; sets extent 1,
+ * dR = 1/n, time 0. */
+om_status om_hydro_init_kh(om_handle h, uint64_t seed);
+/* Hydro: compensated FP64 sums over the interior of mass, x momentum,
+ * y momentum and total energy (out[4]); OM_ERR_NONFINITE if any is not finite. */
+om_status om_hydro_totals(om_handle h, double *out);
+/* Hydro: dt of each step of the last om_run / om_run_n. */
+om_status om_hydro_dt_history(om_handle h, double *out, int n, int *written);
+
+/* ---- measurement ------------------------------------------------------- */
+
+/* Runs a kernel n times inside CUDA events on the handle's stream and
+ * returns the elapsed device time in milliseconds. */
+om_status om_time_run(om_handle h, int kernel_id, int n, float *ms);
+/* Number of kernel launches issued by the last om_run / om_run_n / om_time_run. */
+om_status om_last_launch_count(om_handle h, int *launches);
+/* Per-launch device timing: while enabled, every kernel launch is bracketed
+ * by CUDA events on the handle's stream (runs then skip graph capture).
+ * Disabling clears the totals. */
+om_status om_profile_enable(om_handle h, int enable);
+/* Totals for one kernel (by its __global__ name, e.g. "life_tb_kernel"):
+ * launches, summed device milliseconds and summed work units (cell-updates). */
+om_status om_profile_query(om_handle h, const char *kernel, long *launches,
+                           double *total_ms, double *total_units);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,10 @@
+"""GB300 (sm_103a) backend for Paraiso's Orthotope Machine kernels.
+
+The compute path is libom_gb300.so (CUDA, built in-tree by
+paraiso_gb300.build); this package is its host-side mirror of the
+generated OM classes."""
+from .om import (CYCLIC, OPEN, Config, Hydro, Life, OMError, OrthotopeMachine,  # noqa: F401
+                 default_config, load_library, EXPORTS)
+
+__all__ = ["Life", "Hydro", "OrthotopeMachine", "Config", "OMError", "default_config",
+           "load_library", "CYCLIC", "OPEN", "EXPORTS"]

@@ -1,0 +1,337 @@
+"""Python host side of the GB300 Orthotope Machine runtime.
+
+Mirrors the class Paraiso's generator prints per OM
+(Language/Paraiso/Generator/PlanTrans.hs:51-277): a constructor taking the
+mesh size, `om_size*` / `om_memory_size*` / margin accessors, one accessor
+per static variable, and one method per kernel (`init`, `proceed`).  Every
+call goes through the C ABI of include/om_gb300.h in libom_gb300.so; there
+is no other compute path, and constructing an object fails loudly when the
+library or a GPU is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libom_gb300.so")
+
+OM_OK = 0
+KIND_LIFE = 1
+KIND_HYDRO = 2
+CYCLIC = 0
+OPEN = 1
+
+STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_UNSUPPORTED", 4: "ERR_NOMEM",
+          5: "ERR_NONFINITE", 6: "ERR_TIMEOUT", 7: "ERR_STATE"}
+
+# every entry point declared in include/om_gb300.h
+EXPORTS = [
+    "om_config_default", "om_last_error", "om_version", "om_create", "om_destroy",
+    "om_size", "om_memory_size", "om_lower_margin", "om_upper_margin",
+    "om_kernel_id", "om_run", "om_run_n", "om_scalar_ptr", "om_array_host",
+    "om_array_host_const", "om_array_device", "om_array_read", "om_array_write",
+    "om_life_fill_random", "om_life_population_history", "om_hydro_init_kh",
+    "om_hydro_totals", "om_hydro_dt_history", "om_time_run", "om_last_launch_count",
+    "om_profile_enable", "om_profile_query",
+]
+
+
+class OMError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Config(C.Structure):
+    _fields_ = [("boundary", C.c_int), ("precision", C.c_int), ("gamma", C.c_double),
+                ("device", C.c_int), ("depth", C.c_int), ("tile_x", C.c_int),
+                ("tile_y", C.c_int), ("use_graph", C.c_int), ("variant", C.c_int),
+                ("reserved", C.c_int * 7)]
+
+
+_lib = None
+
+
+def load_library(path: str | None = None) -> C.CDLL:
+    """Load libom_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise ImportError(f"{p} is missing: build it with paraiso_gb300.build.build()")
+    L = C.CDLL(p)
+    vp, i, ip = C.c_void_p, C.c_int, C.POINTER(C.c_int)
+    sig = {
+        "om_config_default": (None, [C.POINTER(Config)]),
+        "om_last_error": (C.c_char_p, []),
+        "om_version": (C.c_char_p, []),
+        "om_create": (i, [i, i, ip, C.POINTER(Config), C.POINTER(vp)]),
+        "om_destroy": (i, [vp]),
+        "om_size": (i, [vp, i, ip]),
+        "om_memory_size": (i, [vp, i, ip]),
+        "om_lower_margin": (i, [vp, i, ip]),
+        "om_upper_margin": (i, [vp, i, ip]),
+        "om_kernel_id": (i, [vp, C.c_char_p, ip]),
+        "om_run": (i, [vp, i]),
+        "om_run_n": (i, [vp, i, i]),
+        "om_scalar_ptr": (i, [vp, C.c_char_p, C.POINTER(vp), ip]),
+        "om_array_host": (i, [vp, C.c_char_p, C.POINTER(vp), C.POINTER(C.c_size_t), ip]),
+        "om_array_host_const": (i, [vp, C.c_char_p, C.POINTER(vp), C.POINTER(C.c_size_t), ip]),
+        "om_array_device": (i, [vp, C.c_char_p, C.POINTER(vp)]),
+        "om_array_read": (i, [vp, C.c_char_p, vp, C.c_size_t]),
+        "om_array_write": (i, [vp, C.c_char_p, vp, C.c_size_t]),
+        "om_life_fill_random": (i, [vp, C.c_uint64, C.c_double]),
+        "om_life_population_history": (i, [vp, vp, i, ip]),
+        "om_hydro_init_kh": (i, [vp, C.c_uint64]),
+        "om_hydro_totals": (i, [vp, vp]),
+        "om_hydro_dt_history": (i, [vp, vp, i, ip]),
+        "om_time_run": (i, [vp, i, i, C.POINTER(C.c_float)]),
+        "om_last_launch_count": (i, [vp, ip]),
+        "om_profile_enable": (i, [vp, i]),
+        "om_profile_query": (i, [vp, C.c_char_p, C.POINTER(C.c_long), C.POINTER(C.c_double),
+                                 C.POINTER(C.c_double)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    if path is None:
+        _lib = L
+    return L
+
+
+def _check(status: int) -> None:
+    if status != OM_OK:
+        msg = load_library().om_last_error().decode(errors="replace")
+        raise OMError(status, msg)
+
+
+def default_config(**kw) -> Config:
+    cfg = Config()
+    load_library().om_config_default(C.byref(cfg))
+    for k, v in kw.items():
+        setattr(cfg, k, v)
+    return cfg
+
+
+class OrthotopeMachine:
+    """One generated OM class instance backed by a device handle."""
+
+    kind = 0
+    array_dtypes: dict[str, type] = {}
+
+    def __init__(self, size: tuple[int, int], config: Config | None = None, **kw):
+        L = load_library()
+        self._L = L
+        cfg = config if config is not None else default_config(**kw)
+        sizes = (C.c_int * 2)(int(size[0]), int(size[1]))
+        h = C.c_void_p()
+        _check(L.om_create(self.kind, 2, sizes, C.byref(cfg), C.byref(h)))
+        self._h = h
+        self.config = cfg
+        self._kid: dict[str, int] = {}
+
+    # -- lifetime
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.om_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- sizes (PlanTrans.hs:167-215)
+    def _q(self, fn, axis: int) -> int:
+        out = C.c_int()
+        _check(fn(self._h, axis, C.byref(out)))
+        return out.value
+
+    def om_size(self, axis: int = -1) -> int:
+        return self._q(self._L.om_size, axis)
+
+    def om_memory_size(self, axis: int = -1) -> int:
+        return self._q(self._L.om_memory_size, axis)
+
+    def om_lower_margin(self, axis: int) -> int:
+        return self._q(self._L.om_lower_margin, axis)
+
+    def om_upper_margin(self, axis: int) -> int:
+        return self._q(self._L.om_upper_margin, axis)
+
+    @property
+    def memory_shape(self) -> tuple[int, int]:
+        return (self.om_memory_size(1), self.om_memory_size(0))
+
+    # -- kernels (PlanTrans.hs:225-277)
+    def kernel_id(self, name: str) -> int:
+        if name not in self._kid:
+            out = C.c_int()
+            _check(self._L.om_kernel_id(self._h, name.encode(), C.byref(out)))
+            self._kid[name] = out.value
+        return self._kid[name]
+
+    def run(self, name: str, n: int = 1) -> None:
+        if n == 1:
+            _check(self._L.om_run(self._h, self.kernel_id(name)))
+        else:
+            _check(self._L.om_run_n(self._h, self.kernel_id(name), int(n)))
+
+    def time_run(self, name: str, n: int) -> float:
+        """Device time (ms, CUDA events on the handle's stream) of n steps."""
+        ms = C.c_float()
+        _check(self._L.om_time_run(self._h, self.kernel_id(name), int(n), C.byref(ms)))
+        return ms.value
+
+    def last_launch_count(self) -> int:
+        out = C.c_int()
+        _check(self._L.om_last_launch_count(self._h, C.byref(out)))
+        return out.value
+
+    def profile(self, enable: bool = True) -> None:
+        _check(self._L.om_profile_enable(self._h, int(enable)))
+
+    def profile_query(self, kernel: str) -> tuple[int, float, float]:
+        """(launches, total device ms, total cell-updates) of one kernel."""
+        n = C.c_long()
+        ms = C.c_double()
+        u = C.c_double()
+        _check(self._L.om_profile_query(self._h, kernel.encode(), C.byref(n), C.byref(ms), C.byref(u)))
+        return n.value, ms.value, u.value
+
+    # -- statics (PlanTrans.hs:117-157)
+    def _scalar(self, name: str):
+        p = C.c_void_p()
+        t = C.c_int()
+        _check(self._L.om_scalar_ptr(self._h, name.encode(), C.byref(p), C.byref(t)))
+        ctype = C.c_int32 if t.value == 0 else C.c_double
+        return C.cast(p, C.POINTER(ctype))
+
+    def get_scalar(self, name: str):
+        return self._scalar(name)[0]
+
+    def set_scalar(self, name: str, value) -> None:
+        self._scalar(name)[0] = value
+
+    def array(self, name: str) -> np.ndarray:
+        """Writable host mirror (memory-sized, [y, x]); marks the host newer."""
+        p = C.c_void_p()
+        n = C.c_size_t()
+        es = C.c_int()
+        _check(self._L.om_array_host(self._h, name.encode(), C.byref(p), C.byref(n), C.byref(es)))
+        dt = self.array_dtypes[name]
+        buf = (C.c_char * (n.value * es.value)).from_address(p.value)
+        return np.frombuffer(buf, dtype=dt).reshape(self.memory_shape)
+
+    def read(self, name: str) -> np.ndarray:
+        """Copy of an array (memory-sized, [y, x])."""
+        dt = self.array_dtypes[name]
+        out = np.empty(self.memory_shape, dtype=dt)
+        _check(self._L.om_array_read(self._h, name.encode(), out.ctypes.data, out.nbytes))
+        return out
+
+    def write(self, name: str, values: np.ndarray) -> None:
+        dt = self.array_dtypes[name]
+        a = np.ascontiguousarray(values, dtype=dt)
+        if a.shape != self.memory_shape:
+            raise ValueError(f"{name}: expected shape {self.memory_shape}, got {a.shape}")
+        _check(self._L.om_array_write(self._h, name.encode(), a.ctypes.data, a.nbytes))
+
+    def write_from_pointer(self, name: str, ptr: int, nbytes: int) -> None:
+        _check(self._L.om_array_write(self._h, name.encode(), C.c_void_p(ptr), nbytes))
+
+    def read_to_pointer(self, name: str, ptr: int, nbytes: int) -> None:
+        _check(self._L.om_array_read(self._h, name.encode(), C.c_void_p(ptr), nbytes))
+
+    def device_pointer(self, name: str) -> int:
+        p = C.c_void_p()
+        _check(self._L.om_array_device(self._h, name.encode(), C.byref(p)))
+        return p.value
+
+
+class Life(OrthotopeMachine):
+    """examples/Life: cell (Array Int), population, generation (Scalar Int)."""
+
+    kind = KIND_LIFE
+    array_dtypes = {"cell": np.int32}
+
+    def __init__(self, size=(80, 48), config: Config | None = None, **kw):
+        super().__init__(size, config, **kw)
+
+    def init(self) -> None:
+        self.run("init")
+
+    def proceed(self, n: int = 1) -> None:
+        self.run("proceed", n)
+
+    @property
+    def population(self) -> int:
+        return self.get_scalar("population")
+
+    @property
+    def generation(self) -> int:
+        return self.get_scalar("generation")
+
+    @generation.setter
+    def generation(self, v: int) -> None:
+        self.set_scalar("generation", v)
+
+    def fill_random(self, seed: int, p: float = 0.3) -> None:
+        _check(self._L.om_life_fill_random(self._h, C.c_uint64(seed), p))
+
+    def population_history(self, n: int) -> np.ndarray:
+        out = np.zeros(max(n, 1), np.int32)
+        w = C.c_int()
+        _check(self._L.om_life_population_history(self._h, out.ctypes.data, n, C.byref(w)))
+        return out[: w.value]
+
+
+class Hydro(OrthotopeMachine):
+    """examples/Hydro: density, velocity0, velocity1, pressure (Array Real);
+    generation (Int), time, cfl, dR0, dR1, extent0, extent1 (Scalar Real)."""
+
+    kind = KIND_HYDRO
+
+    def __init__(self, size=(1024, 1024), config: Config | None = None, **kw):
+        super().__init__(size, config, **kw)
+        dt = np.float64 if self.config.precision == 64 else np.float32
+        self.array_dtypes = {k: dt for k in ("density", "velocity0", "velocity1", "pressure")}
+
+    def init(self) -> None:
+        self.run("init")
+
+    def proceed(self, n: int = 1) -> None:
+        self.run("proceed", n)
+
+    def init_kh(self, seed: int) -> None:
+        _check(self._L.om_hydro_init_kh(self._h, C.c_uint64(seed)))
+
+    def totals(self) -> np.ndarray:
+        out = np.zeros(4, np.float64)
+        _check(self._L.om_hydro_totals(self._h, out.ctypes.data))
+        return out
+
+    def dt_history(self, n: int) -> np.ndarray:
+        out = np.zeros(max(n, 1), np.float64)
+        w = C.c_int()
+        _check(self._L.om_hydro_dt_history(self._h, out.ctypes.data, n, C.byref(w)))
+        return out[: w.value]
+
+    def state(self) -> tuple[np.ndarray, ...]:
+        return tuple(self.read(k) for k in ("density", "velocity0", "velocity1", "pressure"))
+
+    def set_state(self, st) -> None:
+        for k, v in zip(("density", "velocity0", "velocity1", "pressure"), st):
+            self.write(k, v)

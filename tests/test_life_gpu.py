@@ -1,0 +1,126 @@
+"""Life on the GPU through the C ABI, bit-exact against the oracle."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def run_gpu(pg, size, init, steps, **cfg):
+    life = pg.Life(size, **cfg)
+    life.write("cell", init)
+    life.proceed(steps)
+    cells = life.read("cell")
+    pops = life.population_history(steps)
+    out = (cells, pops, life.population, life.generation, life.last_launch_count())
+    life.close()
+    return out
+
+
+def test_life_128_bernoulli_1000(om_lib, oracle):
+    # the 128x128 cyclic, Bernoulli(0.3), 1000-generation workload
+    pg = om_lib
+    life = pg.Life((128, 128))
+    life.fill_random(1, 0.3)
+    init = life.read("cell")
+    assert np.array_equal(init, oracle.life_bernoulli(128, 128, 1, 0.3))
+    life.proceed(1000)
+    ref_cells, ref_pops = oracle.life_run(init, 1000, cyclic=True)
+    assert np.array_equal(life.read("cell"), ref_cells)
+    assert np.array_equal(life.population_history(1000), ref_pops)
+    assert life.population == ref_pops[-1]
+    assert life.generation == 1000
+    life.close()
+
+
+@pytest.mark.parametrize("size", [(37, 29), (1, 7), (5, 1), (80, 48), (33, 64), (130, 17)])
+def test_life_general_path_odd_sizes(om_lib, oracle, size):
+    init = oracle.life_bernoulli(size[0], size[1], 5, 0.35)
+    cells, pops, pop, gen, _ = run_gpu(om_lib, size, init, 25)
+    rc, rp = oracle.life_run(init, 25, cyclic=True)
+    assert np.array_equal(cells, rc)
+    assert np.array_equal(pops, rp)
+    assert pop == rp[-1] and gen == 25
+
+
+@pytest.mark.parametrize("size", [(128, 128), (96, 40), (200, 130)])
+def test_life_open_boundary(om_lib, oracle, size):
+    init = oracle.life_bernoulli(size[0], size[1], 9, 0.3, cyclic=False)
+    init[0, :] = 1   # margins written by the host are zeroed by the first step
+    cells, pops, pop, gen, _ = run_gpu(om_lib, size, init, 40, boundary=1)
+    rc, rp = oracle.life_run(init, 40, cyclic=False)
+    assert np.array_equal(cells, rc)
+    assert np.array_equal(pops, rp)
+
+
+@pytest.mark.parametrize("depth,tw,th", [(16, 0, 0), (1, 4, 8), (7, 3, 5), (32, 8, 64),
+                                         (32, 64, 128), (25, 16, 100)])
+def test_life_temporal_blocking_tiles(om_lib, oracle, depth, tw, th):
+    size = (1024, 640)
+    init = oracle.life_bernoulli(size[0], size[1], 11, 0.3)
+    cells, pops, pop, gen, launches = run_gpu(om_lib, size, init, 70, depth=depth,
+                                              tile_x=tw, tile_y=th)
+    rc, rp = oracle.life_run(init, 70, cyclic=True)
+    assert np.array_equal(cells, rc)
+    assert np.array_equal(pops, rp)
+    assert launches >= 2
+
+
+def test_life_nonbinary_first_step(om_lib, oracle):
+    init = oracle.life_bernoulli(256, 96, 2, 0.3)
+    init[10, 10] = 3
+    init[20, 30] = -1
+    init[50, 200] = 7
+    cells, pops, *_ = run_gpu(om_lib, (256, 96), init, 30)
+    rc, rp = oracle.life_run(init, 30, cyclic=True)
+    assert np.array_equal(cells, rc)
+    assert np.array_equal(pops, rp)
+
+
+def test_life_host_mirror_and_graph_replay(om_lib, oracle):
+    pg = om_lib
+    life = pg.Life((512, 256))
+    life.init()
+    assert life.population == 0 and life.generation == 0
+    m = life.array("cell")          # writable mirror: marks the host newer
+    glider = ((1, 0), (2, 1), (0, 2), (1, 2), (2, 2))
+    for x, y in glider:
+        m[y + 100, x + 100] = 1
+    ref = m.copy()
+    for rep in range(3):            # graph captured once, replayed twice
+        life.proceed(8)
+        ref, rp = oracle.life_run(ref, 8, cyclic=True)
+        assert np.array_equal(life.read("cell"), ref)
+        assert life.population == 5
+    assert life.generation == 24
+    # const reads do not disturb the device copy
+    life.proceed(1)
+    ref, _ = oracle.life_run(ref, 1, cyclic=True)
+    assert np.array_equal(life.read("cell"), ref)
+    life.close()
+
+
+def test_life_full_size_properties(om_lib, oracle):
+    # 16384x16384, Bernoulli(0.3): 20 generations against the oracle, and
+    # the temporally blocked path against the general integer path over 100
+    pg = om_lib
+    n = 16384
+    life = pg.Life((n, n))
+    life.fill_random(1, 0.3)
+    init = life.read("cell")
+    life.proceed(20)
+    rc, rp = oracle.life_run(init, 20, cyclic=True)
+    assert np.array_equal(life.population_history(20), rp)
+    assert np.array_equal(life.read("cell"), rc)
+    del rc
+    life.proceed(80)
+    tb_pops = life.population_history(80)
+    tb_cells = life.read("cell")
+    life.close()
+    # the same 100 generations on the integer one-cell-per-thread kernel
+    gen = pg.Life((n, n), variant=1)
+    gen.write("cell", init)
+    gen.proceed(100)
+    assert gen.last_launch_count() >= 100
+    assert np.array_equal(gen.population_history(100)[20:], tb_pops)
+    assert np.array_equal(gen.read("cell"), tb_cells)
+    gen.close()
