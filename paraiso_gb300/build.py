@@ -19,6 +19,12 @@ BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
+# Per-file flags.  hydro_exact.cu must round every operation as the
+# generated C++ does: no multiply-add contraction, IEEE division and sqrt.
+FILE_FLAGS = {
+    "hydro_exact.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"],
+    "hydro_fast.cu": ["-prec-div=true", "-prec-sqrt=true"],
+}
 
 
 def nvcc() -> str:
@@ -50,7 +56,8 @@ def build(verbose: bool = False, extra_flags: list[str] | None = None) -> str:
         obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
         objs.append(obj)
         if _stale(obj, [src] + headers + [__file__]):
-            jobs.append([nvcc(), *ARCH, *flags, "-c", src, "-o", obj])
+            jobs.append([nvcc(), *ARCH, *flags, *FILE_FLAGS.get(os.path.basename(src), []),
+                         "-c", src, "-o", obj])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -1,0 +1,363 @@
+// hydro_kernels.cuh -- Hydro step kernels, templated on the real type.
+// Included by hydro_exact.cu (no multiply-add contraction: bit-exact with
+// the generated code's arithmetic) and hydro_fast.cu (contraction allowed).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "hydro_scheme.cuh"
+
+namespace om {
+
+// Device scalar block of a Hydro handle.  The first fields are the OM's
+// statics (HydroMain.hs:44-53); the rest are runtime state.
+struct HydroScalars {
+  int32_t generation;
+  int32_t pad0;
+  double time, cfl, dR0, dR1, extent0, extent1;
+  // bit patterns (as unsigned long long of a positive double) of the CFL
+  // minimum of the current state, double-buffered by step parity
+  unsigned long long tsmin[2];
+  double dt_last;
+};
+
+struct HydroStepArgs {
+  const void *rho, *v0, *v1, *p;   // current state (memory-sized arrays)
+  void *nrho, *nv0, *nv1, *np;     // next state
+  int n0, n1;                      // grid (cyclic, no margins)
+  int nt0;                         // tiles along x
+  double gamma;
+  HydroScalars *sc;
+  int read_slot;                   // tsmin slot holding min of the current state
+  double *dt_hist;                 // dt of this step is written to dt_hist[0]
+};
+
+namespace hk {
+
+__device__ __forceinline__ unsigned long long ts_bits(double t) {
+  return (unsigned long long)__double_as_longlong(t);
+}
+
+template <class R> __device__ __forceinline__ R ts_from_bits(unsigned long long b) {
+  return (R)__longlong_as_double((long long)b);
+}
+
+// block-wide min of a positive double (as bits) folded into *dst
+__device__ __forceinline__ void block_min_to(unsigned long long v, unsigned long long *dst,
+                                             unsigned long long *red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w < v ? w : v;
+  }
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    v = lane < nw ? red[lane] : ~0ull;
+    for (int o = 16; o > 0; o >>= 1) {
+      unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+      v = w < v ? w : v;
+    }
+    if (lane == 0) atomicMin(dst, v);
+  }
+}
+
+template <class R>
+__device__ __forceinline__ int wrap(int i, int n) {
+  i %= n;
+  return i < 0 ? i + n : i;
+}
+
+// dt of this step in the OM's Real type: dtG = cfl * reduce Min dts
+template <class R> __device__ __forceinline__ R step_dt(const HydroStepArgs &a) {
+  const R tsmin = ts_from_bits<R>(a.sc->tsmin[a.read_slot]);
+  return (R)a.sc->cfl * tsmin;
+}
+
+}  // namespace hk
+
+// ---------------------------------------------------------------------------
+// CFL timescale minimum of a state (used when no fused step has produced it)
+// ---------------------------------------------------------------------------
+template <class R>
+__global__ void __launch_bounds__(256)
+hydro_tsmin_kernel(const R *__restrict__ rho, const R *__restrict__ v0,
+                   const R *__restrict__ v1, const R *__restrict__ p, size_t n,
+                   double gamma, HydroScalars *sc, int slot) {
+  __shared__ unsigned long long red[32];
+  const R g = (R)gamma, dR0 = (R)sc->dR0, dR1 = (R)sc->dR1;
+  unsigned long long m = ~0ull;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const R t = hs::timescale(g, dR0, dR1, rho[i], v0[i], v1[i], p[i]);
+    const unsigned long long b = hk::ts_bits((double)t);
+    m = b < m ? b : m;
+  }
+  hk::block_min_to(m, &sc->tsmin[slot], red);
+}
+
+// ---------------------------------------------------------------------------
+// Fused two-stage step on a TX x TY tile with a 3-cell cyclic halo.
+// Phases: load (with sound speeds) -> stage-1 walls (order 1, one HLLC per
+// face) -> stage-1 cells (dt/2) -> stage-2 walls (MUSCL + HLLC) -> stage-2
+// cells (dt), written out with the tile's CFL minimum of the new state.
+// ---------------------------------------------------------------------------
+template <class R, int TX, int TY> struct FusedSmem {
+  static constexpr int PX = TX + 6, PY = TY + 6;   // loaded cells
+  static constexpr int QX = TX + 4, QY = TY + 4;   // stage-1 cells
+  static constexpr int FXX = TX + 5, FXY = TY + 4; // stage-1 x walls
+  static constexpr int FYX = TX + 4, FYY = TY + 5; // stage-1 y walls
+  R P[4][PY][PX];
+  R C[PY][PX];
+  R Q[4][QY][QX];
+  hs::Flux<R> fx[FXY * FXX];
+  hs::Flux<R> fy[FYY * FYX];
+};
+
+template <class R, int TX, int TY, int NT>
+__global__ void __launch_bounds__(NT)
+hydro_fused_kernel(HydroStepArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  using S = FusedSmem<R, TX, TY>;
+  S &s = *reinterpret_cast<S *>(smem_raw);
+  __shared__ unsigned long long red[32];
+  const int tid = threadIdx.x;
+  const int t0 = blockIdx.x % a.nt0, t1 = blockIdx.x / a.nt0;
+  const int X0 = t0 * TX, Y0 = t1 * TY;
+  const int n0 = a.n0, n1 = a.n1;
+  const R g = (R)a.gamma;
+  const R dR0 = (R)a.sc->dR0, dR1 = (R)a.sc->dR1;
+  const R dtG = hk::step_dt<R>(a);
+  const R dtHalf = dtG / R(2);
+  const R *rho = (const R *)a.rho, *vx = (const R *)a.v0, *vy = (const R *)a.v1,
+          *pr = (const R *)a.p;
+
+  // phase 0: load primitives and sound speeds
+  for (int i = tid; i < S::PY * S::PX; i += NT) {
+    const int py = i / S::PX, px = i - py * S::PX;
+    const int gy = hk::wrap<R>(Y0 + py - 3, n1), gx = hk::wrap<R>(X0 + px - 3, n0);
+    const size_t gi = (size_t)gy * n0 + gx;
+    const R r = rho[gi], u = vx[gi], v = vy[gi], q = pr[gi];
+    s.P[0][py][px] = r;
+    s.P[1][py][px] = u;
+    s.P[2][py][px] = v;
+    s.P[3][py][px] = q;
+    s.C[py][px] = hs::sound(g, r, q);
+  }
+  __syncthreads();
+
+  // phase 1: stage-1 walls, order-1 reconstruction (L = cell left, R = cell)
+  {
+    constexpr int NX = S::FXY * S::FXX, NY = S::FYY * S::FYX;
+    for (int i = tid; i < NX + NY; i += NT) {
+      if (i < NX) {
+        const int fy = i / S::FXX, fx = i - fy * S::FXX;
+        const int py = fy + 1;
+        const hs::Prim<R> L{s.P[0][py][fx], s.P[1][py][fx], s.P[2][py][fx], s.P[3][py][fx]};
+        const hs::Prim<R> Rt{s.P[0][py][fx + 1], s.P[1][py][fx + 1], s.P[2][py][fx + 1],
+                             s.P[3][py][fx + 1]};
+        s.fx[i] = hs::hllc<0>(g, L, s.C[py][fx], Rt, s.C[py][fx + 1]);
+      } else {
+        const int j = i - NX;
+        const int fy = j / S::FYX, fx = j - fy * S::FYX;
+        const int px = fx + 1;
+        const hs::Prim<R> L{s.P[0][fy][px], s.P[1][fy][px], s.P[2][fy][px], s.P[3][fy][px]};
+        const hs::Prim<R> Rt{s.P[0][fy + 1][px], s.P[1][fy + 1][px], s.P[2][fy + 1][px],
+                             s.P[3][fy + 1][px]};
+        s.fy[j] = hs::hllc<1>(g, L, s.C[fy][px], Rt, s.C[fy + 1][px]);
+      }
+    }
+  }
+  __syncthreads();
+
+  // phase 2: stage-1 cells
+  {
+    const R dtdx0 = dtHalf / dR0, dtdx1 = dtHalf / dR1;
+    for (int i = tid; i < S::QY * S::QX; i += NT) {
+      const int qy = i / S::QX, qx = i - qy * S::QX;
+      const int py = qy + 1, px = qx + 1;
+      const hs::Prim<R> b{s.P[0][py][px], s.P[1][py][px], s.P[2][py][px], s.P[3][py][px]};
+      const hs::Prim<R> q = hs::update(g, b, dtdx0, dtdx1, s.fx[qy * S::FXX + qx],
+                                       s.fx[qy * S::FXX + qx + 1], s.fy[qy * S::FYX + qx],
+                                       s.fy[(qy + 1) * S::FYX + qx]);
+      s.Q[0][qy][qx] = q.rho;
+      s.Q[1][qy][qx] = q.v0;
+      s.Q[2][qy][qx] = q.v1;
+      s.Q[3][qy][qx] = q.p;
+    }
+  }
+  __syncthreads();
+
+  // phase 3: stage-2 walls with MUSCL-minmod reconstruction of stage-1 cells
+  {
+    constexpr int NX = TY * (TX + 1), NY = (TY + 1) * TX;
+    for (int i = tid; i < NX + NY; i += NT) {
+      hs::Prim<R> L, Rt;
+      if (i < NX) {
+        const int sy = i / (TX + 1), sx = i - sy * (TX + 1);
+        const int qy = sy + 2;
+#pragma unroll
+        for (int f = 0; f < 4; ++f) {
+          R l, r;
+          hs::muscl(s.Q[f][qy][sx], s.Q[f][qy][sx + 1], s.Q[f][qy][sx + 2], s.Q[f][qy][sx + 3],
+                    l, r);
+          (&L.rho)[f] = l;
+          (&Rt.rho)[f] = r;
+        }
+        s.fx[i] = hs::hllc<0>(g, L, hs::sound(g, L.rho, L.p), Rt, hs::sound(g, Rt.rho, Rt.p));
+      } else {
+        const int j = i - NX;
+        const int sy = j / TX, sx = j - sy * TX;
+        const int qx = sx + 2;
+#pragma unroll
+        for (int f = 0; f < 4; ++f) {
+          R l, r;
+          hs::muscl(s.Q[f][sy][qx], s.Q[f][sy + 1][qx], s.Q[f][sy + 2][qx], s.Q[f][sy + 3][qx],
+                    l, r);
+          (&L.rho)[f] = l;
+          (&Rt.rho)[f] = r;
+        }
+        s.fy[j] = hs::hllc<1>(g, L, hs::sound(g, L.rho, L.p), Rt, hs::sound(g, Rt.rho, Rt.p));
+      }
+    }
+  }
+  __syncthreads();
+
+  // phase 4: stage-2 cells, written out, with the CFL minimum of the new state
+  unsigned long long m = ~0ull;
+  {
+    const R dtdx0 = dtG / dR0, dtdx1 = dtG / dR1;
+    R *orho = (R *)a.nrho, *ovx = (R *)a.nv0, *ovy = (R *)a.nv1, *opr = (R *)a.np;
+    for (int i = tid; i < TY * TX; i += NT) {
+      const int oy = i / TX, ox = i - oy * TX;
+      const int gy = Y0 + oy, gx = X0 + ox;
+      if (gy >= n1 || gx >= n0) continue;
+      const int py = oy + 3, px = ox + 3;
+      const hs::Prim<R> b{s.P[0][py][px], s.P[1][py][px], s.P[2][py][px], s.P[3][py][px]};
+      const hs::Prim<R> q =
+          hs::update(g, b, dtdx0, dtdx1, s.fx[oy * (TX + 1) + ox], s.fx[oy * (TX + 1) + ox + 1],
+                     s.fy[oy * TX + ox], s.fy[(oy + 1) * TX + ox]);
+      const size_t gi = (size_t)gy * n0 + gx;
+      orho[gi] = q.rho;
+      ovx[gi] = q.v0;
+      ovy[gi] = q.v1;
+      opr[gi] = q.p;
+      const R t = hs::timescale(g, dR0, dR1, q.rho, q.v0, q.v1, q.p);
+      const unsigned long long bits = hk::ts_bits((double)t);
+      m = bits < m ? bits : m;
+    }
+  }
+  hk::block_min_to(m, &a.sc->tsmin[1 - a.read_slot], red);
+  if (blockIdx.x == 0 && tid == 0) {
+    a.dt_hist[0] = (double)dtG;
+    a.sc->dt_last = (double)dtG;
+    a.sc->time = a.sc->time + (double)dtG;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Plain path: the structure of the generated code.  One thread per cell,
+// every Delayed value recomputed from the four primitive arrays in global
+// memory (as Hydro_sub_8 does), grid-stride loops, separate timescale and
+// reduce passes, and copies of the manifests back into the statics.
+// ---------------------------------------------------------------------------
+template <class R>
+__global__ void __launch_bounds__(256)
+hydro_plain_timescale_kernel(const R *__restrict__ rho, const R *__restrict__ v0,
+                             const R *__restrict__ v1, const R *__restrict__ p,
+                             R *__restrict__ ts, size_t n, double gamma,
+                             const HydroScalars *sc) {
+  const R g = (R)gamma, dR0 = (R)sc->dR0, dR1 = (R)sc->dR1;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    ts[i] = hs::timescale(g, dR0, dR1, rho[i], v0[i], v1[i], p[i]);
+}
+
+template <class R>
+__global__ void __launch_bounds__(256)
+hydro_plain_reduce_min_kernel(const R *__restrict__ ts, size_t n, unsigned long long *out) {
+  __shared__ unsigned long long red[32];
+  unsigned long long m = ~0ull;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const unsigned long long b = hk::ts_bits((double)ts[i]);
+    m = b < m ? b : m;
+  }
+  hk::block_min_to(m, out, red);
+}
+
+template <class R> struct PlainView {
+  const R *rho, *v0, *v1, *p;
+  int n0, n1;
+  __device__ __forceinline__ hs::Prim<R> at(int x, int y) const {
+    x = hk::wrap<R>(x, n0);
+    y = hk::wrap<R>(y, n1);
+    const size_t i = (size_t)y * n0 + x;
+    return hs::Prim<R>{rho[i], v0[i], v1[i], p[i]};
+  }
+};
+
+// stage-1 state at (x, y): order-1 walls recomputed from the primitives
+template <class R>
+__device__ __forceinline__ hs::Prim<R> plain_stage1(const PlainView<R> &V, R g, R dtdx0, R dtdx1,
+                                                    int x, int y) {
+  const hs::Prim<R> c = V.at(x, y), xm = V.at(x - 1, y), xp = V.at(x + 1, y),
+                    ym = V.at(x, y - 1), yp = V.at(x, y + 1);
+  const R cc = hs::sound(g, c.rho, c.p);
+  const hs::Flux<R> l0 = hs::hllc<0>(g, xm, hs::sound(g, xm.rho, xm.p), c, cc);
+  const hs::Flux<R> r0 = hs::hllc<0>(g, c, cc, xp, hs::sound(g, xp.rho, xp.p));
+  const hs::Flux<R> l1 = hs::hllc<1>(g, ym, hs::sound(g, ym.rho, ym.p), c, cc);
+  const hs::Flux<R> r1 = hs::hllc<1>(g, c, cc, yp, hs::sound(g, yp.rho, yp.p));
+  return hs::update(g, c, dtdx0, dtdx1, l0, r0, l1, r1);
+}
+
+template <int AX, class R>
+__device__ __forceinline__ hs::Flux<R> plain_wall2(const hs::Prim<R> &a0, const hs::Prim<R> &a1,
+                                                   const hs::Prim<R> &a2, const hs::Prim<R> &a3,
+                                                   R g) {
+  hs::Prim<R> L, Rt;
+  hs::muscl(a0.rho, a1.rho, a2.rho, a3.rho, L.rho, Rt.rho);
+  hs::muscl(a0.v0, a1.v0, a2.v0, a3.v0, L.v0, Rt.v0);
+  hs::muscl(a0.v1, a1.v1, a2.v1, a3.v1, L.v1, Rt.v1);
+  hs::muscl(a0.p, a1.p, a2.p, a3.p, L.p, Rt.p);
+  return hs::hllc<AX>(g, L, hs::sound(g, L.rho, L.p), Rt, hs::sound(g, Rt.rho, Rt.p));
+}
+
+template <class R>
+__global__ void __launch_bounds__(128)
+hydro_plain_step_kernel(PlainView<R> V, R *__restrict__ orho, R *__restrict__ ov0,
+                        R *__restrict__ ov1, R *__restrict__ op, double gamma, R dtG, R dR0,
+                        R dR1) {
+  const R g = (R)gamma;
+  const R dtHalf = dtG / R(2);
+  const R h0 = dtHalf / dR0, h1 = dtHalf / dR1;
+  const R f0 = dtG / dR0, f1 = dtG / dR1;
+  const size_t n = (size_t)V.n0 * V.n1;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int y = (int)(i / V.n0), x = (int)(i - (size_t)y * V.n0);
+    // stage-1 cells along the two axes (Delayed: recomputed here)
+    const hs::Prim<R> qm2 = plain_stage1(V, g, h0, h1, x - 2, y);
+    const hs::Prim<R> qm1 = plain_stage1(V, g, h0, h1, x - 1, y);
+    const hs::Prim<R> q00 = plain_stage1(V, g, h0, h1, x, y);
+    const hs::Prim<R> qp1 = plain_stage1(V, g, h0, h1, x + 1, y);
+    const hs::Prim<R> qp2 = plain_stage1(V, g, h0, h1, x + 2, y);
+    const hs::Flux<R> l0 = plain_wall2<0>(qm2, qm1, q00, qp1, g);
+    const hs::Flux<R> r0 = plain_wall2<0>(qm1, q00, qp1, qp2, g);
+    const hs::Prim<R> ym2 = plain_stage1(V, g, h0, h1, x, y - 2);
+    const hs::Prim<R> ym1 = plain_stage1(V, g, h0, h1, x, y - 1);
+    const hs::Prim<R> yp1 = plain_stage1(V, g, h0, h1, x, y + 1);
+    const hs::Prim<R> yp2 = plain_stage1(V, g, h0, h1, x, y + 2);
+    const hs::Flux<R> l1 = plain_wall2<1>(ym2, ym1, q00, yp1, g);
+    const hs::Flux<R> r1 = plain_wall2<1>(ym1, q00, yp1, yp2, g);
+    const hs::Prim<R> q = hs::update(g, V.at(x, y), f0, f1, l0, r0, l1, r1);
+    orho[i] = q.rho;
+    ov0[i] = q.v0;
+    ov1[i] = q.v1;
+    op[i] = q.p;
+  }
+}
+
+}  // namespace om

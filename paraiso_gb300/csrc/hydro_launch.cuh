@@ -1,0 +1,49 @@
+// hydro_launch.cuh -- host-side launchers of the Hydro kernels, declared for
+// hydro.cu and defined in the translation units that compile the kernels
+// (hydro_exact.cu without multiply-add contraction, hydro_fast.cu with it).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "hydro_kernels.cuh"
+
+namespace om {
+
+// Tile shapes of the fused kernel available to the tuner.
+enum HydroTile { kTile32x8 = 0, kTile32x16 = 1, kTile64x16 = 2, kTileCount = 3 };
+void hydro_tile_dims(int tile, int *tx, int *ty);
+
+// fused two-stage step; `exact` selects the no-contraction build
+cudaError_t hydro_fused_f32(const HydroStepArgs &a, int tile, bool exact, cudaStream_t s,
+                            int *grid_out);
+cudaError_t hydro_fused_f64(const HydroStepArgs &a, int tile, cudaStream_t s, int *grid_out);
+
+// CFL minimum of a state into sc->tsmin[slot] (slot pre-set to all ones)
+cudaError_t hydro_tsmin(int fp64, const void *rho, const void *v0, const void *v1,
+                        const void *p, size_t n, double gamma, HydroScalars *sc, int slot,
+                        int grid, cudaStream_t s);
+
+// plain path pieces
+cudaError_t hydro_plain_timescale(int fp64, const void *rho, const void *v0, const void *v1,
+                                  const void *p, void *ts, size_t n, double gamma,
+                                  const HydroScalars *sc, int grid, cudaStream_t s);
+cudaError_t hydro_plain_reduce_min(int fp64, const void *ts, size_t n, unsigned long long *out,
+                                   int grid, cudaStream_t s);
+cudaError_t hydro_plain_step(int fp64, const void *rho, const void *v0, const void *v1,
+                             const void *p, void *orho, void *ov0, void *ov1, void *op, int n0,
+                             int n1, double gamma, double dtG, double dR0, double dR1, int grid,
+                             cudaStream_t s);
+cudaError_t hydro_scalar_advance(HydroScalars *sc, double dt, double *dt_hist, cudaStream_t s);
+
+// initial states
+cudaError_t hydro_init_jet(int fp64, void *rho, void *v0, void *v1, void *p, int n0, int n1,
+                           double gamma, const HydroScalars *sc, cudaStream_t s);
+cudaError_t hydro_init_kh(int fp64, void *rho, void *v0, void *v1, void *p, int n0, int n1,
+                          unsigned long long seed_mix, cudaStream_t s);
+
+// compensated FP64 totals: partials[blocks][8], then out[4] (device)
+cudaError_t hydro_totals(int fp64, const void *rho, const void *v0, const void *v1,
+                         const void *p, size_t n, double gamma, double *partials, int blocks,
+                         double *out, cudaStream_t s);
+
+}  // namespace om

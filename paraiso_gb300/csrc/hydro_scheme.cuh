@@ -1,0 +1,160 @@
+// hydro_scheme.cuh -- the examples/Hydro finite-volume scheme as device
+// functions, one C operation per OM Arith node in the builder's order, so a
+// translation unit compiled without multiply-add contraction reproduces the
+// generated code's rounding exactly.
+//
+// Reference: examples/Hydro/Hydro.hs:37-127 (primitive <-> conserved algebra,
+// fluxes, sound speed), examples/Hydro/HydroMain.hs:134-276 (proceed,
+// proceedSingle, addFlux, interpolate, hllc).  std::max / std::min follow
+// the generated C++ (Language/Paraiso/Generator/PlanTrans.hs:692-693).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace om {
+namespace hs {
+
+template <class R> __device__ __forceinline__ R omax(R a, R b) { return (a < b) ? b : a; }
+template <class R> __device__ __forceinline__ R omin(R a, R b) { return (b < a) ? b : a; }
+
+template <class R> struct Prim { R rho, v0, v1, p; };
+template <class R> struct Flux { R fd, fm0, fm1, fe; };
+
+// kineticEnergy x = 0.5 * contract (\i -> velocity x !i * momentum x !i)
+template <class R> __device__ __forceinline__ R kinetic(R v0, R v1, R m0, R m1) {
+  return R(0.5) * ((R(0) + v0 * m0) + v1 * m1);
+}
+
+// energy of a primitive record: Ek + 1/(gamma-1) * p
+template <class R> __device__ __forceinline__ R energy_prim(R g, R rho, R v0, R v1, R p) {
+  const R m0 = rho * v0, m1 = rho * v1;
+  return kinetic(v0, v1, m0, m1) + (R(1) / (g - R(1))) * p;
+}
+
+// fluxes along axis AX of a primitive record
+template <int AX, class R>
+__device__ __forceinline__ Flux<R> flux_prim(R g, R rho, R v0, R v1, R p) {
+  const R m0 = rho * v0, m1 = rho * v1;
+  const R e = kinetic(v0, v1, m0, m1) + (R(1) / (g - R(1))) * p;
+  const R h = e + p;
+  const R va = AX == 0 ? v0 : v1;
+  Flux<R> f;
+  f.fd = AX == 0 ? m0 : m1;
+  f.fm0 = m0 * va + p * (AX == 0 ? R(1) : R(0));
+  f.fm1 = m1 * va + p * (AX == 1 ? R(1) : R(0));
+  f.fe = h * va;
+  return f;
+}
+
+// fluxes along AX of a conserved record (velocity m/rho, p = (g-1)(E-Ek))
+template <int AX, class R>
+__device__ __forceinline__ Flux<R> flux_cons(R g, R rho, R m0, R m1, R e) {
+  const R v0 = m0 / rho, v1 = m1 / rho;
+  const R p = (g - R(1)) * (e - kinetic(v0, v1, m0, m1));
+  const R h = e + p;
+  const R va = AX == 0 ? v0 : v1;
+  Flux<R> f;
+  f.fd = AX == 0 ? m0 : m1;
+  f.fm0 = m0 * va + p * (AX == 0 ? R(1) : R(0));
+  f.fm1 = m1 * va + p * (AX == 1 ? R(1) : R(0));
+  f.fe = h * va;
+  return f;
+}
+
+// soundSpeed' dens pres = sqrt (kGamma * pres / dens)
+template <class R> __device__ __forceinline__ R sound(R g, R rho, R p) {
+  return sqrt((g * p) / rho);
+}
+
+// hllcQ sp p, condition as written in HydroMain.hs
+template <class R> __device__ __forceinline__ R hllc_q(R g, R sp, R p) {
+  const R t = sqrt(R(1) + (g + R(1)) / (R(2) * g) * (sp / p - R(1)));
+  return (p <= sp) ? R(1) : t;
+}
+
+template <int AX, class R>
+__device__ __forceinline__ Flux<R> star_flux(R g, R sstar, R shock, R rho, R v0, R v1,
+                                             R p) {
+  const R speed = AX == 0 ? v0 : v1;
+  const R dens = rho * (shock - speed) / (shock - sstar);
+  const R mome0 = dens * (AX == 0 ? sstar : v0);
+  const R mome1 = dens * (AX == 1 ? sstar : v1);
+  const R e = energy_prim(g, rho, v0, v1, p);
+  const R enrg = dens * (e / rho + (sstar - speed) * (sstar + p / rho / (shock - speed)));
+  return flux_cons<AX>(g, dens, mome0, mome1, enrg);
+}
+
+// The wall record's fluxes of hllc i left right (HydroMain.hs:237-268).
+// cl, cr: sound speeds of the two states.
+template <int AX, class R>
+__device__ __forceinline__ Flux<R> hllc(R g, const Prim<R> &L, R cl, const Prim<R> &Rt,
+                                        R cr) {
+  const R densMid = (L.rho + Rt.rho) / R(2);
+  const R soundMid = (cl + cr) / R(2);
+  const R uL = AX == 0 ? L.v0 : L.v1;
+  const R uR = AX == 0 ? Rt.v0 : Rt.v1;
+  const R presStar = omax(R(0), (L.p + Rt.p) / R(2) - densMid * soundMid * (uR - uL));
+  const R shockLeft = uL - cl * hllc_q(g, presStar, L.p);
+  const R shockRight = uR + cr * hllc_q(g, presStar, Rt.p);
+  const R shockStar = (Rt.p - L.p + L.rho * uL * (shockLeft - uL) -
+                       Rt.rho * uR * (shockRight - uR)) /
+                      (L.rho * (shockLeft - uL) - Rt.rho * (shockRight - uR));
+  if (R(0) < shockLeft) return flux_prim<AX>(g, L.rho, L.v0, L.v1, L.p);
+  if (R(0) < shockStar) return star_flux<AX>(g, shockStar, shockLeft, L.rho, L.v0, L.v1, L.p);
+  if (R(0) < shockRight)
+    return star_flux<AX>(g, shockStar, shockRight, Rt.rho, Rt.v0, Rt.v1, Rt.p);
+  return flux_prim<AX>(g, Rt.rho, Rt.v0, Rt.v1, Rt.p);
+}
+
+template <class R> __device__ __forceinline__ R absmaller(R a, R b) {
+  return (a * b <= R(0)) ? R(0) : ((fabs(a) < fabs(b)) ? a : b);
+}
+
+// interpolateSingle 2 (minmod MUSCL): face value left (l) and right (r)
+template <class R>
+__device__ __forceinline__ void muscl(R x0, R x1, R x2, R x3, R &l, R &r) {
+  const R d01 = x1 - x0, d12 = x2 - x1, d23 = x3 - x2;
+  const R d1 = absmaller(d01, d12);
+  const R d2 = absmaller(d12, d23);
+  l = x1 + d1 / R(2);
+  r = x2 - d2 / R(2);
+}
+
+// Conservative update of base state b by the axis-1 walls, then the axis-0
+// walls (foldl1 (.) over the axes applies axis 1 first), then
+// bindPrimitive (max 1e-2 rho) v (max 1e-2 p).
+template <class R>
+__device__ __forceinline__ Prim<R> update(R g, const Prim<R> &b, R dtdx0, R dtdx1,
+                                          const Flux<R> &l0, const Flux<R> &r0,
+                                          const Flux<R> &l1, const Flux<R> &r1) {
+  const R m0 = b.rho * b.v0, m1 = b.rho * b.v1;
+  const R e = kinetic(b.v0, b.v1, m0, m1) + (R(1) / (g - R(1))) * b.p;
+  const R d1 = b.rho + dtdx1 * (l1.fd - r1.fd);
+  const R a0 = m0 + dtdx1 * (l1.fm0 - r1.fm0);
+  const R a1 = m1 + dtdx1 * (l1.fm1 - r1.fm1);
+  const R e1 = e + dtdx1 * (l1.fe - r1.fe);
+  const R d2 = d1 + dtdx0 * (l0.fd - r0.fd);
+  const R b0 = a0 + dtdx0 * (l0.fm0 - r0.fm0);
+  const R b1 = a1 + dtdx0 * (l0.fm1 - r0.fm1);
+  const R e2 = e1 + dtdx0 * (l0.fe - r0.fe);
+  const R v0 = b0 / d2, v1 = b1 / d2;
+  const R pn = (g - R(1)) * (e2 - kinetic(v0, v1, b0, b1));
+  Prim<R> q;
+  q.rho = omax(R(1e-2), d2);
+  q.v0 = v0;
+  q.v1 = v1;
+  q.p = omax(R(1e-2), pn);
+  return q;
+}
+
+// per-cell CFL timescale min_i dR_i / (c + |v_i|)   (HydroMain.hs:150-153)
+template <class R>
+__device__ __forceinline__ R timescale(R g, R dR0, R dR1, R rho, R v0, R v1, R p) {
+  const R c = sound(g, rho, p);
+  const R t0 = dR0 / (c + fabs(v0));
+  const R t1 = dR1 / (c + fabs(v1));
+  return omin(t0, t1);
+}
+
+}  // namespace hs
+}  // namespace om

@@ -356,7 +356,8 @@ om_status om_run_n(om_handle H, int kernel_id, int n) {
   if (n == 0) return OM_OK;
   if (h->ops.reserve) OM_TRY(h->ops.reserve(h, kernel_id, n));
   OM_TRY(prepare(h));
-  const bool graph_ok = h->cfg.use_graph && n > 1 && !h->profiling;
+  const bool graph_ok = h->cfg.use_graph && n > 1 && !h->profiling &&
+                        (!h->ops.graph_ok || h->ops.graph_ok(h, kernel_id));
   if (!graph_ok) {
     OM_TRY(run_plain(H, kernel_id, n));
     return finish(h);

@@ -73,6 +73,8 @@ struct KindOps {
   void (*array_written)(Handle *, Array *) = nullptr;
   // allocate whatever a run of n steps needs, before any stream capture
   om_status (*reserve)(Handle *, int kernel_id, int n) = nullptr;
+  // false when a kernel synchronises with the host mid-run (no graph capture)
+  bool (*graph_ok)(Handle *, int kernel_id) = nullptr;
 };
 
 struct Kernel {
