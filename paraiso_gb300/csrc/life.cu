@@ -454,6 +454,27 @@ static void life_free(Handle *h) {
   h->impl = nullptr;
 }
 
+// One launch of the temporally blocked tile kernel from `cur` into `next`
+// (cyclic, width % 32 == 0, 1 <= gens <= 32, cells 0/1), with the default
+// 32-word x 64-row tiles.  Allocates nothing; used by the caller-buffer
+// entry point in life_noalloc.cu.
+cudaError_t life_tb_launch_into(const int32_t *cur, int32_t *next, int n0, int n1, int gens,
+                                uint32_t *pop, cudaStream_t s) {
+  TbParams p;
+  p.n0 = n0; p.n1 = n1; p.wd = n0 / 32;
+  p.kk = gens;
+  p.tw = std::min(32, p.wd);
+  p.th = std::min(64, n1);
+  p.nt0 = (p.wd + p.tw - 1) / p.tw;
+  p.nt1 = (p.n1 + p.th - 1) / p.th;
+  const size_t smem = tb_smem_bytes(p);
+  cudaError_t e = cudaFuncSetAttribute(life_tb_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  life_tb_kernel<<<p.nt0 * p.nt1, 256, smem, s>>>(cur, next, p, pop);
+  return cudaGetLastError();
+}
+
 om_status life_setup(Handle *h) {
   const int lm = h->cyclic ? 0 : 1;  // stencil radius 1 (OMTrans.hs:103-116)
   for (int ax = 0; ax < 2; ++ax) {
