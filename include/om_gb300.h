@@ -65,7 +65,8 @@ typedef struct {
   int use_graph;    /* capture om_run_n in a CUDA graph (default 1) */
   int variant;      /* 0 = fastest path.  Life 1: integer one-cell-per-thread kernel only.
                        Hydro 1: plain unfused FP64-structured grid-stride kernels */
-  int reserved[7];
+  int life_io;      /* Life cell I/O of the packed kernels: 0 = 128-bit, 1 = 32-bit */
+  int reserved[6];
 } om_config;
 
 /* Fill `cfg` with defaults: cyclic, FP32, gamma 5/3, device 0, tuned tiles. */

@@ -122,36 +122,99 @@ life_general_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next,
   }
 }
 
-// Load `count` packed words into shared memory: word i of the tile is
-// row r = i / nc, column c = i % nc, global row wrap(row0 + r) and global
-// word wrap(col0 + c).  One warp per word: 32 coalesced int32 loads folded
-// into a word by a ballot.  8 words in flight per warp.
-__device__ __forceinline__ void pack_words(const int32_t *__restrict__ cur, int n0,
-                                           int n1, int wd, int row0, int col0,
-                                           int nc, int count, uint32_t *dst,
-                                           int warp, int nwarps, int lane) {
-  for (int base = warp * 8; base < count; base += nwarps * 8) {
-    int32_t v[8];
+// Load an nr x nc block of packed words into shared memory (row stride nc):
+// block row r is global row wrap(row0 + r), block column c is global word
+// wrap(col0 + c).  One warp per row at a time; each word is 32 coalesced
+// int32 loads folded by a ballot, 8 words in flight per warp.  Row and
+// word indices advance incrementally (no division per word).
+__device__ __forceinline__ void pack_rows(const int32_t *__restrict__ cur, int n0, int n1,
+                                          int wd, int row0, int col0, int nc, int nr,
+                                          uint32_t *dst, int warp, int nwarps, int lane) {
+  int gx0 = col0 % wd;
+  if (gx0 < 0) gx0 += wd;
+  const bool narrow = nc > wd;  // tiny grids: a tile row wraps more than once
+  for (int r = warp; r < nr; r += nwarps) {
+    int gy = (row0 + r) % n1;
+    if (gy < 0) gy += n1;
+    const int32_t *row = cur + (size_t)gy * n0 + lane;
+    uint32_t *out = dst + r * nc;
+    for (int c0 = 0; c0 < nc; c0 += 8) {
+      int32_t v[8];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const int i = base + j;
-      v[j] = 0;
-      if (i < count) {
-        const int r = i / nc, c = i - (i / nc) * nc;
-        int gy = (row0 + r) % n1;
-        if (gy < 0) gy += n1;
-        int gx = (col0 + c) % wd;
-        if (gx < 0) gx += wd;
-        v[j] = __ldg(cur + (size_t)gy * n0 + (size_t)gx * 32 + lane);
+      for (int j = 0; j < 8; ++j) {
+        const int c = c0 + j;
+        v[j] = 0;
+        if (c < nc) {
+          int gx = gx0 + c;
+          if (narrow) gx %= wd;
+          else if (gx >= wd) gx -= wd;
+          v[j] = __ldg(row + (size_t)gx * 32);
+        }
+      }
+      uint32_t mine = 0;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const uint32_t w = __ballot_sync(0xffffffffu, v[j] != 0);
+        if (lane == j) mine = w;
+      }
+      if (lane < 8 && c0 + lane < nc) out[c0 + lane] = mine;
+    }
+  }
+}
+
+// Bit t of an 8-bit value moved to bit 4t.
+__device__ __forceinline__ uint32_t spread4(uint32_t x) {
+  x = (x | (x << 12)) & 0x000F000Fu;
+  x = (x | (x << 6)) & 0x03030303u;
+  x = (x | (x << 3)) & 0x11111111u;
+  return x;
+}
+
+// pack_rows with 128-bit cell loads: lane L reads cells 4(L%8)..4(L%8)+3 of
+// word L/8 of a 4-word group, so one warp instruction moves 512 bytes.
+// Ballot j holds cell 4t+j of word m at bit 8m+t; word m is the four bytes
+// m of the ballots interleaved.  G groups (4G words, G x 512 bytes) in
+// flight per warp.
+template <int G>
+__device__ __forceinline__ void pack_rows_vec(const int32_t *__restrict__ cur, int n0, int n1,
+                                              int wd, int row0, int col0, int nc, int nr,
+                                              uint32_t *dst, int warp, int nwarps, int lane) {
+  int gx0 = col0 % wd;
+  if (gx0 < 0) gx0 += wd;
+  const bool narrow = nc > wd;
+  const int sub = lane >> 3, quad = (lane & 7) * 4;
+  for (int r = warp; r < nr; r += nwarps) {
+    int gy = (row0 + r) % n1;
+    if (gy < 0) gy += n1;
+    const int32_t *row = cur + (size_t)gy * n0 + quad;
+    uint32_t *out = dst + r * nc;
+    for (int c0 = 0; c0 < nc; c0 += 4 * G) {
+      int4 v[G];
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        const int cw = c0 + 4 * g + sub;
+        v[g] = make_int4(0, 0, 0, 0);
+        if (cw < nc) {
+          int gx = gx0 + cw;
+          if (narrow) gx %= wd;
+          else if (gx >= wd) gx -= wd;
+          v[g] = __ldg(reinterpret_cast<const int4 *>(row + (size_t)gx * 32));
+        }
+      }
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        const uint32_t b0 = __ballot_sync(0xffffffffu, v[g].x != 0);
+        const uint32_t b1 = __ballot_sync(0xffffffffu, v[g].y != 0);
+        const uint32_t b2 = __ballot_sync(0xffffffffu, v[g].z != 0);
+        const uint32_t b3 = __ballot_sync(0xffffffffu, v[g].w != 0);
+        const int cw = c0 + 4 * g + lane;
+        if (lane < 4 && cw < nc) {
+          const int sh = 8 * lane;
+          out[cw] = spread4((b0 >> sh) & 0xFFu) | (spread4((b1 >> sh) & 0xFFu) << 1) |
+                    (spread4((b2 >> sh) & 0xFFu) << 2) | (spread4((b3 >> sh) & 0xFFu) << 3);
+        }
       }
     }
-    uint32_t mine = 0;
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const uint32_t w = __ballot_sync(0xffffffffu, v[j] != 0);
-      if (lane == j) mine = w;
-    }
-    if (lane < 8 && base + lane < count) dst[base + lane] = mine;
   }
 }
 
@@ -166,7 +229,7 @@ life_smallgrid_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ nex
   uint32_t *A = sm, *B = sm + nw;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nthreads = blockDim.x, nwarps = nthreads >> 5;
-  pack_words(cur, n0, n1, wd, 0, 0, wd, nw, A, warp, nwarps, lane);
+  pack_rows(cur, n0, n1, wd, 0, 0, wd, n1, A, warp, nwarps, lane);
   if (tid < 3) spop[tid] = 0;
   __syncthreads();
   for (int g = 0; g < gens; ++g) {
@@ -210,6 +273,7 @@ struct TbParams {
 // memory and writes back its owned cells.  After g generations the halo's
 // stale front has moved g cells / rows inward; kk <= 32 keeps it inside the
 // halo word, and kk rows of vertical halo keep it off the owned rows.
+template <bool VEC>
 __global__ void __launch_bounds__(256)
 life_tb_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next,
                TbParams p, uint32_t *__restrict__ pop) {
@@ -226,8 +290,10 @@ life_tb_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next,
   const int stride = (p.tw + 2) * (p.th + 2 * kk);
   uint32_t *A = sm, *B = sm + stride;
   if (tid < 32) spop[tid] = 0;
-  pack_words(cur, p.n0, p.n1, p.wd, row0 - kk, col0 - 1, NC, NC * NR, A, warp,
-             nwarps, lane);
+  if (VEC)
+    pack_rows_vec<4>(cur, p.n0, p.n1, p.wd, row0 - kk, col0 - 1, NC, NR, A, warp, nwarps, lane);
+  else
+    pack_rows(cur, p.n0, p.n1, p.wd, row0 - kk, col0 - 1, NC, NR, A, warp, nwarps, lane);
   __syncthreads();
   const int NG = max(1, nthreads / NC);
   for (int g = 1; g <= kk; ++g) {
@@ -261,18 +327,247 @@ life_tb_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next,
     uint32_t *tmp = A; A = B; B = tmp;
   }
   if (tid < kk && spop[tid]) atomicAdd(&pop[tid], spop[tid]);
-  // write back the owned words
-  const int nown = tw_own * th_own;
-  for (int base = warp * 4; base < nown; base += nwarps * 4) {
+  // write back the owned words, one warp per row
+  if (VEC) {
+    // lane L writes cells 4(L%8)..+3 of word L/8 of each 4-word group
+    const int sub = lane >> 3, quad = (lane & 7) * 4;
+    for (int r = warp; r < th_own; r += nwarps) {
+      const uint32_t *src = A + (r + kk) * NC + 1;
+      int32_t *dst = next + (size_t)(row0 + r) * p.n0 + (size_t)col0 * 32 + quad;
+      for (int c0 = 0; c0 < tw_own; c0 += 16) {
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int i = base + j;
-      if (i < nown) {
-        const int r = i / tw_own, c = i - (i / tw_own) * tw_own;
-        const uint32_t w = A[(r + kk) * NC + c + 1];
-        next[(size_t)(row0 + r) * p.n0 + (size_t)(col0 + c) * 32 + lane] =
-            (int32_t)((w >> lane) & 1u);
+        for (int g = 0; g < 4; ++g) {
+          const int cw = c0 + 4 * g + sub;
+          if (cw < tw_own) {
+            const uint32_t w = src[cw] >> quad;
+            *reinterpret_cast<int4 *>(dst + (size_t)cw * 32) =
+                make_int4((int)(w & 1u), (int)((w >> 1) & 1u), (int)((w >> 2) & 1u),
+                          (int)((w >> 3) & 1u));
+          }
+        }
       }
+    }
+  } else {
+    // lane i writes bit i of each word
+    for (int r = warp; r < th_own; r += nwarps) {
+      const uint32_t *src = A + (r + kk) * NC + 1;
+      int32_t *dst = next + (size_t)(row0 + r) * p.n0 + (size_t)col0 * 32 + lane;
+      for (int c0 = 0; c0 < tw_own; c0 += 4) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int c = c0 + j;
+          if (c < tw_own) dst[(size_t)c * 32] = (int32_t)((src[c] >> lane) & 1u);
+        }
+      }
+    }
+  }
+}
+
+// Row sums used by the sliding-window update: horizontal full-adder of the
+// three cells W, C, E of every bit position (f1 ones, f2 twos) and
+// half-adder of W, E (h1, h2), for one 32-cell word.
+struct RowSums {
+  uint32_t raw, f1, f2, h1, h2;
+};
+
+__device__ __forceinline__ RowSums row_sums(uint32_t left, uint32_t w, uint32_t right) {
+  const uint32_t W = __funnelshift_l(left, w, 1), E = __funnelshift_r(w, right, 1);
+  RowSums r;
+  r.raw = w;
+  r.f1 = W ^ w ^ E;
+  r.f2 = (W & w) | (E & (W ^ w));
+  r.h1 = W ^ E;
+  r.h2 = W & E;
+  return r;
+}
+
+// next state of the middle row b from the sums of rows a (above), b, c:
+// num = s0 + 2*(u + k0) with u = a2 + b2 + c2; alive' = (num==3) | (b & num==2)
+// = (u + k0 == 1) & (s0 | b) = ~u2 & (u1 ^ k0) & (s0 | b).
+__device__ __forceinline__ uint32_t life_from_sums(const RowSums &a, const RowSums &b,
+                                                   const RowSums &c) {
+  const uint32_t s0 = a.f1 ^ b.h1 ^ c.f1;
+  const uint32_t k0 = (a.f1 & b.h1) | (c.f1 & (a.f1 ^ b.h1));
+  const uint32_t u1 = a.f2 ^ b.h2 ^ c.f2;
+  const uint32_t u2 = (a.f2 & b.h2) | (c.f2 & (a.f2 ^ b.h2));
+  return ~u2 & (u1 ^ k0) & (s0 | b.raw);
+}
+
+// Temporal blocking with one lane per packed word: a tile is 32 words wide
+// (30 owned + a halo word each side) and th rows tall plus kk halo rows above
+// and below.  Each warp sweeps a contiguous band of rows per generation,
+// taking the left/right neighbour words from the adjacent lanes and keeping
+// the row sums of the previous two rows in registers.
+template <bool VEC>
+__global__ void __launch_bounds__(256, 8)
+life_tb32_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbParams p,
+                 uint32_t *__restrict__ pop) {
+  extern __shared__ uint32_t sm[];
+  __shared__ uint32_t spop[32];
+  constexpr int NC = 32;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nwarps = blockDim.x >> 5;
+  const int t = blockIdx.x;
+  const int t0 = t % p.nt0, t1 = t / p.nt0;
+  const int col0 = t0 * p.tw, row0 = t1 * p.th;
+  const int tw_own = min(p.tw, p.wd - col0), th_own = min(p.th, p.n1 - row0);
+  const int kk = p.kk;
+  const int NR = th_own + 2 * kk;
+  const int stride = NC * (p.th + 2 * kk);
+  uint32_t *A = sm, *B = sm + stride;
+  if (tid < 32) spop[tid] = 0;
+  if (VEC)
+    pack_rows_vec<4>(cur, p.n0, p.n1, p.wd, row0 - kk, col0 - 1, NC, NR, A, warp, nwarps, lane);
+  else
+    pack_rows(cur, p.n0, p.n1, p.wd, row0 - kk, col0 - 1, NC, NR, A, warp, nwarps, lane);
+  __syncthreads();
+  const bool own_c = lane >= 1 && lane <= tw_own;
+  for (int g = 1; g <= kk; ++g) {
+    const int lo = g, hi = NR - g;
+    const int chunk = (hi - lo + nwarps - 1) / nwarps;
+    const int rs = lo + warp * chunk, re = min(rs + chunk, hi);
+    uint32_t cnt = 0;
+    if (rs < re) {
+      uint32_t w = A[(rs - 1) * NC + lane];
+      RowSums a = row_sums(__shfl_up_sync(0xffffffffu, w, 1) & (lane ? ~0u : 0u), w,
+                           __shfl_down_sync(0xffffffffu, w, 1) & (lane < 31 ? ~0u : 0u));
+      w = A[rs * NC + lane];
+      RowSums b = row_sums(__shfl_up_sync(0xffffffffu, w, 1) & (lane ? ~0u : 0u), w,
+                           __shfl_down_sync(0xffffffffu, w, 1) & (lane < 31 ? ~0u : 0u));
+      for (int r = rs; r < re; ++r) {
+        w = A[(r + 1) * NC + lane];
+        const RowSums c = row_sums(__shfl_up_sync(0xffffffffu, w, 1) & (lane ? ~0u : 0u), w,
+                                   __shfl_down_sync(0xffffffffu, w, 1) & (lane < 31 ? ~0u : 0u));
+        const uint32_t out = life_from_sums(a, b, c);
+        B[r * NC + lane] = out;
+        if (own_c && r >= kk && r < kk + th_own) cnt += __popc(out);
+        a = b;
+        b = c;
+      }
+    }
+    cnt = __reduce_add_sync(0xffffffffu, cnt);
+    if (lane == 0 && cnt) atomicAdd(&spop[g - 1], cnt);
+    __syncthreads();
+    uint32_t *tmp = A; A = B; B = tmp;
+  }
+  if (tid < kk && spop[tid]) atomicAdd(&pop[tid], spop[tid]);
+  // write back the owned words (block columns 1..tw_own), one warp per row
+  if (VEC) {
+    const int sub = lane >> 3, quad = (lane & 7) * 4;
+    for (int r = warp; r < th_own; r += nwarps) {
+      const uint32_t *src = A + (r + kk) * NC + 1;
+      int32_t *dst = next + (size_t)(row0 + r) * p.n0 + (size_t)col0 * 32 + quad;
+      for (int c0 = 0; c0 < tw_own; c0 += 16) {
+#pragma unroll
+        for (int gq = 0; gq < 4; ++gq) {
+          const int cw = c0 + 4 * gq + sub;
+          if (cw < tw_own) {
+            const uint32_t wv = src[cw] >> quad;
+            *reinterpret_cast<int4 *>(dst + (size_t)cw * 32) =
+                make_int4((int)(wv & 1u), (int)((wv >> 1) & 1u), (int)((wv >> 2) & 1u),
+                          (int)((wv >> 3) & 1u));
+          }
+        }
+      }
+    }
+  } else {
+    for (int r = warp; r < th_own; r += nwarps) {
+      const uint32_t *src = A + (r + kk) * NC + 1;
+      int32_t *dst = next + (size_t)(row0 + r) * p.n0 + (size_t)col0 * 32 + lane;
+      for (int c = 0; c < tw_own; ++c) dst[(size_t)c * 32] = (int32_t)((src[c] >> lane) & 1u);
+    }
+  }
+}
+
+// Register-resident temporal blocking.  A block is NW warps x R rows of 32
+// packed words (30 owned + halo word each side); warp w keeps rows
+// [wR, wR+R) in registers for all kk generations and trades only its first
+// and last row with the neighbouring warps through shared memory, once per
+// generation.  Rows are not shrunk per generation: the stale front from the
+// block's outer rows and columns moves one cell per generation and never
+// reaches the owned rows [kk, kk + th_own) and words 1..tw_own.
+template <int R, int NW, bool VEC>
+__global__ void __launch_bounds__(NW * 32, (NW >= 16 ? 2 : 4))
+life_reg_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbParams p,
+                uint32_t *__restrict__ pop) {
+  constexpr int NC = 32, NR = R * NW;
+  extern __shared__ uint32_t A[];  // NR x NC packed words
+  __shared__ uint32_t ex[2][NW][2][NC];
+  __shared__ uint32_t spop[32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int t = blockIdx.x;
+  const int t0 = t % p.nt0, t1 = t / p.nt0;
+  const int col0 = t0 * p.tw, row0 = t1 * p.th;
+  const int tw_own = min(p.tw, p.wd - col0), th_own = min(p.th, p.n1 - row0);
+  const int kk = p.kk;
+  if (tid < 32) spop[tid] = 0;
+  if (VEC)
+    pack_rows_vec<8>(cur, p.n0, p.n1, p.wd, row0 - kk, col0 - 1, NC, NR, A, warp, NW, lane);
+  else
+    pack_rows(cur, p.n0, p.n1, p.wd, row0 - kk, col0 - 1, NC, NR, A, warp, NW, lane);
+  __syncthreads();
+  uint32_t rows[R];
+#pragma unroll
+  for (int i = 0; i < R; ++i) rows[i] = A[(warp * R + i) * NC + lane];
+  // owned rows of this warp as a bit mask; owned columns as a lane mask
+  uint32_t ownrows = 0;
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int gr = warp * R + i - kk;
+    if (gr >= 0 && gr < th_own) ownrows |= 1u << i;
+  }
+  const uint32_t colmask = (lane >= 1 && lane <= tw_own) ? ~0u : 0u;
+  for (int g = 0; g < kk; ++g) {
+    const int b = g & 1;
+    ex[b][warp][0][lane] = rows[0];
+    ex[b][warp][1][lane] = rows[R - 1];
+    __syncthreads();
+    const uint32_t up = warp > 0 ? ex[b][warp - 1][1][lane] : 0u;
+    const uint32_t down = warp < NW - 1 ? ex[b][warp + 1][0][lane] : 0u;
+    RowSums ra = row_sums(__shfl_up_sync(0xffffffffu, up, 1), up,
+                          __shfl_down_sync(0xffffffffu, up, 1));
+    RowSums rb = row_sums(__shfl_up_sync(0xffffffffu, rows[0], 1), rows[0],
+                          __shfl_down_sync(0xffffffffu, rows[0], 1));
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const uint32_t wn = (i + 1 < R) ? rows[i + 1] : down;
+      const RowSums rc = row_sums(__shfl_up_sync(0xffffffffu, wn, 1), wn,
+                                  __shfl_down_sync(0xffffffffu, wn, 1));
+      const uint32_t out = life_from_sums(ra, rb, rc);
+      rows[i] = out;
+      if (ownrows & (1u << i)) cnt += __popc(out & colmask);
+      ra = rb;
+      rb = rc;
+    }
+    cnt = __reduce_add_sync(0xffffffffu, cnt);
+    if (lane == 0 && cnt) atomicAdd(&spop[g], cnt);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < R; ++i) A[(warp * R + i) * NC + lane] = rows[i];
+  __syncthreads();
+  if (tid < kk && spop[tid]) atomicAdd(&pop[tid], spop[tid]);
+  const int sub = lane >> 3, quad = (lane & 7) * 4;
+  for (int r = warp; r < th_own; r += NW) {
+    const uint32_t *src = A + (r + kk) * NC + 1;
+    int32_t *dst = next + (size_t)(row0 + r) * p.n0 + (size_t)col0 * 32;
+    if (VEC) {
+      for (int c0 = 0; c0 < tw_own; c0 += 16) {
+#pragma unroll
+        for (int gq = 0; gq < 4; ++gq) {
+          const int cw = c0 + 4 * gq + sub;
+          if (cw < tw_own) {
+            const uint32_t wv = src[cw] >> quad;
+            *reinterpret_cast<int4 *>(dst + (size_t)cw * 32 + quad) =
+                make_int4((int)(wv & 1u), (int)((wv >> 1) & 1u), (int)((wv >> 2) & 1u),
+                          (int)((wv >> 3) & 1u));
+          }
+        }
+      }
+    } else {
+      for (int c = 0; c < tw_own; ++c)
+        dst[(size_t)c * 32 + lane] = (int32_t)((src[c] >> lane) & 1u);
     }
   }
 }
@@ -328,17 +623,64 @@ static om_status life_init(Handle *h, int n) {
   return OM_OK;
 }
 
-static void life_pick_tiles(Handle *h, TbParams &p) {
-  LifeState *st = life_state(h);
-  p.kk = st->depth > 0 ? std::min(st->depth, 32) : 16;
-  p.tw = st->tile_w > 0 ? st->tile_w : 32;
-  p.th = st->tile_h > 0 ? st->tile_h : 64;
-  p.tw = std::min(p.tw, p.wd);
-  p.th = std::min(p.th, p.n1);
+// Register-resident kernel variants: R rows per warp x NW warps per block.
+struct RegVariant {
+  int R, NW;
+};
+static const RegVariant kRegVariants[] = {{16, 8}, {24, 8}, {16, 16}, {32, 8}, {24, 16}, {32, 16}};
+static const int kNumRegVariants = 6;
+
+template <bool VEC>
+static cudaError_t launch_reg(int v, const int32_t *cur, int32_t *next, const TbParams &p,
+                              uint32_t *pop, cudaStream_t s) {
+  const RegVariant rv = kRegVariants[v];
+  const size_t smem = sizeof(uint32_t) * 32 * rv.R * rv.NW;
+  void (*k)(const int32_t *, int32_t *, TbParams, uint32_t *) = nullptr;
+  switch (v) {
+    case 0: k = life_reg_kernel<16, 8, VEC>; break;
+    case 1: k = life_reg_kernel<24, 8, VEC>; break;
+    case 2: k = life_reg_kernel<16, 16, VEC>; break;
+    case 3: k = life_reg_kernel<32, 8, VEC>; break;
+    case 4: k = life_reg_kernel<24, 16, VEC>; break;
+    default: k = life_reg_kernel<32, 16, VEC>; break;
+  }
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k<<<p.nt0 * p.nt1, rv.NW * 32, smem, s>>>(cur, next, p, pop);
+  return cudaGetLastError();
 }
 
-static size_t tb_smem_bytes(const TbParams &p) {
-  return 2 * sizeof(uint32_t) * (size_t)(p.tw + 2) * (p.th + 2 * p.kk);
+// register variant for kk generations: the smallest block whose owned rows
+// (block rows - 2kk) reach the requested tile height (default 320, the
+// 24-row x 16-warp block at depth 32: fastest in the GB300 tile sweep)
+static int reg_variant(int kk, int want_th) {
+  const int want = want_th > 0 ? want_th : 320;
+  int best = -1;
+  for (int v = 0; v < kNumRegVariants; ++v) {
+    const int th = kRegVariants[v].R * kRegVariants[v].NW - 2 * kk;
+    if (th >= want) { best = v; break; }
+    if (th >= 1) best = v;
+  }
+  return best < 0 ? kNumRegVariants - 1 : best;
+}
+
+// Tile choice: tile_w 0 (default) selects the register-resident kernel,
+// 30 the one-lane-per-word shared-memory kernel, other widths the general
+// tile kernel.  Depth defaults to 32 generations per launch.
+static bool life_pick_tiles(Handle *h, TbParams &p) {
+  LifeState *st = life_state(h);
+  const bool lane_per_word = st->tile_w == 0 || st->tile_w == 30;
+  p.kk = st->depth > 0 ? std::min(st->depth, 32) : 32;
+  p.tw = lane_per_word ? 30 : st->tile_w;
+  p.th = st->tile_h > 0 ? st->tile_h : 128;
+  p.tw = std::min(p.tw, p.wd);
+  p.th = std::min(p.th, p.n1);
+  return lane_per_word;
+}
+
+static size_t tb_smem_bytes(const TbParams &p, bool lane_per_word) {
+  const int nc = lane_per_word ? 32 : p.tw + 2;
+  return 2 * sizeof(uint32_t) * (size_t)nc * (p.th + 2 * p.kk);
 }
 
 static om_status launch_general(Handle *h, uint32_t *pop) {
@@ -395,25 +737,53 @@ static om_status life_proceed(Handle *h, int n) {
     } else {
       TbParams p;
       p.n0 = n0; p.n1 = n1; p.wd = wd;
-      life_pick_tiles(h, p);
+      const bool l32 = life_pick_tiles(h, p);
+      const bool reg = st->tile_w == 0;
       const int kmax = p.kk;
       p.nt0 = (p.wd + p.tw - 1) / p.tw;
       p.nt1 = (p.n1 + p.th - 1) / p.th;
       // split the remaining generations into launches of near-equal depth
       const int rem = n - g;
       const int nl = (rem + kmax - 1) / kmax;
-      const size_t smem_max = tb_smem_bytes(p);
-      OM_CUDA_CHECK(cudaFuncSetAttribute(life_tb_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem_max));
+      const size_t smem_max = tb_smem_bytes(p, l32);
+      const bool vec = h->cfg.life_io != 1;
+      auto kern = l32 ? (vec ? life_tb32_kernel<true> : life_tb32_kernel<false>)
+                      : (vec ? life_tb_kernel<true> : life_tb_kernel<false>);
+      const char *kname = l32 ? "life_tb32_kernel" : "life_tb_kernel";
+      if (!reg)
+        OM_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem_max));
       for (int l = 0; l < nl; ++l) {
         const int kk = rem / nl + (l < rem % nl ? 1 : 0);
         p.kk = kk;
+        if (reg) {
+          const int v = reg_variant(kk, st->tile_h);
+          TbParams q = p;
+          q.tw = std::min(30, wd);
+          q.th = std::min(kRegVariants[v].R * kRegVariants[v].NW - 2 * kk, n1);
+          q.nt0 = (wd + q.tw - 1) / q.tw;
+          q.nt1 = (n1 + q.th - 1) / q.th;
+          cudaEvent_t ev = prof_begin(h);
+          cudaError_t e = vec ? launch_reg<true>(v, (const int32_t *)a.d(), (int32_t *)a.d_next(),
+                                                 q, st->d_pop + g, h->stream)
+                              : launch_reg<false>(v, (const int32_t *)a.d(),
+                                                  (int32_t *)a.d_next(), q, st->d_pop + g,
+                                                  h->stream);
+          if (e != cudaSuccess) {
+            set_error(std::string("life_reg_kernel: ") + cudaGetErrorString(e));
+            return OM_ERR_CUDA;
+          }
+          prof_end(h, ev, "life_reg_kernel", (double)n0 * n1 * kk);
+          h->launches++;
+          a.swap();
+          g += kk;
+          continue;
+        }
         cudaEvent_t ev = prof_begin(h);
-        life_tb_kernel<<<p.nt0 * p.nt1, 256, tb_smem_bytes(p), h->stream>>>(
+        kern<<<p.nt0 * p.nt1, 256, tb_smem_bytes(p, l32), h->stream>>>(
             (const int32_t *)a.d(), (int32_t *)a.d_next(), p, st->d_pop + g);
         OM_CUDA_CHECK(cudaGetLastError());
-        prof_end(h, ev, "life_tb_kernel", (double)n0 * n1 * kk);
+        prof_end(h, ev, kname, (double)n0 * n1 * kk);
         h->launches++;
         a.swap();
         g += kk;
@@ -467,11 +837,11 @@ cudaError_t life_tb_launch_into(const int32_t *cur, int32_t *next, int n0, int n
   p.th = std::min(64, n1);
   p.nt0 = (p.wd + p.tw - 1) / p.tw;
   p.nt1 = (p.n1 + p.th - 1) / p.th;
-  const size_t smem = tb_smem_bytes(p);
-  cudaError_t e = cudaFuncSetAttribute(life_tb_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
+  const size_t smem = tb_smem_bytes(p, false);
+  cudaError_t e = cudaFuncSetAttribute(life_tb_kernel<false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  life_tb_kernel<<<p.nt0 * p.nt1, 256, smem, s>>>(cur, next, p, pop);
+  life_tb_kernel<false><<<p.nt0 * p.nt1, 256, smem, s>>>(cur, next, p, pop);
   return cudaGetLastError();
 }
 

@@ -32,7 +32,8 @@ def test_life_128_bernoulli_1000(om_lib, oracle):
     life.close()
 
 
-@pytest.mark.parametrize("size", [(37, 29), (1, 7), (5, 1), (80, 48), (33, 64), (130, 17)])
+@pytest.mark.parametrize("size", [(37, 29), (1, 7), (5, 1), (80, 48), (33, 64), (130, 17),
+                                  (96, 5000), (160, 3)])
 def test_life_general_path_odd_sizes(om_lib, oracle, size):
     init = oracle.life_bernoulli(size[0], size[1], 5, 0.35)
     cells, pops, pop, gen, _ = run_gpu(om_lib, size, init, 25)
@@ -52,13 +53,17 @@ def test_life_open_boundary(om_lib, oracle, size):
     assert np.array_equal(pops, rp)
 
 
+@pytest.mark.parametrize("io", [0, 1])
 @pytest.mark.parametrize("depth,tw,th", [(16, 0, 0), (1, 4, 8), (7, 3, 5), (32, 8, 64),
-                                         (32, 64, 128), (25, 16, 100)])
-def test_life_temporal_blocking_tiles(om_lib, oracle, depth, tw, th):
+                                         (32, 64, 128), (25, 16, 100), (32, 16, 128),
+                                         (32, 30, 64), (9, 30, 17), (0, 0, 0),
+                                         (32, 0, 64), (32, 0, 192), (32, 0, 300), (32, 0, 400),
+                                         (5, 0, 0), (31, 0, 100)])
+def test_life_temporal_blocking_tiles(om_lib, oracle, depth, tw, th, io):
     size = (1024, 640)
     init = oracle.life_bernoulli(size[0], size[1], 11, 0.3)
     cells, pops, pop, gen, launches = run_gpu(om_lib, size, init, 70, depth=depth,
-                                              tile_x=tw, tile_y=th)
+                                              tile_x=tw, tile_y=th, life_io=io)
     rc, rp = oracle.life_run(init, 70, cyclic=True)
     assert np.array_equal(cells, rc)
     assert np.array_equal(pops, rp)
