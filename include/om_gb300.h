@@ -66,7 +66,9 @@ typedef struct {
   int variant;      /* 0 = fastest path.  Life 1: integer one-cell-per-thread kernel only.
                        Hydro 1: plain unfused FP64-structured grid-stride kernels */
   int life_io;      /* Life cell I/O of the packed kernels: 0 = 128-bit, 1 = 32-bit */
-  int reserved[6];
+  int life_kernel;  /* Life packed kernel: 0 = register-resident blocks,
+                       k >= 1 = warp-specialised persistent kernel, variant k-1 */
+  int reserved[5];
 } om_config;
 
 /* Fill `cfg` with defaults: cyclic, FP32, gamma 5/3, device 0, tuned tiles. */

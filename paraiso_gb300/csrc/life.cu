@@ -497,8 +497,11 @@ life_reg_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbP
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int t = blockIdx.x;
   const int t0 = t % p.nt0, t1 = t / p.nt0;
-  const int col0 = t0 * p.tw, row0 = t1 * p.th;
-  const int tw_own = min(p.tw, p.wd - col0), th_own = min(p.th, p.n1 - row0);
+  // tiles split the grid evenly (sizes differ by at most one word / row)
+  const int col0 = (int)((long long)t0 * p.wd / p.nt0);
+  const int row0 = (int)((long long)t1 * p.n1 / p.nt1);
+  const int tw_own = (int)((long long)(t0 + 1) * p.wd / p.nt0) - col0;
+  const int th_own = (int)((long long)(t1 + 1) * p.n1 / p.nt1) - row0;
   const int kk = p.kk;
   if (tid < 32) spop[tid] = 0;
   if (VEC)
@@ -570,6 +573,115 @@ life_reg_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbP
         dst[(size_t)c * 32 + lane] = (int32_t)((src[c] >> lane) & 1u);
     }
   }
+}
+
+// Warp-specialised persistent variant of the register-resident kernel: one
+// CTA per SM walks its share of the tiles through a three-stage pipeline
+// over three shared-memory tile buffers.  In stage s, producer warps pack
+// tile s, consumer warps advance tile s-1 by kk generations in registers
+// (edge rows traded through shared memory behind a named barrier that only
+// the consumers use), and store warps write tile s-2 back, so loads,
+// compute and stores of consecutive tiles overlap.  One __syncthreads ends
+// every stage; there are no spin waits.
+template <int R, int NWC, int NWP, int NWS>
+__global__ void __launch_bounds__((NWC + NWP + NWS) * 32, 1)
+life_ws_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbParams p,
+               uint32_t *__restrict__ pop) {
+  constexpr int NC = 32, NR = R * NWC;
+  extern __shared__ uint32_t buf[];  // 3 x NR x NC packed words
+  __shared__ uint32_t ex[2][NWC][2][NC];
+  __shared__ uint32_t spop[32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int kk = p.kk;
+  const int ntiles = p.nt0 * p.nt1;
+  const int m = ntiles > (int)blockIdx.x ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  if (tid < 32) spop[tid] = 0;
+  __syncthreads();
+  for (int s = 0; s < m + 2; ++s) {
+    if (warp < NWC) {
+      if (s >= 1 && s <= m) {
+        // consumers: advance tile s-1
+        const int t = blockIdx.x + (s - 1) * gridDim.x;
+        const int col0 = (t % p.nt0) * p.tw, row0 = (t / p.nt0) * p.th;
+        const int tw_own = min(p.tw, p.wd - col0), th_own = min(p.th, p.n1 - row0);
+        uint32_t *A = buf + ((s - 1) % 3) * NR * NC;
+        uint32_t rows[R];
+#pragma unroll
+        for (int i = 0; i < R; ++i) rows[i] = A[(warp * R + i) * NC + lane];
+        uint32_t ownrows = 0;
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+          const int gr = warp * R + i - kk;
+          if (gr >= 0 && gr < th_own) ownrows |= 1u << i;
+        }
+        const uint32_t colmask = (lane >= 1 && lane <= tw_own) ? ~0u : 0u;
+        for (int g = 0; g < kk; ++g) {
+          const int b = g & 1;
+          ex[b][warp][0][lane] = rows[0];
+          ex[b][warp][1][lane] = rows[R - 1];
+          asm volatile("bar.sync 1, %0;" ::"r"(NWC * 32) : "memory");
+          const uint32_t up = warp > 0 ? ex[b][warp - 1][1][lane] : 0u;
+          const uint32_t down = warp < NWC - 1 ? ex[b][warp + 1][0][lane] : 0u;
+          RowSums ra = row_sums(__shfl_up_sync(0xffffffffu, up, 1), up,
+                                __shfl_down_sync(0xffffffffu, up, 1));
+          RowSums rb = row_sums(__shfl_up_sync(0xffffffffu, rows[0], 1), rows[0],
+                                __shfl_down_sync(0xffffffffu, rows[0], 1));
+          uint32_t cnt = 0;
+#pragma unroll
+          for (int i = 0; i < R; ++i) {
+            const uint32_t wn = (i + 1 < R) ? rows[i + 1] : down;
+            const RowSums rc = row_sums(__shfl_up_sync(0xffffffffu, wn, 1), wn,
+                                        __shfl_down_sync(0xffffffffu, wn, 1));
+            const uint32_t out = life_from_sums(ra, rb, rc);
+            rows[i] = out;
+            if (ownrows & (1u << i)) cnt += __popc(out & colmask);
+            ra = rb;
+            rb = rc;
+          }
+          cnt = __reduce_add_sync(0xffffffffu, cnt);
+          if (lane == 0 && cnt) atomicAdd(&spop[g], cnt);
+        }
+#pragma unroll
+        for (int i = 0; i < R; ++i) A[(warp * R + i) * NC + lane] = rows[i];
+      }
+    } else if (warp < NWC + NWP) {
+      if (s < m) {
+        // producers: pack tile s
+        const int t = blockIdx.x + s * gridDim.x;
+        const int col0 = (t % p.nt0) * p.tw, row0 = (t / p.nt0) * p.th;
+        pack_rows_vec<8>(cur, p.n0, p.n1, p.wd, row0 - kk, col0 - 1, NC, NR,
+                         buf + (s % 3) * NR * NC, warp - NWC, NWP, lane);
+      }
+    } else {
+      if (s >= 2) {
+        // store warps: write back tile s-2
+        const int t = blockIdx.x + (s - 2) * gridDim.x;
+        const int col0 = (t % p.nt0) * p.tw, row0 = (t / p.nt0) * p.th;
+        const int tw_own = min(p.tw, p.wd - col0), th_own = min(p.th, p.n1 - row0);
+        const uint32_t *A = buf + ((s - 2) % 3) * NR * NC;
+        const int sw = warp - NWC - NWP;
+        const int sub = lane >> 3, quad = (lane & 7) * 4;
+        for (int r = sw; r < th_own; r += NWS) {
+          const uint32_t *src = A + (r + kk) * NC + 1;
+          int32_t *dst = next + (size_t)(row0 + r) * p.n0 + (size_t)col0 * 32 + quad;
+          for (int c0 = 0; c0 < tw_own; c0 += 16) {
+#pragma unroll
+            for (int gq = 0; gq < 4; ++gq) {
+              const int cw = c0 + 4 * gq + sub;
+              if (cw < tw_own) {
+                const uint32_t wv = src[cw] >> quad;
+                *reinterpret_cast<int4 *>(dst + (size_t)cw * 32) =
+                    make_int4((int)(wv & 1u), (int)((wv >> 1) & 1u), (int)((wv >> 2) & 1u),
+                              (int)((wv >> 3) & 1u));
+              }
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (tid < kk && spop[tid]) atomicAdd(&pop[tid], spop[tid]);
 }
 
 __global__ void life_fill_kernel(int32_t *cell, int n0, int n1, int ms0, int lm,
@@ -648,6 +760,97 @@ static cudaError_t launch_reg(int v, const int32_t *cur, int32_t *next, const Tb
   if (e != cudaSuccess) return e;
   k<<<p.nt0 * p.nt1, rv.NW * 32, smem, s>>>(cur, next, p, pop);
   return cudaGetLastError();
+}
+
+// warp-specialised variants: R rows x NWC consumer warps, NWP producer and
+// NWS store warps, one CTA per SM
+struct WsVariant {
+  int R, NWC, NWP, NWS;
+};
+static const WsVariant kWsVariants[] = {{24, 16, 8, 8}, {16, 16, 8, 8}, {24, 16, 12, 4},
+                                        {20, 16, 8, 8}};
+static const int kNumWsVariants = 4;
+
+static cudaError_t launch_ws(int v, const int32_t *cur, int32_t *next, const TbParams &p,
+                             uint32_t *pop, int sms, cudaStream_t s) {
+  const WsVariant wv = kWsVariants[v];
+  const size_t smem = sizeof(uint32_t) * 3 * 32 * wv.R * wv.NWC;
+  void (*k)(const int32_t *, int32_t *, TbParams, uint32_t *) = nullptr;
+  switch (v) {
+    case 0: k = life_ws_kernel<24, 16, 8, 8>; break;
+    case 1: k = life_ws_kernel<16, 16, 8, 8>; break;
+    case 2: k = life_ws_kernel<24, 16, 12, 4>; break;
+    default: k = life_ws_kernel<20, 16, 8, 8>; break;
+  }
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const int ntiles = p.nt0 * p.nt1;
+  const int grid = ntiles < sms ? ntiles : sms;
+  k<<<grid, (wv.NWC + wv.NWP + wv.NWS) * 32, smem, s>>>(cur, next, p, pop);
+  return cudaGetLastError();
+}
+
+// Resident blocks per SM of a register variant (queried once per device).
+static int reg_occupancy(int device, int v, bool vec) {
+  static int cache[64][kNumRegVariants][2];
+  if (device < 0 || device >= 64) return 1;
+  int &c = cache[device][v][vec ? 1 : 0];
+  if (c) return c;
+  const RegVariant rv = kRegVariants[v];
+  const size_t smem = sizeof(uint32_t) * 32 * rv.R * rv.NW;
+  void (*k)(const int32_t *, int32_t *, TbParams, uint32_t *) = nullptr;
+  switch (v) {
+    case 0: k = vec ? life_reg_kernel<16, 8, true> : life_reg_kernel<16, 8, false>; break;
+    case 1: k = vec ? life_reg_kernel<24, 8, true> : life_reg_kernel<24, 8, false>; break;
+    case 2: k = vec ? life_reg_kernel<16, 16, true> : life_reg_kernel<16, 16, false>; break;
+    case 3: k = vec ? life_reg_kernel<32, 8, true> : life_reg_kernel<32, 8, false>; break;
+    case 4: k = vec ? life_reg_kernel<24, 16, true> : life_reg_kernel<24, 16, false>; break;
+    default: k = vec ? life_reg_kernel<32, 16, true> : life_reg_kernel<32, 16, false>; break;
+  }
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, rv.NW * 32, smem) != cudaSuccess || n < 1) {
+    cudaGetLastError();
+    n = 1;
+  }
+  c = n;
+  return n;
+}
+
+// Launch plan for the register kernel: the variant and tile grid (nt0 x nt1,
+// tiles split evenly) minimising waves x resident-blocks x block-rows, i.e.
+// the issue time of an instruction-bound kernel including the last,
+// partly empty wave.  Returns the variant.
+static int reg_plan(int device, bool vec, int wd, int n1, int kk, int *nt0_out, int *nt1_out) {
+  const int sms = sm_count(device);
+  double best_cost = 1e300;
+  int best_v = 1, best0 = (wd + 29) / 30, best1 = 1;
+  for (int v = 0; v < kNumRegVariants; ++v) {
+    const int NR = kRegVariants[v].R * kRegVariants[v].NW;
+    const int thm = NR - 2 * kk;
+    if (thm < 8) continue;
+    const int occ = reg_occupancy(device, v, vec);
+    const long long slots = (long long)occ * sms;
+    const int nt0min = (wd + 29) / 30;
+    const int nt1min = (n1 + thm - 1) / thm;
+    for (int nt0 = nt0min; nt0 <= nt0min + 2 && nt0 <= wd; ++nt0)
+      for (int nt1 = nt1min; nt1 <= nt1min + 24 && nt1 <= n1; ++nt1) {
+        const long long tiles = (long long)nt0 * nt1;
+        const long long waves = (tiles + slots - 1) / slots;
+        // per-tile work ~ block rows x lanes in use (owned words + 2 halo)
+        const double lanes = std::min(32.0, (double)wd / nt0 + 2.0);
+        const double cost = (double)waves * occ * NR * (lanes / 32.0 * 0.25 + 0.75);
+        if (cost < best_cost - 1e-9) {
+          best_cost = cost;
+          best_v = v;
+          best0 = nt0;
+          best1 = nt1;
+        }
+      }
+  }
+  *nt0_out = best0;
+  *nt1_out = best1;
+  return best_v;
 }
 
 // register variant for kk generations: the smallest block whose owned rows
@@ -756,13 +959,39 @@ static om_status life_proceed(Handle *h, int n) {
       for (int l = 0; l < nl; ++l) {
         const int kk = rem / nl + (l < rem % nl ? 1 : 0);
         p.kk = kk;
-        if (reg) {
-          const int v = reg_variant(kk, st->tile_h);
+        if (reg && h->cfg.life_kernel >= 1) {
+          // warp-specialised persistent kernel, variant life_kernel - 1
+          const int v = std::min(h->cfg.life_kernel - 1, kNumWsVariants - 1);
+          const WsVariant wv = kWsVariants[v];
           TbParams q = p;
           q.tw = std::min(30, wd);
-          q.th = std::min(kRegVariants[v].R * kRegVariants[v].NW - 2 * kk, n1);
+          q.th = std::min(wv.R * wv.NWC - 2 * kk, n1);
           q.nt0 = (wd + q.tw - 1) / q.tw;
           q.nt1 = (n1 + q.th - 1) / q.th;
+          cudaEvent_t ev = prof_begin(h);
+          cudaError_t e = launch_ws(v, (const int32_t *)a.d(), (int32_t *)a.d_next(), q,
+                                    st->d_pop + g, sm_count(h->device), h->stream);
+          if (e != cudaSuccess) {
+            set_error(std::string("life_ws_kernel: ") + cudaGetErrorString(e));
+            return OM_ERR_CUDA;
+          }
+          prof_end(h, ev, "life_ws_kernel", (double)n0 * n1 * kk);
+          h->launches++;
+          a.swap();
+          g += kk;
+          continue;
+        }
+        if (reg) {
+          TbParams q = p;
+          const int v = st->tile_h > 0 ? reg_variant(kk, st->tile_h)
+                                       : reg_plan(h->device, vec, wd, n1, kk, &q.nt0, &q.nt1);
+          if (st->tile_h > 0) {
+            const int thm = std::min(kRegVariants[v].R * kRegVariants[v].NW - 2 * kk, n1);
+            q.nt0 = (wd + 29) / 30;
+            q.nt1 = (n1 + thm - 1) / thm;
+          }
+          q.tw = (wd + q.nt0 - 1) / q.nt0;
+          q.th = (n1 + q.nt1 - 1) / q.nt1;
           cudaEvent_t ev = prof_begin(h);
           cudaError_t e = vec ? launch_reg<true>(v, (const int32_t *)a.d(), (int32_t *)a.d_next(),
                                                  q, st->d_pop + g, h->stream)

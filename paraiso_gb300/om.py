@@ -49,7 +49,7 @@ class Config(C.Structure):
     _fields_ = [("boundary", C.c_int), ("precision", C.c_int), ("gamma", C.c_double),
                 ("device", C.c_int), ("depth", C.c_int), ("tile_x", C.c_int),
                 ("tile_y", C.c_int), ("use_graph", C.c_int), ("variant", C.c_int),
-                ("life_io", C.c_int), ("reserved", C.c_int * 6)]
+                ("life_io", C.c_int), ("life_kernel", C.c_int), ("reserved", C.c_int * 5)]
 
 
 _lib = None

@@ -70,6 +70,18 @@ def test_life_temporal_blocking_tiles(om_lib, oracle, depth, tw, th, io):
     assert launches >= 2
 
 
+@pytest.mark.parametrize("kernel", [1, 2, 3, 4])
+@pytest.mark.parametrize("depth", [32, 13])
+def test_life_warp_specialised(om_lib, oracle, kernel, depth):
+    size = (2048, 1500)   # several tiles per CTA on a small grid, partial tiles
+    init = oracle.life_bernoulli(size[0], size[1], 17, 0.3)
+    cells, pops, pop, gen, launches = run_gpu(om_lib, size, init, 45, depth=depth,
+                                              life_kernel=kernel)
+    rc, rp = oracle.life_run(init, 45, cyclic=True)
+    assert np.array_equal(cells, rc)
+    assert np.array_equal(pops, rp)
+
+
 def test_life_nonbinary_first_step(om_lib, oracle):
     init = oracle.life_bernoulli(256, 96, 2, 0.3)
     init[10, 10] = 3
