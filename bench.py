@@ -247,16 +247,141 @@ def life_workload(args, dist: Dist) -> dict:
 
 
 def profile_traffic(kernel: str, n: int):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", f"{kernel}_traffic.json")
+    """DRAM bytes per launch of `kernel` at grid size n, from the committed ncu
+    summary profiles/<kernel>_traffic.txt ("key: value" lines)."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_traffic.txt")
     try:
+        d = {}
         with open(path) as f:
-            d = json.load(f)
-        if d.get("n") == n:
-            return d
+            for line in f:
+                if ":" in line and not line.startswith("#"):
+                    k, v = line.split(":", 1)
+                    d[k.strip()] = v.strip()
+        if int(d["n"]) == n:
+            return {"bytes_per_launch": float(d["bytes_per_launch"]), "source": path}
     except Exception:
         pass
     return None
+
+
+def hydro_workload(args, dist: Dist) -> dict:
+    import paraiso_gb300 as pg
+    from paraiso_gb300 import build as pgbuild
+    pgbuild.build()
+    n = args.size or 4096
+    cells = n * n
+    h = pg.Hydro((n, n), precision=32, gamma=1.4, device=dist.local_rank,
+                 tile_x=args.tile_x, tile_y=args.tile_y)
+    h.init_kh(1 + dist.rank)
+    h.set_scalar("cfl", 0.4)
+    h.proceed(max(args.warmup, 1))
+    clocks = ClockSampler(dist.local_rank)
+    clocks.start()
+    dist.barrier()
+    ms = h.time_run("proceed", args.steps)
+    launches = h.last_launch_count()
+    dist.barrier()
+    clk = clocks.stop()
+    ms = dist.max(ms)
+    value = cells * args.steps * dist.world / (ms * 1e-3) / 1e9
+    # dominant kernel per launch
+    h.profile(True)
+    h.time_run("proceed", min(args.steps, 10))
+    nl, kms, _ = h.profile_query("hydro_fused_kernel_f32")
+    h.profile(False)
+    peak, peak_kind = peaks()
+    per_launch_ms = kms / max(nl, 1)
+    achieved = 32.0 * cells / (per_launch_ms * 1e-3) / 1e9
+    traffic = profile_traffic("hydro_fused_kernel_f32", n)
+    roofline = {"bound": "hbm", "kernel": "hydro_fused_kernel_f32", "achieved": round(achieved, 1),
+                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "traffic": traffic["bytes_per_launch"] if traffic else None,
+                "algorithmic_bytes_per_launch": 32.0 * cells, "launch_ms": round(per_launch_ms, 4),
+                "peak_source": f"{peak_kind} MEASURED_PEAKS.json hbm_gbs",
+                "note": "32 B per cell-update (4 FP32 fields in + out); the fused step is "
+                        "bound by FP32 CUDA-core issue, not HBM"}
+    # end to end: per step upload the four fields from pinned host memory, one
+    # step, read the four fields back
+    import torch
+    hosts = [torch.empty(cells, dtype=torch.float32).pin_memory() for _ in range(4)]
+    names = ("density", "velocity0", "velocity1", "pressure")
+    for t, nm in zip(hosts, names):
+        h.read_to_pointer(nm, t.data_ptr(), cells * 4)
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for t, nm in zip(hosts, names):
+            h.write_from_pointer(nm, t.data_ptr(), cells * 4)
+        h.proceed(1)
+        for t, nm in zip(hosts, names):
+            h.read_to_pointer(nm, t.data_ptr(), cells * 4)
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e = {"value": round(cells * e2e_steps * dist.world / e2e_s / 1e9, 3),
+           "unit": "Gcell-updates/s", "h2d_bytes_per_step": 4 * cells * 4,
+           "d2h_bytes_per_step": 4 * cells * 4, "steps": e2e_steps}
+    # the plain FP64 GPU path (the generated structure) and FP64 accuracy reference
+    plain = pg.Hydro((n, n), precision=64, variant=1, gamma=1.4, device=dist.local_rank)
+    plain.init_kh(1 + dist.rank)
+    plain.set_scalar("cfl", 0.4)
+    plain.proceed(1)
+    pms = plain.time_run("proceed", 2) / 2
+    plain.close()
+    plain_gcell = cells / (pms * 1e-3) / 1e9
+    acc = None
+    if args.accuracy_steps > 0:
+        import numpy as np
+        a = pg.Hydro((n, n), precision=32, gamma=1.4, device=dist.local_rank)
+        b = pg.Hydro((n, n), precision=64, gamma=1.4, device=dist.local_rank)
+        for x in (a, b):
+            x.init_kh(1 + dist.rank)
+            x.set_scalar("cfl", 0.4)
+        a.proceed(args.accuracy_steps)
+        b.proceed(args.accuracy_steps)
+        sa = [x.astype(np.float64) for x in a.state()]
+        sb = b.state()
+        def cons(st):
+            r, u, v, p = st
+            return {"density": r, "momentum0": r * u, "momentum1": r * v,
+                    "energy": 0.5 * r * (u * u + v * v) + p / 0.4}
+        ca, cb = cons(sa), cons(sb)
+        acc = {"steps": args.accuracy_steps, "reference": "FP64 fused path (bit-exact with the oracle)"}
+        for k in ca:
+            d = np.abs(ca[k] - cb[k])
+            acc[k] = {"l1_rel": float(d.mean() / np.abs(cb[k]).mean()), "linf": float(d.max())}
+        ta, tb = a.totals(), b.totals()
+        acc["totals_rel_diff"] = [float((x - y) / y) if y else float(x - y) for x, y in zip(ta, tb)]
+        a.close()
+        b.close()
+    h.close()
+    out = {
+        "metric": "Hydro cell-updates/s (Gcell-updates/s), FP32 bulk, FP64 dt/totals",
+        "value": round(value, 3), "unit": "Gcell-updates/s", "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"hydro {n}x{n} periodic Kelvin-Helmholtz, gamma 1.4, CFL 0.4, "
+                               "noise seed 1+rank, one step per step", "n0": n, "n1": n,
+                   "parallelism": f"replicas x{dist.world}",
+                   "l2": "inputs larger than L2" if n >= 4096 else "inputs may fit in L2"},
+        "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+        "plain_fp64_gpu": {"value": round(plain_gcell, 4), "unit": "Gcell-updates/s",
+                           "speedup": round(value / dist.world / plain_gcell, 1)},
+        "accuracy": acc,
+    }
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        from oracle import pyoracle as O
+        O.build()
+        m = min(n, 2048)
+        st = O.hydro_init_kh(m, m, 1)
+        t0 = time.perf_counter()
+        O.hydro_run(st, 1, cyclic=True, gamma=1.4, cfl=0.4)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round(m * m / dt / 1e9, 5), "unit": "Gcell-updates/s",
+                               "cores": O.lib().oracle_num_threads(), "kind": "port",
+                               "sample": f"1 FP64 step of {m}x{m} Kelvin-Helmholtz, "
+                                         f"oracle/om_oracle.cpp (OpenMP), {dt:.2f} s"}
+    return out
 
 
 def life_cpu_baseline(n: int, args) -> dict:
@@ -319,7 +444,8 @@ def main() -> int:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="life16k",
-                    choices=["life16k", "life128"])
+                    choices=["life16k", "life128", "hydro4k"])
+    ap.add_argument("--accuracy-steps", type=int, default=100)
     ap.add_argument("--size", type=int, default=0)
     ap.add_argument("--generations", type=int, default=0)
     ap.add_argument("--depth", type=int, default=0)
@@ -335,6 +461,8 @@ def main() -> int:
     try:
         if args.impl == "reference":
             out = reference_arm(args, dist)
+        elif args.workload == "hydro4k":
+            out = hydro_workload(args, dist)
         else:
             out = life_workload(args, dist)
         if out is not None and dist.rank == 0:

@@ -23,7 +23,8 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
 # generated C++ does: no multiply-add contraction, IEEE division and sqrt.
 FILE_FLAGS = {
     "hydro_exact.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"],
-    "hydro_fast.cu": ["-prec-div=true", "-prec-sqrt=true"],
+    # the production FP32 step: approximate division/sqrt, flush-to-zero
+    "hydro_fast.cu": ["-use_fast_math"],
 }
 
 

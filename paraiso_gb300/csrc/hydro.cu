@@ -154,11 +154,17 @@ static om_status proceed_plain(Handle *h, int n) {
     OM_CUDA_CHECK(cudaMemcpyAsync(st->h_min, st->d_min, sizeof(unsigned long long),
                                   cudaMemcpyDeviceToHost, h->stream));
     OM_CUDA_CHECK(cudaStreamSynchronize(h->stream));
-    double tsmin;
-    std::memcpy(&tsmin, st->h_min, sizeof(double));
     double dtG;
-    if (st->fp64) dtG = hs_->cfl * tsmin;
-    else dtG = (double)((float)hs_->cfl * (float)tsmin);
+    if (st->fp64) {
+      double tsmin;
+      std::memcpy(&tsmin, st->h_min, sizeof(double));
+      dtG = hs_->cfl * tsmin;
+    } else {
+      const uint32_t bits = (uint32_t)*st->h_min;
+      float tsmin;
+      std::memcpy(&tsmin, &bits, sizeof(float));
+      dtG = (double)((float)hs_->cfl * tsmin);
+    }
     cudaEvent_t ev = prof_begin(h);
     OM_CUDA_CHECK(hydro_plain_step(st->fp64, h->arrays[0].d(), h->arrays[1].d(),
                                    h->arrays[2].d(), h->arrays[3].d(), h->arrays[0].d_next(),

@@ -16,8 +16,8 @@ struct HydroScalars {
   int32_t generation;
   int32_t pad0;
   double time, cfl, dR0, dR1, extent0, extent1;
-  // bit patterns (as unsigned long long of a positive double) of the CFL
-  // minimum of the current state, double-buffered by step parity
+  // bit pattern of the CFL minimum of the current state (see hk::ts_bits),
+  // double-buffered by step parity
   unsigned long long tsmin[2];
   double dt_last;
 };
@@ -35,15 +35,26 @@ struct HydroStepArgs {
 
 namespace hk {
 
-__device__ __forceinline__ unsigned long long ts_bits(double t) {
+// A CFL minimum is kept as the bit pattern of a positive value of the OM's
+// Real type (float bits zero-extended, or double bits): the bit patterns of
+// positive IEEE values order like the values, so atomicMin on them is a min.
+template <class R> __device__ __forceinline__ unsigned long long ts_bits(R t);
+template <> __device__ __forceinline__ unsigned long long ts_bits<float>(float t) {
+  return (unsigned long long)__float_as_uint(t);
+}
+template <> __device__ __forceinline__ unsigned long long ts_bits<double>(double t) {
   return (unsigned long long)__double_as_longlong(t);
 }
 
-template <class R> __device__ __forceinline__ R ts_from_bits(unsigned long long b) {
-  return (R)__longlong_as_double((long long)b);
+template <class R> __device__ __forceinline__ R ts_from_bits(unsigned long long b);
+template <> __device__ __forceinline__ float ts_from_bits<float>(unsigned long long b) {
+  return __uint_as_float((unsigned int)b);
+}
+template <> __device__ __forceinline__ double ts_from_bits<double>(unsigned long long b) {
+  return __longlong_as_double((long long)b);
 }
 
-// block-wide min of a positive double (as bits) folded into *dst
+// block-wide min of CFL bit patterns folded into *dst
 __device__ __forceinline__ void block_min_to(unsigned long long v, unsigned long long *dst,
                                              unsigned long long *red) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -92,7 +103,7 @@ hydro_tsmin_kernel(const R *__restrict__ rho, const R *__restrict__ v0,
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
     const R t = hs::timescale(g, dR0, dR1, rho[i], v0[i], v1[i], p[i]);
-    const unsigned long long b = hk::ts_bits((double)t);
+    const unsigned long long b = hk::ts_bits<R>(t);
     m = b < m ? b : m;
   }
   hk::block_min_to(m, &sc->tsmin[slot], red);
@@ -245,7 +256,7 @@ hydro_fused_kernel(HydroStepArgs a) {
       ovy[gi] = q.v1;
       opr[gi] = q.p;
       const R t = hs::timescale(g, dR0, dR1, q.rho, q.v0, q.v1, q.p);
-      const unsigned long long bits = hk::ts_bits((double)t);
+      const unsigned long long bits = hk::ts_bits<R>(t);
       m = bits < m ? bits : m;
     }
   }
@@ -282,7 +293,7 @@ hydro_plain_reduce_min_kernel(const R *__restrict__ ts, size_t n, unsigned long 
   unsigned long long m = ~0ull;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
-    const unsigned long long b = hk::ts_bits((double)ts[i]);
+    const unsigned long long b = hk::ts_bits<R>(ts[i]);
     m = b < m ? b : m;
   }
   hk::block_min_to(m, out, red);

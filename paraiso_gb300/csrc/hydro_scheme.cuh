@@ -99,11 +99,18 @@ __device__ __forceinline__ Flux<R> hllc(R g, const Prim<R> &L, R cl, const Prim<
   const R shockStar = (Rt.p - L.p + L.rho * uL * (shockLeft - uL) -
                        Rt.rho * uR * (shockRight - uR)) /
                       (L.rho * (shockLeft - uL) - Rt.rho * (shockRight - uR));
-  if (R(0) < shockLeft) return flux_prim<AX>(g, L.rho, L.v0, L.v1, L.p);
-  if (R(0) < shockStar) return star_flux<AX>(g, shockStar, shockLeft, L.rho, L.v0, L.v1, L.p);
-  if (R(0) < shockRight)
-    return star_flux<AX>(g, shockStar, shockRight, Rt.rho, Rt.v0, Rt.v1, Rt.p);
-  return flux_prim<AX>(g, Rt.rho, Rt.v0, Rt.v1, Rt.p);
+  // select (0 < SL) L (select (0 < S*) L* (select (0 < SR) R* R)): pick the
+  // side first, then evaluate one physical or star flux on it, so a warp
+  // whose faces take different cases does not run both star states
+  const bool posL = R(0) < shockLeft, posS = R(0) < shockStar, posR = R(0) < shockRight;
+  const bool useL = posL || posS;
+  const bool star = useL ? !posL : posR;
+  const R xr = useL ? L.rho : Rt.rho, x0 = useL ? L.v0 : Rt.v0, x1 = useL ? L.v1 : Rt.v1,
+          xp = useL ? L.p : Rt.p;
+  const R shock = useL ? shockLeft : shockRight;
+  const Flux<R> fs = star_flux<AX>(g, shockStar, shock, xr, x0, x1, xp);
+  const Flux<R> fp = flux_prim<AX>(g, xr, x0, x1, xp);
+  return star ? fs : fp;
 }
 
 template <class R> __device__ __forceinline__ R absmaller(R a, R b) {
