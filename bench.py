@@ -384,6 +384,75 @@ def hydro_workload(args, dist: Dist) -> dict:
     return out
 
 
+def ensemble_workload(args, dist: Dist) -> dict:
+    import paraiso_gb300 as pg
+    from paraiso_gb300 import build as pgbuild
+    pgbuild.build()
+    count = args.count
+    sizes = pg.ensemble_sizes(count, 1 + dist.rank)
+    e = pg.Ensemble(sizes, precision=32, gamma=1.4, device=dist.local_rank,
+                    tile_x=args.tile_x, tile_y=args.tile_y)
+    e.init_kh(1000 * (1 + dist.rank))
+    info = e.info()
+    cells = info["cells"]
+    e.step(max(args.warmup, 1))
+    # timed: K steps replayed from the CUDA graph of K steps (captured in warm-up)
+    e.step(args.steps)
+    clocks = ClockSampler(dist.local_rank)
+    clocks.start()
+    dist.barrier()
+    ms = e.time_step(args.steps)
+    dist.barrier()
+    clk = clocks.stop()
+    ms = dist.max(ms)
+    t0 = time.perf_counter()
+    e.step(args.steps)              # the public call: graph replay + scalar sync
+    graph_s = dist.max(time.perf_counter() - t0)
+    value = cells * args.steps * dist.world / (ms * 1e-3) / 1e9
+    # the same instances advanced one grid at a time through the single-grid API
+    seq_ms = 0.0
+    nseq = min(count, args.seq_instances)
+    seq_cells = 0
+    for k in range(nseq):
+        h = pg.Hydro(sizes[k], precision=32, gamma=1.4, device=dist.local_rank)
+        h.init_kh(1000 * (1 + dist.rank) + k)
+        h.set_scalar("cfl", 0.4)
+        h.proceed(1)
+        seq_ms += h.time_run("proceed", 10)
+        seq_cells += sizes[k][0] * sizes[k][1]
+        h.close()
+    seq_gcell = seq_cells * 10 / (seq_ms * 1e-3) / 1e9
+    peak, _ = peaks()
+    achieved = 32.0 * cells / (ms / args.steps * 1e-3) / 1e9
+    times = [e.scalar(k, "time") for k in range(count)]
+    out = {
+        "metric": "Hydro ensemble cell-updates/s (Gcell-updates/s), FP32, per-instance CFL dt",
+        "value": round(value, 3), "unit": "Gcell-updates/s", "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"{count} periodic Kelvin-Helmholtz instances, n0,n1 uniform over "
+                               "multiples of 32 in [256,2048] (seed 1+rank), one persistent "
+                               "launch per step, CUDA graph", "instances": count,
+                   "cells": cells, "work_items": info["work_items"], "grid": info["grid"],
+                   "parallelism": f"replicas x{dist.world}"},
+        "roofline": {"bound": "hbm", "kernel": "hydro_ensemble_kernel", "achieved": round(achieved, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": None, "algorithmic_bytes_per_launch": 32.0 * cells,
+                     "launch_ms": round(ms / args.steps, 4)},
+        "e2e": {"value": round(cells * args.steps * dist.world / graph_s / 1e9, 3),
+                "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                "note": "om_ensemble_step(K) through the public API, scalars synced once"},
+        "gpu_launches": 2 * args.steps, "clocks": clk,
+        "single_grid_launches": {"value": round(seq_gcell, 3), "unit": "Gcell-updates/s",
+                                 "instances": nseq,
+                                 "note": "same instances, one grid at a time (om_run_n per grid)"},
+        "instance_time_range": [min(times), max(times)],
+    }
+    e.close()
+    return out
+
+
 def life_cpu_baseline(n: int, args) -> dict:
     from oracle import pyoracle as O
     O.build()
@@ -444,7 +513,9 @@ def main() -> int:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="life16k",
-                    choices=["life16k", "life128", "hydro4k"])
+                    choices=["life16k", "life128", "hydro4k", "ensemble"])
+    ap.add_argument("--count", type=int, default=64)
+    ap.add_argument("--seq-instances", type=int, default=16)
     ap.add_argument("--accuracy-steps", type=int, default=100)
     ap.add_argument("--size", type=int, default=0)
     ap.add_argument("--generations", type=int, default=0)
@@ -463,6 +534,8 @@ def main() -> int:
             out = reference_arm(args, dist)
         elif args.workload == "hydro4k":
             out = hydro_workload(args, dist)
+        elif args.workload == "ensemble":
+            out = ensemble_workload(args, dist)
         else:
             out = life_workload(args, dist)
         if out is not None and dist.rank == 0:

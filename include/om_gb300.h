@@ -169,6 +169,39 @@ om_status om_profile_enable(om_handle h, int enable);
 om_status om_profile_query(om_handle h, const char *kernel, long *launches,
                            double *total_ms, double *total_units);
 
+/* ---- batched Hydro ensembles (no counterpart in the reference) ---------- */
+
+typedef struct om_ensemble_s *om_ensemble;
+
+/* count independent periodic Hydro grids, sizes[2k], sizes[2k+1] = n0, n1 of
+ * instance k (uneven sizes allowed).  cfg: precision 32 (variant 0 fast or
+ * 2 exact) or 64, gamma, tile_x 64 / tile_y 8 pick the FP32 tile shape.
+ * Every instance starts with cfl 0.4, extent 1, dR = 1/n, time 0. */
+om_status om_ensemble_create(int count, const int *sizes, const om_config *cfg,
+                             om_ensemble *out);
+om_status om_ensemble_destroy(om_ensemble e);
+/* count, total interior cells, persistent grid size, tile work items */
+om_status om_ensemble_info(om_ensemble e, int *count, long long *total_cells, int *grid,
+                           int *work_items);
+/* Kelvin-Helmholtz state of om_hydro_init_kh in every instance, seed base+k. */
+om_status om_ensemble_init_kh(om_ensemble e, uint64_t base_seed);
+/* n steps: one persistent launch per step over every (instance, tile), each
+ * instance with its own CFL dt and time; replayed from a CUDA graph. */
+om_status om_ensemble_step(om_ensemble e, int n);
+/* n steps timed with CUDA events on the ensemble's stream (milliseconds). */
+om_status om_ensemble_time_step(om_ensemble e, int n, float *ms);
+/* Copy field ("density", "velocity0", "velocity1", "pressure") of instance k
+ * (n0*n1 elements, host or device memory). */
+om_status om_ensemble_read(om_ensemble e, int k, const char *field, void *dst, size_t bytes);
+om_status om_ensemble_write(om_ensemble e, int k, const char *field, const void *src,
+                            size_t bytes);
+/* Scalars of instance k: "time", "cfl", "dR0", "dR1", "dt" (last step). */
+om_status om_ensemble_scalar(om_ensemble e, int k, const char *name, double *value);
+om_status om_ensemble_set_scalar(om_ensemble e, int k, const char *name, double value);
+/* Compensated FP64 totals (mass, momentum x/y, energy) of instance k. */
+om_status om_ensemble_totals(om_ensemble e, int k, double *out);
+om_status om_ensemble_last_launch_count(om_ensemble e, int *launches);
+
 /* ---- caller-owned buffers, no allocation -------------------------------- */
 
 /* Largest `generations` one om_life_proceed_noalloc call accepts. */

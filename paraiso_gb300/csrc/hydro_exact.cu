@@ -42,6 +42,45 @@ cudaError_t hydro_fused_f32_exact(const HydroStepArgs &a, cudaStream_t s, int *g
   return launch_fused<float, 32, 16, 256>(a, s, grid_out);
 }
 
+template <class R, int TX, int TY, int NT>
+static cudaError_t launch_ensemble(const HydroStepArgs *args, const int *prefix, int count,
+                                   int grid, cudaStream_t s) {
+  const size_t smem = sizeof(FusedSmem<R, TX, TY>);
+  cudaError_t e = cudaFuncSetAttribute(hydro_ensemble_kernel<R, TX, TY, NT>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  hydro_ensemble_kernel<R, TX, TY, NT><<<grid, NT, smem, s>>>(args, prefix, count);
+  return cudaGetLastError();
+}
+
+template <class R, int TX, int TY, int NT> static int occupancy_of() {
+  const size_t smem = sizeof(FusedSmem<R, TX, TY>);
+  cudaFuncSetAttribute(hydro_ensemble_kernel<R, TX, TY, NT>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, hydro_ensemble_kernel<R, TX, TY, NT>, NT,
+                                                    smem) != cudaSuccess || n < 1) {
+    cudaGetLastError();
+    n = 1;
+  }
+  return n;
+}
+
+cudaError_t hydro_ensemble_f64(const HydroStepArgs *args, const int *prefix, int count, int tile,
+                               int grid, cudaStream_t s) {
+  (void)tile;
+  return launch_ensemble<double, 32, 16, 256>(args, prefix, count, grid, s);
+}
+
+cudaError_t hydro_ensemble_f32_exact(const HydroStepArgs *args, const int *prefix, int count,
+                                     int grid, cudaStream_t s) {
+  return launch_ensemble<float, 32, 16, 256>(args, prefix, count, grid, s);
+}
+
+int hydro_ensemble_occupancy_exact(int fp64) {
+  return fp64 ? occupancy_of<double, 32, 16, 256>() : occupancy_of<float, 32, 16, 256>();
+}
+
 cudaError_t hydro_tsmin(int fp64, const void *rho, const void *v0, const void *v1,
                         const void *p, size_t n, double gamma, HydroScalars *sc, int slot,
                         int grid, cudaStream_t s) {

@@ -23,6 +23,53 @@ static cudaError_t launch_fast(const HydroStepArgs &a0, cudaStream_t s, int *gri
   return cudaGetLastError();
 }
 
+cudaError_t hydro_ensemble_f32_exact(const HydroStepArgs *args, const int *prefix, int count,
+                                     int grid, cudaStream_t s);
+int hydro_ensemble_occupancy_exact(int fp64);
+
+template <int TX, int TY, int NT>
+static cudaError_t launch_ens(const HydroStepArgs *args, const int *prefix, int count, int grid,
+                              cudaStream_t s) {
+  const size_t smem = sizeof(FusedSmem<float, TX, TY>);
+  cudaError_t e = cudaFuncSetAttribute(hydro_ensemble_kernel<float, TX, TY, NT>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  hydro_ensemble_kernel<float, TX, TY, NT><<<grid, NT, smem, s>>>(args, prefix, count);
+  return cudaGetLastError();
+}
+
+template <int TX, int TY, int NT> static int occ_fast() {
+  const size_t smem = sizeof(FusedSmem<float, TX, TY>);
+  cudaFuncSetAttribute(hydro_ensemble_kernel<float, TX, TY, NT>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, hydro_ensemble_kernel<float, TX, TY, NT>,
+                                                    NT, smem) != cudaSuccess || n < 1) {
+    cudaGetLastError();
+    n = 1;
+  }
+  return n;
+}
+
+cudaError_t hydro_ensemble_f32(const HydroStepArgs *args, const int *prefix, int count, int tile,
+                               bool exact, int grid, cudaStream_t s) {
+  if (exact) return hydro_ensemble_f32_exact(args, prefix, count, grid, s);
+  switch (tile) {
+    case kTile32x8: return launch_ens<32, 8, 256>(args, prefix, count, grid, s);
+    case kTile64x16: return launch_ens<64, 16, 512>(args, prefix, count, grid, s);
+    default: return launch_ens<32, 16, 256>(args, prefix, count, grid, s);
+  }
+}
+
+int hydro_ensemble_occupancy(int fp64, int tile, bool exact) {
+  if (fp64 || exact) return hydro_ensemble_occupancy_exact(fp64);
+  switch (tile) {
+    case kTile32x8: return occ_fast<32, 8, 256>();
+    case kTile64x16: return occ_fast<64, 16, 512>();
+    default: return occ_fast<32, 16, 256>();
+  }
+}
+
 cudaError_t hydro_fused_f32(const HydroStepArgs &a, int tile, bool exact, cudaStream_t s,
                             int *grid_out) {
   if (exact) return hydro_fused_f32_exact(a, s, grid_out);

@@ -127,15 +127,14 @@ template <class R, int TX, int TY> struct FusedSmem {
   hs::Flux<R> fy[FYY * FYX];
 };
 
+// One tile of the fused step (tile index `tile` of the grid described by a),
+// run by a whole block; the tile with index 0 advances the instance's time.
 template <class R, int TX, int TY, int NT>
-__global__ void __launch_bounds__(NT)
-hydro_fused_kernel(HydroStepArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
+                                           FusedSmem<R, TX, TY> &s, unsigned long long *red) {
   using S = FusedSmem<R, TX, TY>;
-  S &s = *reinterpret_cast<S *>(smem_raw);
-  __shared__ unsigned long long red[32];
   const int tid = threadIdx.x;
-  const int t0 = blockIdx.x % a.nt0, t1 = blockIdx.x / a.nt0;
+  const int t0 = tile % a.nt0, t1 = tile / a.nt0;
   const int X0 = t0 * TX, Y0 = t1 * TY;
   const int n0 = a.n0, n1 = a.n1;
   const R g = (R)a.gamma;
@@ -261,10 +260,43 @@ hydro_fused_kernel(HydroStepArgs a) {
     }
   }
   hk::block_min_to(m, &a.sc->tsmin[1 - a.read_slot], red);
-  if (blockIdx.x == 0 && tid == 0) {
+  if (tile == 0 && tid == 0) {
     a.dt_hist[0] = (double)dtG;
     a.sc->dt_last = (double)dtG;
     a.sc->time = a.sc->time + (double)dtG;
+  }
+}
+
+template <class R, int TX, int TY, int NT>
+__global__ void __launch_bounds__(NT)
+hydro_fused_kernel(HydroStepArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ unsigned long long red[32];
+  fused_tile<R, TX, TY, NT>(a, blockIdx.x, *reinterpret_cast<FusedSmem<R, TX, TY> *>(smem_raw),
+                            red);
+}
+
+// Ensemble step: every tile of every instance is one work item; the
+// persistent grid strides over the flattened item list (prefix[k] = first
+// item of instance k), so instances of any size advance in one launch, each
+// with its own dt, CFL minimum and time (its HydroStepArgs).
+template <class R, int TX, int TY, int NT>
+__global__ void __launch_bounds__(NT)
+hydro_ensemble_kernel(const HydroStepArgs *__restrict__ args, const int *__restrict__ prefix,
+                      int count) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ unsigned long long red[32];
+  auto &s = *reinterpret_cast<FusedSmem<R, TX, TY> *>(smem_raw);
+  const int total = prefix[count];
+  for (int item = blockIdx.x; item < total; item += gridDim.x) {
+    int lo = 0, hi = count - 1;  // instance k with prefix[k] <= item < prefix[k+1]
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (prefix[mid] <= item) lo = mid;
+      else hi = mid - 1;
+    }
+    fused_tile<R, TX, TY, NT>(args[lo], item - prefix[lo], s, red);
+    __syncthreads();
   }
 }
 

@@ -18,6 +18,15 @@ cudaError_t hydro_fused_f32(const HydroStepArgs &a, int tile, bool exact, cudaSt
                             int *grid_out);
 cudaError_t hydro_fused_f64(const HydroStepArgs &a, int tile, cudaStream_t s, int *grid_out);
 
+// ensemble step over every instance (persistent grid of `grid` blocks, 0 =
+// resident blocks x SMs); args/prefix in device memory
+cudaError_t hydro_ensemble_f32(const HydroStepArgs *args, const int *prefix, int count, int tile,
+                               bool exact, int grid, cudaStream_t s);
+cudaError_t hydro_ensemble_f64(const HydroStepArgs *args, const int *prefix, int count, int tile,
+                               int grid, cudaStream_t s);
+// resident blocks per SM of the ensemble kernel for (fp64, tile, exact)
+int hydro_ensemble_occupancy(int fp64, int tile, bool exact);
+
 // CFL minimum of a state into sc->tsmin[slot] (slot pre-set to all ones)
 cudaError_t hydro_tsmin(int fp64, const void *rho, const void *v0, const void *v1,
                         const void *p, size_t n, double gamma, HydroScalars *sc, int slot,

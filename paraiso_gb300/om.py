@@ -36,6 +36,10 @@ EXPORTS = [
     "om_life_fill_random", "om_life_population_history", "om_hydro_init_kh",
     "om_hydro_totals", "om_hydro_dt_history", "om_time_run", "om_last_launch_count",
     "om_profile_enable", "om_profile_query",
+    "om_ensemble_create", "om_ensemble_destroy", "om_ensemble_info", "om_ensemble_init_kh",
+    "om_ensemble_step", "om_ensemble_time_step", "om_ensemble_read", "om_ensemble_write",
+    "om_ensemble_scalar", "om_ensemble_set_scalar", "om_ensemble_totals",
+    "om_ensemble_last_launch_count", "om_life_proceed_noalloc",
 ]
 
 
@@ -92,6 +96,18 @@ def load_library(path: str | None = None) -> C.CDLL:
         "om_time_run": (i, [vp, i, i, C.POINTER(C.c_float)]),
         "om_last_launch_count": (i, [vp, ip]),
         "om_profile_enable": (i, [vp, i]),
+        "om_ensemble_create": (i, [i, ip, C.POINTER(Config), C.POINTER(vp)]),
+        "om_ensemble_destroy": (i, [vp]),
+        "om_ensemble_info": (i, [vp, ip, C.POINTER(C.c_longlong), ip, ip]),
+        "om_ensemble_init_kh": (i, [vp, C.c_uint64]),
+        "om_ensemble_step": (i, [vp, i]),
+        "om_ensemble_time_step": (i, [vp, i, C.POINTER(C.c_float)]),
+        "om_ensemble_read": (i, [vp, i, C.c_char_p, vp, C.c_size_t]),
+        "om_ensemble_write": (i, [vp, i, C.c_char_p, vp, C.c_size_t]),
+        "om_ensemble_scalar": (i, [vp, i, C.c_char_p, C.POINTER(C.c_double)]),
+        "om_ensemble_set_scalar": (i, [vp, i, C.c_char_p, C.c_double]),
+        "om_ensemble_totals": (i, [vp, i, vp]),
+        "om_ensemble_last_launch_count": (i, [vp, ip]),
         "om_profile_query": (i, [vp, C.c_char_p, C.POINTER(C.c_long), C.POINTER(C.c_double),
                                  C.POINTER(C.c_double)]),
     }
@@ -335,3 +351,102 @@ class Hydro(OrthotopeMachine):
     def set_state(self, st) -> None:
         for k, v in zip(("density", "velocity0", "velocity1", "pressure"), st):
             self.write(k, v)
+
+
+def ensemble_sizes(count: int, seed: int, lo: int = 256, hi: int = 2048, step: int = 32):
+    """Instance sizes (n0, n1) drawn uniformly from the multiples of `step` in
+    [lo, hi] with the library's counter hash: n = step * (lo/step + h % m)."""
+    def mix(z):
+        z &= (1 << 64) - 1
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & ((1 << 64) - 1)
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & ((1 << 64) - 1)
+        return z ^ (z >> 31)
+    m = (hi - lo) // step + 1
+    out = []
+    for k in range(count):
+        h0 = mix(mix(seed) + (2 * k) * 0x9E3779B97F4A7C15)
+        h1 = mix(mix(seed) + (2 * k + 1) * 0x9E3779B97F4A7C15)
+        out.append((lo + step * (h0 % m), lo + step * (h1 % m)))
+    return out
+
+
+class Ensemble:
+    """Batched Hydro: independent periodic grids of uneven sizes, one
+    persistent launch per step (om_ensemble_* of include/om_gb300.h)."""
+
+    FIELDS = ("density", "velocity0", "velocity1", "pressure")
+
+    def __init__(self, sizes, config: Config | None = None, **kw):
+        L = load_library()
+        self._L = L
+        cfg = config if config is not None else default_config(**kw)
+        self.sizes = [(int(a), int(b)) for a, b in sizes]
+        flat = (C.c_int * (2 * len(self.sizes)))(*[v for s in self.sizes for v in s])
+        h = C.c_void_p()
+        _check(L.om_ensemble_create(len(self.sizes), flat, C.byref(cfg), C.byref(h)))
+        self._h = h
+        self.config = cfg
+        self.dtype = np.float64 if cfg.precision == 64 else np.float32
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.om_ensemble_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self):
+        c, t, g, w = C.c_int(), C.c_longlong(), C.c_int(), C.c_int()
+        _check(self._L.om_ensemble_info(self._h, C.byref(c), C.byref(t), C.byref(g), C.byref(w)))
+        return {"count": c.value, "cells": t.value, "grid": g.value, "work_items": w.value}
+
+    def init_kh(self, base_seed: int) -> None:
+        _check(self._L.om_ensemble_init_kh(self._h, C.c_uint64(base_seed)))
+
+    def step(self, n: int = 1) -> None:
+        _check(self._L.om_ensemble_step(self._h, int(n)))
+
+    def time_step(self, n: int) -> float:
+        ms = C.c_float()
+        _check(self._L.om_ensemble_time_step(self._h, int(n), C.byref(ms)))
+        return ms.value
+
+    def read(self, k: int, field: str) -> np.ndarray:
+        n0, n1 = self.sizes[k]
+        out = np.empty((n1, n0), self.dtype)
+        _check(self._L.om_ensemble_read(self._h, k, field.encode(), out.ctypes.data, out.nbytes))
+        return out
+
+    def write(self, k: int, field: str, values) -> None:
+        n0, n1 = self.sizes[k]
+        a = np.ascontiguousarray(values, self.dtype).reshape(n1, n0)
+        _check(self._L.om_ensemble_write(self._h, k, field.encode(), a.ctypes.data, a.nbytes))
+
+    def state(self, k: int):
+        return tuple(self.read(k, f) for f in self.FIELDS)
+
+    def set_state(self, k: int, st) -> None:
+        for f, v in zip(self.FIELDS, st):
+            self.write(k, f, v)
+
+    def scalar(self, k: int, name: str) -> float:
+        v = C.c_double()
+        _check(self._L.om_ensemble_scalar(self._h, k, name.encode(), C.byref(v)))
+        return v.value
+
+    def set_scalar(self, k: int, name: str, value: float) -> None:
+        _check(self._L.om_ensemble_set_scalar(self._h, k, name.encode(), float(value)))
+
+    def totals(self, k: int) -> np.ndarray:
+        out = np.zeros(4, np.float64)
+        _check(self._L.om_ensemble_totals(self._h, k, out.ctypes.data))
+        return out
+
+    def last_launch_count(self) -> int:
+        v = C.c_int()
+        _check(self._L.om_ensemble_last_launch_count(self._h, C.byref(v)))
+        return v.value
