@@ -153,6 +153,23 @@ om_status om_hydro_totals(om_handle h, double *out);
 /* Hydro: dt of each step of the last om_run / om_run_n. */
 om_status om_hydro_dt_history(om_handle h, double *out, int n, int *written);
 
+/* ---- adjoint (no counterpart in the reference) -------------------------- */
+
+/* One reverse-mode step at the handle's current state: cot_next[4] (device
+ * arrays, memory-sized: cotangent of density, velocity0, velocity1, pressure
+ * after one proceed) -> cot_prev[4] (cotangent of the current state),
+ * through both stages, MUSCL-minmod, HLLC, the clamps and the step's CFL dt
+ * (routed to the arg-min cell of the timescale). */
+om_status om_hydro_vjp(om_handle h, void *const *cot_next, void *const *cot_prev);
+/* Gradient of loss = mean((density_T - target)^2) over `steps` proceed
+ * steps from the current state, w.r.t. that state (grad[4]: host or device
+ * arrays), with checkpoints every `checkpoint_every` steps (0: sqrt(steps)).
+ * The handle ends at the final state; *loss receives the loss. */
+om_status om_hydro_adjoint_run(om_handle h, int steps, const void *target,
+                               int checkpoint_every, double *loss, void *const *grad);
+/* Device time of one adjoint step at the current state (ms, mean of reps). */
+om_status om_hydro_time_vjp(om_handle h, int reps, float *ms);
+
 /* ---- measurement ------------------------------------------------------- */
 
 /* Runs a kernel n times inside CUDA events on the handle's stream and
@@ -168,6 +185,17 @@ om_status om_profile_enable(om_handle h, int enable);
  * launches, summed device milliseconds and summed work units (cell-updates). */
 om_status om_profile_query(om_handle h, const char *kernel, long *launches,
                            double *total_ms, double *total_units);
+
+/* ---- autotuning (replaces the reference's genetic-algorithm tuning loop,
+ * Language/Paraiso/Tuning/Genetic.hs) ------------------------------------ */
+
+/* Times every candidate of a small grid of launch knobs on a mesh of this
+ * size and returns the fastest configuration (and its cell-updates/s).
+ * Life: kernel family, temporal depth, block rows; Hydro: fused tile shape.
+ * `base` fixes everything else (boundary, precision, gamma, device).
+ * Results are cached per (kind, size, precision, device) in the process. */
+om_status om_autotune(int kind, int ndim, const int *sizes, const om_config *base,
+                      om_config *best, double *best_rate);
 
 /* ---- batched Hydro ensembles (no counterpart in the reference) ---------- */
 
@@ -201,6 +229,9 @@ om_status om_ensemble_set_scalar(om_ensemble e, int k, const char *name, double 
 /* Compensated FP64 totals (mass, momentum x/y, energy) of instance k. */
 om_status om_ensemble_totals(om_ensemble e, int k, double *out);
 om_status om_ensemble_last_launch_count(om_ensemble e, int *launches);
+/* Autotune the ensemble's tile shape for these instance sizes. */
+om_status om_autotune_ensemble(int count, const int *sizes, const om_config *base,
+                               om_config *best, double *best_rate);
 
 /* ---- caller-owned buffers, no allocation -------------------------------- */
 

@@ -200,6 +200,16 @@ static uint64_t hydro_state_key(Handle *h) {
   return (valid ? 1 : 0) | (uint64_t)st->slot << 1;
 }
 
+static void hydro_restore_key(Handle *h, uint64_t key) {
+  HydroState *st = hst(h);
+  st->ts_valid = (key & 1) != 0;
+  st->slot = (int)((key >> 1) & 1);
+  if (st->ts_valid) {
+    st->ts_dR0 = hsc_host(h)->dR0;
+    st->ts_dR1 = hsc_host(h)->dR1;
+  }
+}
+
 static bool hydro_graph_ok(Handle *h, int kernel_id) {
   (void)kernel_id;
   return hst(h)->variant != 1;  // the plain path round-trips to the host
@@ -225,9 +235,12 @@ static void hydro_array_written(Handle *h, Array *a) {
   hst(h)->ts_valid = false;
 }
 
+void adjoint_release(Handle *h);
+
 static void hydro_free(Handle *h) {
   HydroState *st = hst(h);
   if (!st) return;
+  adjoint_release(h);
   cudaFree(st->d_dt);
   cudaFree(st->d_ts);
   cudaFree(st->d_min);
@@ -237,6 +250,90 @@ static void hydro_free(Handle *h) {
   if (st->h_totals) cudaFreeHost(st->h_totals);
   delete st;
   h->impl = nullptr;
+}
+
+// dt of the next step and the CFL minimum bits of the current state
+om_status hydro_current_dt(Handle *h, double *dt, unsigned long long *bits) {
+  HydroState *st = hst(h);
+  OM_TRY(upload_scalars(h));
+  OM_TRY(ensure_tsmin(h));
+  unsigned long long b = 0;
+  OM_CUDA_CHECK(cudaMemcpyAsync(&b, &hsc_dev(h)->tsmin[st->slot], sizeof(b),
+                                cudaMemcpyDeviceToHost, h->stream));
+  OM_CUDA_CHECK(cudaStreamSynchronize(h->stream));
+  // keep the host mirror's copy of the slot consistent with the device
+  hsc_host(h)->tsmin[st->slot] = b;
+  const double cfl = hsc_host(h)->cfl;
+  if (st->fp64) {
+    double t;
+    std::memcpy(&t, &b, sizeof(t));
+    *dt = cfl * t;
+  } else {
+    const uint32_t lo = (uint32_t)b;
+    float t;
+    std::memcpy(&t, &lo, sizeof(t));
+    *dt = (double)((float)cfl * t);
+  }
+  *bits = b;
+  return OM_OK;
+}
+
+struct HydroCkState {
+  bool ts_valid;
+  int slot;
+  double ts_dR0, ts_dR1;
+};
+static_assert(sizeof(HydroCkState) <= 64, "checkpoint bookkeeping size");
+
+om_status hydro_checkpoint_alloc(Handle *h, HydroCheckpoint *c) {
+  const size_t bytes = h->memory_size_total() * h->arrays[0].elem_size;
+  for (int i = 0; i < 4; ++i)
+    if (cudaMalloc(&c->f[i], bytes) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("Hydro checkpoint allocation failed");
+      return OM_ERR_NOMEM;
+    }
+  return OM_OK;
+}
+
+void hydro_checkpoint_free(HydroCheckpoint *c) {
+  for (int i = 0; i < 4; ++i) {
+    if (c->f[i]) cudaFree(c->f[i]);
+    c->f[i] = nullptr;
+  }
+}
+
+om_status hydro_save(Handle *h, HydroCheckpoint *c) {
+  const size_t bytes = h->memory_size_total() * h->arrays[0].elem_size;
+  for (int i = 0; i < 4; ++i) {
+    OM_TRY(bring_device(h, h->arrays[i]));
+    OM_CUDA_CHECK(cudaMemcpyAsync(c->f[i], h->arrays[i].d(), bytes, cudaMemcpyDeviceToDevice,
+                                  h->stream));
+  }
+  std::memcpy(c->sc, h->h_scalars, sizeof(HydroScalars));
+  HydroState *st = hst(h);
+  HydroCkState k{st->ts_valid, st->slot, st->ts_dR0, st->ts_dR1};
+  std::memcpy(c->state, &k, sizeof(k));
+  return OM_OK;
+}
+
+om_status hydro_restore(Handle *h, const HydroCheckpoint *c) {
+  const size_t bytes = h->memory_size_total() * h->arrays[0].elem_size;
+  for (int i = 0; i < 4; ++i) {
+    OM_CUDA_CHECK(cudaMemcpyAsync(h->arrays[i].d(), c->f[i], bytes, cudaMemcpyDeviceToDevice,
+                                  h->stream));
+    h->arrays[i].newer = h->arrays[i].host ? Newer::kDevice : Newer::kBoth;
+  }
+  std::memcpy(h->h_scalars, c->sc, sizeof(HydroScalars));
+  OM_TRY(upload_scalars(h));
+  HydroState *st = hst(h);
+  HydroCkState k;
+  std::memcpy(&k, c->state, sizeof(k));
+  st->ts_valid = k.ts_valid;
+  st->slot = k.slot;
+  st->ts_dR0 = k.ts_dR0;
+  st->ts_dR1 = k.ts_dR1;
+  return OM_OK;
 }
 
 om_status hydro_setup(Handle *h) {
@@ -264,6 +361,7 @@ om_status hydro_setup(Handle *h) {
   h->impl_free = hydro_free;
   h->ops.state_key = hydro_state_key;
   h->ops.after_replay = hydro_after_replay;
+  h->ops.restore_key = hydro_restore_key;
   h->ops.array_written = hydro_array_written;
   h->ops.reserve = hydro_reserve;
   h->ops.graph_ok = hydro_graph_ok;

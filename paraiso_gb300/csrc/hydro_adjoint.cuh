@@ -1,0 +1,374 @@
+// hydro_adjoint.cuh -- reverse-mode (adjoint) rules of the examples/Hydro
+// scheme pieces in hydro_scheme.cuh.  Each *_rev function recomputes what it
+// needs of its forward and adds input cotangents (accumulating with +=) from
+// output cotangents.  Branch decisions (HLLC case, minmod pick, max clamps,
+// hllcQ case, CFL min) are those of the forward; the derivative follows the
+// branch taken, as finite differences do away from the switching points.
+#pragma once
+
+#include "hydro_scheme.cuh"
+
+namespace om {
+namespace ha {
+
+using hs::Flux;
+using hs::Prim;
+
+// cotangents of a primitive record
+template <class R> struct PrimBar {
+  R rho, v0, v1, p;
+};
+
+template <class R> __device__ __forceinline__ void zero(PrimBar<R> &a) {
+  a.rho = a.v0 = a.v1 = a.p = R(0);
+}
+
+// c = sqrt(g p / rho): cotangent cb -> (rho, p)
+template <class R>
+__device__ __forceinline__ void sound_rev(R g, R rho, R p, R c, R cb, R &rhob, R &pb) {
+  if (cb == R(0)) return;
+  const R tb = cb / (R(2) * c);
+  pb += tb * g / rho;
+  rhob -= tb * (g * p / rho) / rho;
+}
+
+// kinetic energy 0.5 (v0 m0 + v1 m1)
+template <class R>
+__device__ __forceinline__ void kinetic_rev(R v0, R v1, R m0, R m1, R keb, R &v0b, R &v1b,
+                                            R &m0b, R &m1b) {
+  const R h = R(0.5) * keb;
+  v0b += h * m0;
+  v1b += h * m1;
+  m0b += h * v0;
+  m1b += h * v1;
+}
+
+// flux_prim<AX> reverse: fb -> (rho, v0, v1, p)
+template <int AX, class R>
+__device__ __forceinline__ void flux_prim_rev(R g, R rho, R v0, R v1, R p, const Flux<R> &fb,
+                                              PrimBar<R> &xb) {
+  const R m0 = rho * v0, m1 = rho * v1;
+  const R e = hs::kinetic(v0, v1, m0, m1) + (R(1) / (g - R(1))) * p;
+  const R h = e + p;
+  const R va = AX == 0 ? v0 : v1;
+  R m0b = 0, m1b = 0, vab = 0, v0b = 0, v1b = 0, pb = 0;
+  if (AX == 0) m0b += fb.fd; else m1b += fb.fd;
+  m0b += fb.fm0 * va;
+  m1b += fb.fm1 * va;
+  vab += fb.fm0 * m0 + fb.fm1 * m1;
+  pb += AX == 0 ? fb.fm0 : fb.fm1;
+  const R hb = fb.fe * va;
+  vab += fb.fe * h;
+  const R eb = hb;
+  pb += hb;
+  pb += eb / (g - R(1));
+  kinetic_rev(v0, v1, m0, m1, eb, v0b, v1b, m0b, m1b);
+  if (AX == 0) v0b += vab; else v1b += vab;
+  xb.rho += m0b * v0 + m1b * v1;
+  xb.v0 += v0b + m0b * rho;
+  xb.v1 += v1b + m1b * rho;
+  xb.p += pb;
+}
+
+// flux_cons<AX> reverse: fb -> (rho, m0, m1, e)
+template <int AX, class R>
+__device__ __forceinline__ void flux_cons_rev(R g, R rho, R m0, R m1, R e, const Flux<R> &fb,
+                                              R &rhob, R &m0b, R &m1b, R &eb) {
+  const R v0 = m0 / rho, v1 = m1 / rho;
+  const R p = (g - R(1)) * (e - hs::kinetic(v0, v1, m0, m1));
+  const R h = e + p;
+  const R va = AX == 0 ? v0 : v1;
+  R v0b = 0, v1b = 0, pb = 0, vab = 0;
+  if (AX == 0) m0b += fb.fd; else m1b += fb.fd;
+  m0b += fb.fm0 * va;
+  m1b += fb.fm1 * va;
+  vab += fb.fm0 * m0 + fb.fm1 * m1;
+  pb += AX == 0 ? fb.fm0 : fb.fm1;
+  const R hb = fb.fe * va;
+  vab += fb.fe * h;
+  eb += hb;
+  pb += hb;
+  eb += (g - R(1)) * pb;
+  const R keb = -(g - R(1)) * pb;
+  kinetic_rev(v0, v1, m0, m1, keb, v0b, v1b, m0b, m1b);
+  if (AX == 0) v0b += vab; else v1b += vab;
+  m0b += v0b / rho;
+  m1b += v1b / rho;
+  rhob -= (v0b * v0 + v1b * v1) / rho;
+}
+
+// star_flux<AX> reverse: fb -> (sstar, shock, rho, v0, v1, p)
+template <int AX, class R>
+__device__ __forceinline__ void star_flux_rev(R g, R sstar, R shock, R rho, R v0, R v1, R p,
+                                              const Flux<R> &fb, R &sstarb, R &shockb,
+                                              PrimBar<R> &xb) {
+  const R speed = AX == 0 ? v0 : v1;
+  const R su = shock - speed, ss = shock - sstar;
+  const R dens = rho * su / ss;
+  const R mome0 = dens * (AX == 0 ? sstar : v0);
+  const R mome1 = dens * (AX == 1 ? sstar : v1);
+  const R m0 = rho * v0, m1 = rho * v1;
+  const R e = hs::kinetic(v0, v1, m0, m1) + (R(1) / (g - R(1))) * p;
+  const R pr = p / rho;
+  const R w = pr / su;
+  const R z = sstar + w;
+  const R y = (sstar - speed) * z;
+  const R x = e / rho + y;
+  const R enrg = dens * x;
+  R densb = 0, mome0b = 0, mome1b = 0, enrgb = 0;
+  flux_cons_rev<AX>(g, dens, mome0, mome1, enrg, fb, densb, mome0b, mome1b, enrgb);
+  R rhob = 0, v0b = 0, v1b = 0, pb = 0, sub = 0, ssb = 0, speedb = 0;
+  densb += enrgb * x;
+  const R xbar = enrgb * dens;
+  const R ebar = xbar / rho;
+  rhob -= xbar * e / rho / rho;
+  const R ybar = xbar;
+  sstarb += ybar * z;
+  speedb -= ybar * z;
+  const R zbar = ybar * (sstar - speed);
+  sstarb += zbar;
+  const R wbar = zbar;
+  const R prb = wbar / su;
+  sub -= wbar * w / su;
+  pb += prb / rho;
+  rhob -= prb * pr / rho;
+  pb += ebar / (g - R(1));
+  R m0b = 0, m1b = 0;
+  kinetic_rev(v0, v1, m0, m1, ebar, v0b, v1b, m0b, m1b);
+  rhob += m0b * v0 + m1b * v1;
+  v0b += m0b * rho;
+  v1b += m1b * rho;
+  if (AX == 0) {
+    densb += mome0b * sstar;
+    sstarb += mome0b * dens;
+    densb += mome1b * v1;
+    v1b += mome1b * dens;
+  } else {
+    densb += mome0b * v0;
+    v0b += mome0b * dens;
+    densb += mome1b * sstar;
+    sstarb += mome1b * dens;
+  }
+  rhob += densb * su / ss;
+  sub += densb * rho / ss;
+  ssb -= densb * dens / ss;
+  shockb += sub;
+  speedb -= sub;
+  shockb += ssb;
+  sstarb -= ssb;
+  if (AX == 0) v0b += speedb; else v1b += speedb;
+  xb.rho += rhob;
+  xb.v0 += v0b;
+  xb.v1 += v1b;
+  xb.p += pb;
+}
+
+// hllcQ reverse: cotangent of q -> (sp, p)
+template <class R>
+__device__ __forceinline__ void hllc_q_rev(R g, R sp, R p, R qb, R &spb, R &pb) {
+  if (p <= sp) return;  // constant branch
+  const R k = (g + R(1)) / (R(2) * g);
+  const R t = R(1) + k * (sp / p - R(1));
+  const R q = sqrt(t);
+  const R tb = qb / (R(2) * q);
+  spb += tb * k / p;
+  pb -= tb * k * sp / p / p;
+}
+
+// hllc<AX> reverse: cotangent of the wall fluxes -> cotangents of the two
+// primitive states (the sound speeds' dependence on them included).
+template <int AX, class R>
+__device__ __forceinline__ void hllc_rev(R g, const Prim<R> &L, const Prim<R> &Rt,
+                                         const Flux<R> &fb, PrimBar<R> &Lb, PrimBar<R> &Rb) {
+  const R cl = hs::sound(g, L.rho, L.p), cr = hs::sound(g, Rt.rho, Rt.p);
+  const R densMid = (L.rho + Rt.rho) / R(2);
+  const R soundMid = (cl + cr) / R(2);
+  const R uL = AX == 0 ? L.v0 : L.v1;
+  const R uR = AX == 0 ? Rt.v0 : Rt.v1;
+  const R psraw = (L.p + Rt.p) / R(2) - densMid * soundMid * (uR - uL);
+  const R presStar = hs::omax(R(0), psraw);
+  const R qL = hs::hllc_q(g, presStar, L.p), qR = hs::hllc_q(g, presStar, Rt.p);
+  const R shockLeft = uL - cl * qL;
+  const R shockRight = uR + cr * qR;
+  const R num = Rt.p - L.p + L.rho * uL * (shockLeft - uL) - Rt.rho * uR * (shockRight - uR);
+  const R den = L.rho * (shockLeft - uL) - Rt.rho * (shockRight - uR);
+  const R shockStar = num / den;
+  const bool posL = R(0) < shockLeft, posS = R(0) < shockStar, posR = R(0) < shockRight;
+  const bool useL = posL || posS;
+  const bool star = useL ? !posL : posR;
+  const Prim<R> &X = useL ? L : Rt;
+  PrimBar<R> &Xb = useL ? Lb : Rb;
+  if (!star) {
+    flux_prim_rev<AX>(g, X.rho, X.v0, X.v1, X.p, fb, Xb);
+    return;
+  }
+  const R shock = useL ? shockLeft : shockRight;
+  R sstarb = 0, shockb = 0;
+  star_flux_rev<AX>(g, shockStar, shock, X.rho, X.v0, X.v1, X.p, fb, sstarb, shockb, Xb);
+  R SLb = useL ? shockb : R(0), SRb = useL ? R(0) : shockb;
+  R rhoLb = 0, rhoRb = 0, uLb = 0, uRb = 0, pLb = 0, pRb = 0, clb = 0, crb = 0;
+  // shockStar = num / den
+  const R numb = sstarb / den;
+  const R denb = -sstarb * shockStar / den;
+  pRb += numb;
+  pLb -= numb;
+  rhoLb += numb * uL * (shockLeft - uL);
+  uLb += numb * L.rho * (shockLeft - uL);
+  {
+    const R t = numb * L.rho * uL;
+    SLb += t;
+    uLb -= t;
+  }
+  rhoRb -= numb * uR * (shockRight - uR);
+  uRb -= numb * Rt.rho * (shockRight - uR);
+  {
+    const R t = -numb * Rt.rho * uR;
+    SRb += t;
+    uRb -= t;
+  }
+  rhoLb += denb * (shockLeft - uL);
+  SLb += denb * L.rho;
+  uLb -= denb * L.rho;
+  rhoRb -= denb * (shockRight - uR);
+  SRb -= denb * Rt.rho;
+  uRb += denb * Rt.rho;
+  // shock speeds
+  uLb += SLb;
+  clb -= SLb * qL;
+  const R qLb = -SLb * cl;
+  uRb += SRb;
+  crb += SRb * qR;
+  const R qRb = SRb * cr;
+  R psb = 0;
+  hllc_q_rev(g, presStar, L.p, qLb, psb, pLb);
+  hllc_q_rev(g, presStar, Rt.p, qRb, psb, pRb);
+  const R psrawb = (R(0) < psraw) ? psb : R(0);
+  pLb += psrawb / R(2);
+  pRb += psrawb / R(2);
+  const R dmb = -psrawb * soundMid * (uR - uL);
+  const R smb = -psrawb * densMid * (uR - uL);
+  uRb -= psrawb * densMid * soundMid;
+  uLb += psrawb * densMid * soundMid;
+  rhoLb += dmb / R(2);
+  rhoRb += dmb / R(2);
+  clb += smb / R(2);
+  crb += smb / R(2);
+  sound_rev(g, L.rho, L.p, cl, clb, rhoLb, pLb);
+  sound_rev(g, Rt.rho, Rt.p, cr, crb, rhoRb, pRb);
+  Lb.rho += rhoLb;
+  Lb.p += pLb;
+  Rb.rho += rhoRb;
+  Rb.p += pRb;
+  if (AX == 0) {
+    Lb.v0 += uLb;
+    Rb.v0 += uRb;
+  } else {
+    Lb.v1 += uLb;
+    Rb.v1 += uRb;
+  }
+}
+
+// minmod MUSCL reverse for one field: (lb, rb) -> x0..x3
+template <class R>
+__device__ __forceinline__ void muscl_rev(R x0, R x1, R x2, R x3, R lb, R rb, R &x0b, R &x1b,
+                                          R &x2b, R &x3b) {
+  const R d01 = x1 - x0, d12 = x2 - x1, d23 = x3 - x2;
+  x1b += lb;
+  x2b += rb;
+  const R d1b = lb / R(2), d2b = -rb / R(2);
+  R d01b = 0, d12b = 0, d23b = 0;
+  if (!(d01 * d12 <= R(0))) {
+    if (fabs(d01) < fabs(d12)) d01b += d1b; else d12b += d1b;
+  }
+  if (!(d12 * d23 <= R(0))) {
+    if (fabs(d12) < fabs(d23)) d12b += d2b; else d23b += d2b;
+  }
+  x1b += d01b;
+  x0b -= d01b;
+  x2b += d12b;
+  x1b -= d12b;
+  x3b += d23b;
+  x2b -= d23b;
+}
+
+// Conserved-state cotangent Ub (rho, m0, m1, E) of the update's output, from
+// the primitive cotangent qb of update(): reverse of the clamps, velocity
+// division and pressure recovery.  d2, b0, b1, e2: the new conserved state.
+template <class R>
+__device__ __forceinline__ void cons_from_prim_rev(R g, R d2, R b0, R b1, R e2,
+                                                   const PrimBar<R> &qb, R Ub[4]) {
+  const R v0 = b0 / d2, v1 = b1 / d2;
+  const R pn = (g - R(1)) * (e2 - hs::kinetic(v0, v1, b0, b1));
+  R d2b = (R(1e-2) < d2) ? qb.rho : R(0);
+  const R pnb = (R(1e-2) < pn) ? qb.p : R(0);
+  R v0b = qb.v0, v1b = qb.v1, b0b = 0, b1b = 0;
+  const R e2b = (g - R(1)) * pnb;
+  const R keb = -(g - R(1)) * pnb;
+  kinetic_rev(v0, v1, b0, b1, keb, v0b, v1b, b0b, b1b);
+  b0b += v0b / d2;
+  b1b += v1b / d2;
+  d2b -= (v0b * v0 + v1b * v1) / d2;
+  Ub[0] = d2b;
+  Ub[1] = b0b;
+  Ub[2] = b1b;
+  Ub[3] = e2b;
+}
+
+// Reverse of the conserved record of a primitive base state, cons(b):
+// Ub (rho, m0, m1, E) -> bb
+template <class R>
+__device__ __forceinline__ void cons_of_prim_rev(R g, const Prim<R> &b, const R Ub[4],
+                                                 PrimBar<R> &bb) {
+  const R m0 = b.rho * b.v0, m1 = b.rho * b.v1;
+  R rhob = Ub[0], m0b = Ub[1], m1b = Ub[2], v0b = 0, v1b = 0;
+  const R eb = Ub[3];
+  bb.p += eb / (g - R(1));
+  kinetic_rev(b.v0, b.v1, m0, m1, eb, v0b, v1b, m0b, m1b);
+  rhob += m0b * b.v0 + m1b * b.v1;
+  v0b += m0b * b.rho;
+  v1b += m1b * b.rho;
+  bb.rho += rhob;
+  bb.v0 += v0b;
+  bb.v1 += v1b;
+}
+
+// The update's new conserved state (d2, b0, b1, e2) before the primitive
+// recovery, with the same operation order as hs::update.
+template <class R>
+__device__ __forceinline__ void update_cons(R g, const Prim<R> &b, R dtdx0, R dtdx1,
+                                            const Flux<R> &l0, const Flux<R> &r0,
+                                            const Flux<R> &l1, const Flux<R> &r1, R out[4]) {
+  const R m0 = b.rho * b.v0, m1 = b.rho * b.v1;
+  const R e = hs::kinetic(b.v0, b.v1, m0, m1) + (R(1) / (g - R(1))) * b.p;
+  const R d1 = b.rho + dtdx1 * (l1.fd - r1.fd);
+  const R a0 = m0 + dtdx1 * (l1.fm0 - r1.fm0);
+  const R a1 = m1 + dtdx1 * (l1.fm1 - r1.fm1);
+  const R e1 = e + dtdx1 * (l1.fe - r1.fe);
+  out[0] = d1 + dtdx0 * (l0.fd - r0.fd);
+  out[1] = a0 + dtdx0 * (l0.fm0 - r0.fm0);
+  out[2] = a1 + dtdx0 * (l0.fm1 - r0.fm1);
+  out[3] = e1 + dtdx0 * (l0.fe - r0.fe);
+}
+
+// timescale reverse at one cell: tb -> (rho, v0, v1, p)
+template <class R>
+__device__ __forceinline__ void timescale_rev(R g, R dR0, R dR1, const Prim<R> &x, R tb,
+                                              PrimBar<R> &xb) {
+  const R c = hs::sound(g, x.rho, x.p);
+  const R s0 = c + fabs(x.v0), s1 = c + fabs(x.v1);
+  const R t0 = dR0 / s0, t1 = dR1 / s1;
+  R cb = 0;
+  if (t1 < t0) {
+    const R s1b = -tb * t1 / s1;
+    cb += s1b;
+    xb.v1 += s1b * (x.v1 < R(0) ? R(-1) : R(1));
+  } else {
+    const R s0b = -tb * t0 / s0;
+    cb += s0b;
+    xb.v0 += s0b * (x.v0 < R(0) ? R(-1) : R(1));
+  }
+  sound_rev(g, x.rho, x.p, c, cb, xb.rho, xb.p);
+}
+
+}  // namespace ha
+}  // namespace om

@@ -5,6 +5,7 @@
 
 #include <cuda_runtime.h>
 
+#include "../../include/om_gb300.h"
 #include "hydro_kernels.cuh"
 
 namespace om {
@@ -54,5 +55,21 @@ cudaError_t hydro_init_kh(int fp64, void *rho, void *v0, void *v1, void *p, int 
 cudaError_t hydro_totals(int fp64, const void *rho, const void *v0, const void *v1,
                          const void *p, size_t n, double gamma, double *partials, int blocks,
                          double *out, cudaStream_t s);
+
+// A saved Hydro state (hydro.cu): the four arrays (device copies), the
+// scalar block and the cached-minimum bookkeeping, so that a restore
+// continues bit-identically.  Used by the adjoint's checkpointing.
+struct Handle;
+struct HydroCheckpoint {
+  void *f[4] = {nullptr, nullptr, nullptr, nullptr};
+  unsigned char sc[sizeof(HydroScalars)];
+  unsigned char state[64];
+};
+om_status hydro_checkpoint_alloc(Handle *h, HydroCheckpoint *c);
+void hydro_checkpoint_free(HydroCheckpoint *c);
+om_status hydro_save(Handle *h, HydroCheckpoint *c);
+om_status hydro_restore(Handle *h, const HydroCheckpoint *c);
+// dt of the next step and the CFL minimum bits of the current state
+om_status hydro_current_dt(Handle *h, double *dt, unsigned long long *bits);
 
 }  // namespace om

@@ -1039,6 +1039,8 @@ static void life_after_replay(Handle *h, int kernel_id, int n) {
   }
 }
 
+static void life_restore_key(Handle *h, uint64_t key) { life_state(h)->binary = key != 0; }
+
 static void life_array_written(Handle *h, Array *a) {
   (void)a;
   life_state(h)->binary = false;
@@ -1088,6 +1090,7 @@ om_status life_setup(Handle *h) {
   h->impl_free = life_free;
   h->ops.state_key = life_state_key;
   h->ops.after_replay = life_after_replay;
+  h->ops.restore_key = life_restore_key;
   h->ops.array_written = life_array_written;
   h->ops.reserve = life_reserve;
   OM_TRY(alloc_array(h, "cell", sizeof(int32_t)));

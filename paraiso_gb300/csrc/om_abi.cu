@@ -365,7 +365,8 @@ om_status om_run_n(om_handle H, int kernel_id, int n) {
   uint64_t mask = 0;
   for (size_t i = 0; i < h->arrays.size(); ++i)
     mask |= (uint64_t)h->arrays[i].cur << i;
-  const uint64_t key2 = mask ^ ((h->ops.state_key ? h->ops.state_key(h) : 0) << 32);
+  const uint64_t skey = h->ops.state_key ? h->ops.state_key(h) : 0;
+  const uint64_t key2 = mask ^ (skey << 32);
   auto key = std::make_tuple(kernel_id, n, key2);
   auto it = H->graphs.find(key);
   if (it == H->graphs.end()) {
@@ -393,6 +394,7 @@ om_status om_run_n(om_handle H, int kernel_id, int n) {
     // replay below applies it once
     for (size_t i = 0; i < h->arrays.size(); ++i)
       h->arrays[i].cur = (int)((mask >> i) & 1);
+    if (h->ops.restore_key) h->ops.restore_key(h, skey);
     it = H->graphs.emplace(key, e).first;
   }
   OM_CUDA_CHECK(cudaGraphLaunch(it->second.exec, h->stream));

@@ -69,6 +69,9 @@ struct KindOps {
   uint64_t (*state_key)(Handle *) = nullptr;
   // apply the host-side effects of a run whose graph was replayed
   void (*after_replay)(Handle *, int kernel_id, int n) = nullptr;
+  // put back the host-side state described by a state_key (capturing a run
+  // executes its host bookkeeping once; the replay applies it again)
+  void (*restore_key)(Handle *, uint64_t key) = nullptr;
   // an array's contents were replaced from outside (host mirror or copy)
   void (*array_written)(Handle *, Array *) = nullptr;
   // allocate whatever a run of n steps needs, before any stream capture

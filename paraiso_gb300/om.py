@@ -39,7 +39,8 @@ EXPORTS = [
     "om_ensemble_create", "om_ensemble_destroy", "om_ensemble_info", "om_ensemble_init_kh",
     "om_ensemble_step", "om_ensemble_time_step", "om_ensemble_read", "om_ensemble_write",
     "om_ensemble_scalar", "om_ensemble_set_scalar", "om_ensemble_totals",
-    "om_ensemble_last_launch_count", "om_life_proceed_noalloc",
+    "om_ensemble_last_launch_count", "om_life_proceed_noalloc", "om_autotune",
+    "om_autotune_ensemble", "om_hydro_vjp", "om_hydro_adjoint_run", "om_hydro_time_vjp",
 ]
 
 
@@ -108,6 +109,13 @@ def load_library(path: str | None = None) -> C.CDLL:
         "om_ensemble_set_scalar": (i, [vp, i, C.c_char_p, C.c_double]),
         "om_ensemble_totals": (i, [vp, i, vp]),
         "om_ensemble_last_launch_count": (i, [vp, ip]),
+        "om_autotune": (i, [i, i, ip, C.POINTER(Config), C.POINTER(Config),
+                            C.POINTER(C.c_double)]),
+        "om_autotune_ensemble": (i, [i, ip, C.POINTER(Config), C.POINTER(Config),
+                                     C.POINTER(C.c_double)]),
+        "om_hydro_vjp": (i, [vp, C.POINTER(vp), C.POINTER(vp)]),
+        "om_hydro_adjoint_run": (i, [vp, i, vp, i, C.POINTER(C.c_double), C.POINTER(vp)]),
+        "om_hydro_time_vjp": (i, [vp, i, C.POINTER(C.c_float)]),
         "om_profile_query": (i, [vp, C.c_char_p, C.POINTER(C.c_long), C.POINTER(C.c_double),
                                  C.POINTER(C.c_double)]),
     }
@@ -348,6 +356,42 @@ class Hydro(OrthotopeMachine):
     def state(self) -> tuple[np.ndarray, ...]:
         return tuple(self.read(k) for k in ("density", "velocity0", "velocity1", "pressure"))
 
+    # -- adjoint (om_hydro_vjp / om_hydro_adjoint_run)
+    def _dev(self, arrays):
+        import torch
+        dt = torch.float64 if self.config.precision == 64 else torch.float32
+        return [torch.as_tensor(np.ascontiguousarray(a, self.array_dtypes["density"]),
+                                dtype=dt).cuda() for a in arrays]
+
+    def vjp(self, cot_next):
+        """Cotangent of the current state from the cotangent of the state after
+        one proceed (four memory-sized arrays)."""
+        import torch
+        src = self._dev(cot_next)
+        dst = [torch.empty_like(src[0]) for _ in range(4)]
+        torch.cuda.synchronize()
+        a = (C.c_void_p * 4)(*[t.data_ptr() for t in src])
+        b = (C.c_void_p * 4)(*[t.data_ptr() for t in dst])
+        _check(self._L.om_hydro_vjp(self._h, a, b))
+        return tuple(t.cpu().numpy() for t in dst)
+
+    def adjoint_run(self, steps: int, target, checkpoint_every: int = 0):
+        """(loss, gradient) of mean((density_T - target)^2) over `steps` steps
+        w.r.t. the current state; the handle ends at step T."""
+        dt = self.array_dtypes["density"]
+        tgt = np.ascontiguousarray(target, dt)
+        grads = [np.empty(self.memory_shape, dt) for _ in range(4)]
+        ptrs = (C.c_void_p * 4)(*[g.ctypes.data for g in grads])
+        loss = C.c_double()
+        _check(self._L.om_hydro_adjoint_run(self._h, int(steps), tgt.ctypes.data,
+                                            int(checkpoint_every), C.byref(loss), ptrs))
+        return loss.value, tuple(grads)
+
+    def time_vjp(self, reps: int = 5) -> float:
+        ms = C.c_float()
+        _check(self._L.om_hydro_time_vjp(self._h, int(reps), C.byref(ms)))
+        return ms.value
+
     def set_state(self, st) -> None:
         for k, v in zip(("density", "velocity0", "velocity1", "pressure"), st):
             self.write(k, v)
@@ -450,3 +494,26 @@ class Ensemble:
         v = C.c_int()
         _check(self._L.om_ensemble_last_launch_count(self._h, C.byref(v)))
         return v.value
+
+
+def autotune(kind: str, size, **base) -> tuple[Config, float]:
+    """Fastest launch configuration for a Life or Hydro mesh of this size
+    (om_autotune): returns (config, cell-updates/s)."""
+    L = load_library()
+    k = {"life": KIND_LIFE, "hydro": KIND_HYDRO}[kind]
+    cfg = default_config(**base)
+    best = Config()
+    rate = C.c_double()
+    sizes = (C.c_int * 2)(int(size[0]), int(size[1]))
+    _check(L.om_autotune(k, 2, sizes, C.byref(cfg), C.byref(best), C.byref(rate)))
+    return best, rate.value
+
+
+def autotune_ensemble(sizes, **base) -> tuple[Config, float]:
+    L = load_library()
+    cfg = default_config(**base)
+    best = Config()
+    rate = C.c_double()
+    flat = (C.c_int * (2 * len(sizes)))(*[int(v) for s in sizes for v in s])
+    _check(L.om_autotune_ensemble(len(sizes), flat, C.byref(cfg), C.byref(best), C.byref(rate)))
+    return best, rate.value

@@ -148,6 +148,23 @@ def test_graph_replay_and_host_writes(om_lib, oracle):
     h.close()
 
 
+@pytest.mark.parametrize("chunks", [(3, 2), (1, 3, 1, 2), (5, 5, 1)])
+def test_graph_runs_of_odd_length(om_lib, oracle, chunks):
+    # a graph-captured run of odd length leaves the cached CFL minimum in the
+    # other slot; the next run must read it from there
+    size = (48, 32)
+    st = kh_state(oracle, size, 6, np.float64)
+    h = make(om_lib, size, 64, 0)
+    h.set_state(st)
+    for c in chunks:
+        h.proceed(c)
+    ref, t, _ = oracle_run(oracle, st, sum(chunks), size, np.float64)
+    for a, b in zip(h.state(), ref):
+        assert np.array_equal(a, b)
+    assert h.get_scalar("time") == t
+    h.close()
+
+
 def test_init_kernels(om_lib, oracle):
     size = (64, 32)
     h = make(om_lib, size, 64, 0)
