@@ -390,8 +390,13 @@ def ensemble_workload(args, dist: Dist) -> dict:
     pgbuild.build()
     count = args.count
     sizes = pg.ensemble_sizes(count, 1 + dist.rank)
+    tile_x, tile_y, tiles_by = args.tile_x, args.tile_y, "command line"
+    if tile_x == 0 and tile_y == 0:
+        # tile shape picked by the autotuner on these very instance sizes
+        best, _ = pg.autotune_ensemble(sizes, precision=32, gamma=1.4, device=dist.local_rank)
+        tile_x, tile_y, tiles_by = best.tile_x, best.tile_y, "om_autotune_ensemble"
     e = pg.Ensemble(sizes, precision=32, gamma=1.4, device=dist.local_rank,
-                    tile_x=args.tile_x, tile_y=args.tile_y)
+                    tile_x=tile_x, tile_y=tile_y)
     e.init_kh(1000 * (1 + dist.rank))
     info = e.info()
     cells = info["cells"]
@@ -435,6 +440,7 @@ def ensemble_workload(args, dist: Dist) -> dict:
                                "multiples of 32 in [256,2048] (seed 1+rank), one persistent "
                                "launch per step, CUDA graph", "instances": count,
                    "cells": cells, "work_items": info["work_items"], "grid": info["grid"],
+                   "tile": {"tile_x": tile_x, "tile_y": tile_y, "picked_by": tiles_by},
                    "parallelism": f"replicas x{dist.world}"},
         "roofline": {"bound": "hbm", "kernel": "hydro_ensemble_kernel", "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
@@ -450,6 +456,108 @@ def ensemble_workload(args, dist: Dist) -> dict:
         "instance_time_range": [min(times), max(times)],
     }
     e.close()
+    return out
+
+
+def adjoint_target(n: int, seed: int = 7):
+    """Smooth periodic target density: 1.5 + sum of 8 Fourier modes with
+    small integer wave numbers, amplitudes scaled to a total of 0.1."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    x = (np.arange(n) + 0.5) / n
+    X, Y = np.meshgrid(x, x)
+    amps = rng.uniform(0.2, 1.0, 8)
+    amps *= 0.1 / amps.sum()
+    t = np.full((n, n), 1.5)
+    for a in amps:
+        p, q = rng.integers(-4, 5, 2)
+        if p == 0 and q == 0:
+            p = 1
+        t += a * np.sin(2 * np.pi * (p * X + q * Y) + rng.uniform(0, 2 * np.pi))
+    return t
+
+
+def adjoint_workload(args, dist: Dist) -> dict:
+    import numpy as np
+    import paraiso_gb300 as pg
+    from paraiso_gb300 import build as pgbuild
+    pgbuild.build()
+    n = args.size or 1024
+    T = args.adj_steps
+    cells = n * n
+    target = adjoint_target(n)
+    h = pg.Hydro((n, n), precision=args.adj_precision, gamma=1.4, device=dist.local_rank)
+    h.init_kh(1)
+    h.set_scalar("cfl", 0.4)
+    st0 = h.state()
+    if args.tie_noise > 0:
+        # break the ties of the CFL minimum of the Kelvin-Helmholtz start
+        rng0 = np.random.default_rng(99)
+        st0 = tuple(a * (1 + args.tie_noise * rng0.standard_normal(a.shape)).astype(a.dtype)
+                    for a in st0)
+        h.set_state(st0)
+    # forward step and adjoint step, device time on the handle's stream
+    h.proceed(max(args.warmup, 1))
+    fwd_ms = h.time_run("proceed", 20) / 20
+    vjp_ms = h.time_vjp(10)
+    # the full gradient: forward with sqrt(T) checkpoints, recompute, backward
+    h.set_state(st0)
+    h.set_scalar("time", 0.0)
+    t0 = time.perf_counter()
+    loss, grad = h.adjoint_run(T, target.astype(st0[0].dtype))
+    grad_s = time.perf_counter() - t0
+    grad64 = [g.astype(np.float64) for g in grad]
+    h.close()
+    # finite differences with the FP64 forward along seeded directions
+    f64 = pg.Hydro((n, n), precision=64, gamma=1.4, device=dist.local_rank)
+    st64 = tuple(a.astype(np.float64) for a in st0)
+
+    def L(s):
+        f64.set_state(s)
+        f64.set_scalar("time", 0.0)
+        f64.set_scalar("cfl", 0.4)
+        f64.set_scalar("dR0", 1.0 / n)
+        f64.set_scalar("dR1", 1.0 / n)
+        f64.proceed(T)
+        return float(((f64.read("density") - target) ** 2).mean())
+
+    rng = np.random.default_rng(2024)
+    fd_rows = []
+    for k in range(args.fd_dirs):
+        d = [rng.standard_normal((n, n)) * s for s in (0.1, 0.05, 0.05, 0.0)]
+        ad = sum(float((g * b).sum()) for g, b in zip(grad64, d))
+        row = {"ad": ad}
+        for eps in args.fd_eps:
+            lp = L(tuple(a + eps * b for a, b in zip(st64, d)))
+            lm = L(tuple(a - eps * b for a, b in zip(st64, d)))
+            fd = (lp - lm) / (2 * eps)
+            row[f"fd_{eps:g}"] = fd
+            row[f"rel_{eps:g}"] = abs(ad - fd) / max(abs(fd), 1e-300)
+        fd_rows.append(row)
+    f64.close()
+    summary = {}
+    for eps in args.fd_eps:
+        rels = sorted(r[f"rel_{eps:g}"] for r in fd_rows)
+        if not rels:
+            continue
+        summary[f"{eps:g}"] = {"median_rel": rels[len(rels) // 2], "max_rel": rels[-1],
+                               "within_1e-4": sum(x <= 1e-4 for x in rels)}
+    out = {
+        "metric": "Hydro adjoint: adjoint step / forward step time, gradient vs FD",
+        "adjoint_precision": args.adj_precision, "tie_noise": args.tie_noise,
+        "value": round(vjp_ms / fwd_ms, 3), "unit": "adjoint_step/forward_step",
+        "higher_is_better": False, "n_gpus": dist.world, "steps": T, "warmup": args.warmup,
+        "dtype": "f32", "data": "synthetic", "vs_baseline": None, "scaling": "weak",
+        "config": {"workload": f"hydro adjoint {n}x{n} Kelvin-Helmholtz (seed 1), {T} FP32 steps, "
+                               "loss mean((rho_T - target)^2), target 1.5 + 8 Fourier modes "
+                               "(amplitude 0.1), gradient w.r.t. initial rho, vx, vy, p",
+                   "n0": n, "n1": n},
+        "forward_step_ms": round(fwd_ms, 4), "adjoint_step_ms": round(vjp_ms, 4),
+        "gradient_run_s": round(grad_s, 3), "loss": loss,
+        "forward_gcell_s": round(cells / (fwd_ms * 1e-3) / 1e9, 3),
+        "fd": {"directions": args.fd_dirs, "forward": "FP64 fused (bit-exact with the oracle)",
+               "summary": summary, "rows": fd_rows[: min(4, len(fd_rows))]},
+    }
     return out
 
 
@@ -509,14 +617,20 @@ def reference_arm(args, dist: Dist) -> dict | None:
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 1000 for hydro4k, else 200)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="life16k",
-                    choices=["life16k", "life128", "hydro4k", "ensemble"])
+                    choices=["life16k", "life128", "hydro4k", "ensemble", "adjoint"])
+    ap.add_argument("--adj-steps", type=int, default=200)
+    ap.add_argument("--adj-precision", type=int, default=32)
+    ap.add_argument("--tie-noise", type=float, default=0.0)
+    ap.add_argument("--fd-dirs", type=int, default=32)
+    ap.add_argument("--fd-eps", type=float, nargs="+", default=[1e-3, 1e-5, 1e-7])
     ap.add_argument("--count", type=int, default=64)
     ap.add_argument("--seq-instances", type=int, default=16)
-    ap.add_argument("--accuracy-steps", type=int, default=100)
+    ap.add_argument("--accuracy-steps", type=int, default=1000)
     ap.add_argument("--size", type=int, default=0)
     ap.add_argument("--generations", type=int, default=0)
     ap.add_argument("--depth", type=int, default=0)
@@ -526,6 +640,8 @@ def main() -> int:
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 1000 if args.workload == "hydro4k" else 200
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     dist = Dist()
@@ -536,6 +652,8 @@ def main() -> int:
             out = hydro_workload(args, dist)
         elif args.workload == "ensemble":
             out = ensemble_workload(args, dist)
+        elif args.workload == "adjoint":
+            out = adjoint_workload(args, dist)
         else:
             out = life_workload(args, dist)
         if out is not None and dist.rank == 0:

@@ -49,10 +49,30 @@ template <class R> struct Fields {
 template <class R> struct Geo {
   int n0, n1;
   R g, dR0, dR1, dt;
+  const double *dtp;  // the step's dt in device memory (read at kernel start)
+  // periodic index of a cell at most 4 cells outside the mesh
   __device__ __forceinline__ size_t at(int x, int y) const {
-    x %= n0; if (x < 0) x += n0;
-    y %= n1; if (y < 0) y += n1;
+    if (n0 >= 8 && n1 >= 8) {
+      x += x < 0 ? n0 : 0;
+      x -= x >= n0 ? n0 : 0;
+      y += y < 0 ? n1 : 0;
+      y -= y >= n1 ? n1 : 0;
+    } else {
+      x %= n0; if (x < 0) x += n0;
+      y %= n1; if (y < 0) y += n1;
+    }
     return (size_t)y * n0 + x;
+  }
+};
+
+// one stored flux per face and axis: 4 arrays per axis
+template <class R> struct FluxStore {
+  R *f[8];  // axis 0: fd, fm0, fm1, fe; axis 1: fd, fm0, fm1, fe
+  __device__ __forceinline__ Flux<R> get(int ax, size_t i) const {
+    return Flux<R>{f[4 * ax][i], f[4 * ax + 1][i], f[4 * ax + 2][i], f[4 * ax + 3][i]};
+  }
+  __device__ __forceinline__ void set(int ax, size_t i, const Flux<R> &v) const {
+    f[4 * ax][i] = v.fd; f[4 * ax + 1][i] = v.fm0; f[4 * ax + 2][i] = v.fm1; f[4 * ax + 3][i] = v.fe;
   }
 };
 
@@ -96,34 +116,84 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
   return t;
 }
 
-// A: stage-1 state
+// A1: stage-1 walls, one per face and axis (face i: left wall of cell i)
 template <class R>
-__global__ void __launch_bounds__(256) adj_stage1(Fields<R> P, Fields<R> Q, Geo<R> G) {
+__global__ void __launch_bounds__(256)
+adj_walls1(Fields<R> P, FluxStore<R> F1, Geo<R> G, unsigned long long *minbits) {
   const size_t n = (size_t)G.n0 * G.n1;
-  const R h = G.dt / R(2);
-  const R d0 = h / G.dR0, d1 = h / G.dR1;
+  unsigned long long best = ~0ull;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
     const int y = (int)(i / G.n0), x = (int)(i - (size_t)y * G.n0);
-    Q.set(i, hs::update(G.g, P.get(i), d0, d1, wall1<0>(P, G, x, y), wall1<0>(P, G, x + 1, y),
-                        wall1<1>(P, G, x, y), wall1<1>(P, G, x, y + 1)));
+    F1.set(0, i, wall1<0>(P, G, x, y));
+    F1.set(1, i, wall1<1>(P, G, x, y));
+    const Prim<R> q = P.get(i);
+    const unsigned long long b = hk::ts_bits<R>(hs::timescale(G.g, G.dR0, G.dR1, q.rho, q.v0,
+                                                              q.v1, q.p));
+    best = b < best ? b : best;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long w = __shfl_xor_sync(0xffffffffu, best, o);
+    best = w < best ? w : best;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMin(minbits, best);
+}
+
+// A2: stage-1 state from the stored walls
+template <class R>
+__global__ void __launch_bounds__(256)
+adj_stage1(Fields<R> P, FluxStore<R> F1, Fields<R> Q, Geo<R> G,
+           const unsigned long long *minbits, unsigned long long *argmin) {
+  G.dt = (R)*G.dtp;
+  const size_t n = (size_t)G.n0 * G.n1;
+  const R h = G.dt / R(2);
+  const R d0 = h / G.dR0, d1 = h / G.dR1;
+  const unsigned long long mb = *minbits;
+  unsigned long long best = ~0ull;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int y = (int)(i / G.n0), x = (int)(i - (size_t)y * G.n0);
+    const Prim<R> b = P.get(i);
+    Q.set(i, hs::update(G.g, b, d0, d1, F1.get(0, i), F1.get(0, G.at(x + 1, y)),
+                        F1.get(1, i), F1.get(1, G.at(x, y + 1))));
+    const R t = hs::timescale(G.g, G.dR0, G.dR1, b.rho, b.v0, b.v1, b.p);
+    if (hk::ts_bits<R>(t) == mb && i < best) best = i;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long w = __shfl_xor_sync(0xffffffffu, best, o);
+    best = w < best ? w : best;
+  }
+  if ((threadIdx.x & 31) == 0 && best != ~0ull) atomicMin(argmin, best);
+}
+
+// A3: stage-2 walls (MUSCL on the stage-1 state), one per face and axis
+template <class R>
+__global__ void __launch_bounds__(256) adj_walls2(Fields<R> Q, FluxStore<R> F2, Geo<R> G) {
+  const size_t n = (size_t)G.n0 * G.n1;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int y = (int)(i / G.n0), x = (int)(i - (size_t)y * G.n0);
+    F2.set(0, i, wall2<0>(Q, G, x, y));
+    F2.set(1, i, wall2<1>(Q, G, x, y));
   }
 }
 
 // B: stage-2 update reverse per cell
 template <class R>
 __global__ void __launch_bounds__(256)
-adj_stage2_cells(Fields<R> P, Fields<R> Q, Fields<R> Ub, Fields<R> U2b, Fields<R> Pbase,
+adj_stage2_cells(Fields<R> P, FluxStore<R> F2, Fields<R> Ub, Fields<R> U2b, Fields<R> Pbase,
                  Geo<R> G, double *partial) {
+  G.dt = (R)*G.dtp;
   __shared__ double sh[8];
   const size_t n = (size_t)G.n0 * G.n1;
   const R d0 = G.dt / G.dR0, d1 = G.dt / G.dR1;
+  const R rdR0 = R(1) / G.dR0, rdR1 = R(1) / G.dR1;
   double dtb = 0;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
     const int y = (int)(i / G.n0), x = (int)(i - (size_t)y * G.n0);
-    const Flux<R> l0 = wall2<0>(Q, G, x, y), r0 = wall2<0>(Q, G, x + 1, y);
-    const Flux<R> l1 = wall2<1>(Q, G, x, y), r1 = wall2<1>(Q, G, x, y + 1);
+    const Flux<R> l0 = F2.get(0, i), r0 = F2.get(0, G.at(x + 1, y));
+    const Flux<R> l1 = F2.get(1, i), r1 = F2.get(1, G.at(x, y + 1));
     const Prim<R> b = P.get(i);
     R u[4];
     ha::update_cons(G.g, b, d0, d1, l0, r0, l1, r1, u);
@@ -140,7 +210,7 @@ adj_stage2_cells(Fields<R> P, Fields<R> Q, Fields<R> Ub, Fields<R> U2b, Fields<R
                  U[3] * (l0.fe - r0.fe);
     const R t1 = U[0] * (l1.fd - r1.fd) + U[1] * (l1.fm0 - r1.fm0) + U[2] * (l1.fm1 - r1.fm1) +
                  U[3] * (l1.fe - r1.fe);
-    dtb += (double)t0 / (double)G.dR0 + (double)t1 / (double)G.dR1;
+    dtb += (double)(t0 * rdR0 + t1 * rdR1);
   }
   const double s = block_sum(dtb, sh);
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
@@ -151,11 +221,20 @@ template <class R> struct FaceBar {
   R *f[8];
 };
 
+// reconstruction cotangents of one axis: slot k (0..3) of the stencil of
+// face f (cells f-2 .. f+1), per field: 16 arrays
+template <class R> struct SlotBar {
+  R *f[16];  // [k * 4 + field]
+};
+
 // C: stage-2 walls reverse; face i along AX is the left wall of cell i and
-// the right wall of cell i - e
+// the right wall of cell i - e.  The HLLC reverse gives the cotangents of the
+// reconstructed face states; the MUSCL reverse spreads them over the four
+// stencil cells, stored per stencil slot for the gather in D.
 template <class R>
-__global__ void __launch_bounds__(256)
-adj_stage2_faces(Fields<R> Q, Fields<R> U2b, FaceBar<R> FX, FaceBar<R> FY, Geo<R> G) {
+__global__ void __launch_bounds__(256, 3)
+adj_stage2_faces(Fields<R> Q, Fields<R> U2b, SlotBar<R> SX, SlotBar<R> SY, Geo<R> G) {
+  G.dt = (R)*G.dtp;
   const size_t n = (size_t)G.n0 * G.n1;
   const R d0 = G.dt / G.dR0, d1 = G.dt / G.dR1;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -179,53 +258,48 @@ adj_stage2_faces(Fields<R> Q, Fields<R> U2b, FaceBar<R> FX, FaceBar<R> FY, Geo<R
         face2_states<1>(Q, G, x, y, L, Rt, st);
         ha::hllc_rev<1>(G.g, L, Rt, fb, Lb, Rb);
       }
-      FaceBar<R> &F = ax == 0 ? FX : FY;
-      F.f[0][i] = Lb.rho; F.f[1][i] = Lb.v0; F.f[2][i] = Lb.v1; F.f[3][i] = Lb.p;
-      F.f[4][i] = Rb.rho; F.f[5][i] = Rb.v0; F.f[6][i] = Rb.v1; F.f[7][i] = Rb.p;
+      SlotBar<R> &S = ax == 0 ? SX : SY;
+      const R lb[4] = {Lb.rho, Lb.v0, Lb.v1, Lb.p}, rb[4] = {Rb.rho, Rb.v0, Rb.v1, Rb.p};
+#pragma unroll
+      for (int c4 = 0; c4 < 4; ++c4) {
+        R xb[4] = {0, 0, 0, 0};
+        const R *xs = &st[0].rho;
+        ha::muscl_rev((&st[0].rho)[c4], (&st[1].rho)[c4], (&st[2].rho)[c4], (&st[3].rho)[c4],
+                      lb[c4], rb[c4], xb[0], xb[1], xb[2], xb[3]);
+        (void)xs;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) S.f[k * 4 + c4][i] = xb[k];
+      }
     }
   }
 }
 
-// D: gather the reconstruction cotangents into Qb, then stage-1 update reverse
+// D: gather the reconstruction cotangents into Qb (face f = q + df holds this
+// cell in stencil slot 2 - df), then stage-1 update reverse
 template <class R>
 __global__ void __launch_bounds__(256)
-adj_stage1_cells(Fields<R> P, Fields<R> Q, FaceBar<R> FX, FaceBar<R> FY, Fields<R> U1b,
+adj_stage1_cells(Fields<R> P, FluxStore<R> F1, SlotBar<R> SX, SlotBar<R> SY, Fields<R> U1b,
                  Fields<R> Pbase, Geo<R> G, double *partial) {
+  G.dt = (R)*G.dtp;
   __shared__ double sh[8];
   const size_t n = (size_t)G.n0 * G.n1;
   const R h = G.dt / R(2);
   const R d0 = h / G.dR0, d1 = h / G.dR1;
+  const R rdR0 = R(1) / G.dR0, rdR1 = R(1) / G.dR1;
   double dtb = 0;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
     const int y = (int)(i / G.n0), x = (int)(i - (size_t)y * G.n0);
     R qb[4] = {0, 0, 0, 0};
-    // faces f = q-1 .. q+2 along each axis use this cell as stencil entry q - f + 2
 #pragma unroll
-    for (int ax = 0; ax < 2; ++ax) {
-      const FaceBar<R> &F = ax == 0 ? FX : FY;
+    for (int df = -1; df <= 2; ++df) {
+      const size_t fx = G.at(x + df, y), fy = G.at(x, y + df);
+      const int k = 2 - df;
 #pragma unroll
-      for (int df = -1; df <= 2; ++df) {
-        const int fx = ax == 0 ? x + df : x, fy = ax == 0 ? y : y + df;
-        const size_t fi = G.at(fx, fy);
-        const int k = 2 - df;  // this cell's index in the face stencil
-        R xs[4][4];
-#pragma unroll
-        for (int s = 0; s < 4; ++s) {
-          const Prim<R> v = ax == 0 ? Q.get(G.at(fx - 2 + s, fy)) : Q.get(G.at(fx, fy - 2 + s));
-          xs[0][s] = v.rho; xs[1][s] = v.v0; xs[2][s] = v.v1; xs[3][s] = v.p;
-        }
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          R b4[4] = {0, 0, 0, 0};
-          ha::muscl_rev(xs[c][0], xs[c][1], xs[c][2], xs[c][3], F.f[c][fi], F.f[4 + c][fi],
-                        b4[0], b4[1], b4[2], b4[3]);
-          qb[c] += b4[k];
-        }
-      }
+      for (int c = 0; c < 4; ++c) qb[c] += SX.f[k * 4 + c][fx] + SY.f[k * 4 + c][fy];
     }
-    const Flux<R> l0 = wall1<0>(P, G, x, y), r0 = wall1<0>(P, G, x + 1, y);
-    const Flux<R> l1 = wall1<1>(P, G, x, y), r1 = wall1<1>(P, G, x, y + 1);
+    const Flux<R> l0 = F1.get(0, i), r0 = F1.get(0, G.at(x + 1, y));
+    const Flux<R> l1 = F1.get(1, i), r1 = F1.get(1, G.at(x, y + 1));
     const Prim<R> b = P.get(i);
     R u[4];
     ha::update_cons(G.g, b, d0, d1, l0, r0, l1, r1, u);
@@ -243,7 +317,7 @@ adj_stage1_cells(Fields<R> P, Fields<R> Q, FaceBar<R> FX, FaceBar<R> FY, Fields<
     const R t1 = U[0] * (l1.fd - r1.fd) + U[1] * (l1.fm0 - r1.fm0) + U[2] * (l1.fm1 - r1.fm1) +
                  U[3] * (l1.fe - r1.fe);
     // dtdx = (dt / 2) / dR
-    dtb += 0.5 * ((double)t0 / (double)G.dR0 + (double)t1 / (double)G.dR1);
+    dtb += (double)(R(0.5) * (t0 * rdR0 + t1 * rdR1));
   }
   const double s = block_sum(dtb, sh);
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
@@ -251,8 +325,9 @@ adj_stage1_cells(Fields<R> P, Fields<R> Q, FaceBar<R> FX, FaceBar<R> FY, Fields<
 
 // E: stage-1 walls reverse
 template <class R>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 3)
 adj_stage1_faces(Fields<R> P, Fields<R> U1b, FaceBar<R> FX, FaceBar<R> FY, Geo<R> G) {
+  G.dt = (R)*G.dtp;
   const size_t n = (size_t)G.n0 * G.n1;
   const R h = G.dt / R(2);
   const R d0 = h / G.dR0, d1 = h / G.dR1;
@@ -298,54 +373,24 @@ adj_gather(Fields<R> Pbase, FaceBar<R> FX, FaceBar<R> FY, Fields<R> Pb, Geo<R> G
   }
 }
 
-// arg-min of the timescale, recomputed here (so that it does not depend on
-// how the forward build rounded it): pass 1 the minimum bits, pass 2 the
-// lowest index holding them
+// G: dt cotangent to the arg-min cell.  The block partials are summed by one
+// block in a fixed order (strided per thread, then a fixed tree), so the
+// result does not depend on scheduling.
 template <class R>
 __global__ void __launch_bounds__(256)
-adj_min_bits(Fields<R> P, Geo<R> G, unsigned long long *out) {
-  const size_t n = (size_t)G.n0 * G.n1;
-  unsigned long long best = ~0ull;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x) {
-    const Prim<R> q = P.get(i);
-    const unsigned long long b = hk::ts_bits<R>(hs::timescale(G.g, G.dR0, G.dR1, q.rho, q.v0,
-                                                              q.v1, q.p));
-    best = b < best ? b : best;
+adj_dt(Fields<R> P, Fields<R> Pb, Geo<R> G, const double *partials, int nparts, R cfl,
+       const unsigned long long *argmin, double *dtb_out) {
+  __shared__ double sh[256];
+  double acc = 0;
+  for (int k = threadIdx.x; k < nparts; k += blockDim.x) acc += partials[k];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long w = __shfl_xor_sync(0xffffffffu, best, o);
-    best = w < best ? w : best;
-  }
-  if ((threadIdx.x & 31) == 0) atomicMin(out, best);
-}
-
-template <class R>
-__global__ void __launch_bounds__(256)
-adj_argmin(Fields<R> P, Geo<R> G, const unsigned long long *minbits, unsigned long long *out) {
-  const size_t n = (size_t)G.n0 * G.n1;
-  const unsigned long long mb = *minbits;
-  unsigned long long best = ~0ull;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x) {
-    const Prim<R> q = P.get(i);
-    const R t = hs::timescale(G.g, G.dR0, G.dR1, q.rho, q.v0, q.v1, q.p);
-    if (hk::ts_bits<R>(t) == mb && i < best) best = i;
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long w = __shfl_xor_sync(0xffffffffu, best, o);
-    best = w < best ? w : best;
-  }
-  if ((threadIdx.x & 31) == 0 && best != ~0ull) atomicMin(out, best);
-}
-
-// G: dt cotangent (fixed-order sum of the block partials) to the arg-min cell
-template <class R>
-__global__ void adj_dt(Fields<R> P, Fields<R> Pb, Geo<R> G, const double *partials, int nparts,
-                       R cfl, const unsigned long long *argmin, double *dtb_out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double dtb = 0;
-  for (int k = 0; k < nparts; ++k) dtb += partials[k];
+  if (threadIdx.x != 0) return;
+  const double dtb = sh[0];
   if (dtb_out) *dtb_out = dtb;
   const unsigned long long j = *argmin;
   if (j == ~0ull) return;
@@ -383,7 +428,13 @@ adj_loss(const R *rho, const R *target, R *rhob, size_t n, double *partial) {
 struct AdjointScratch {
   int fp64 = -1;
   size_t cells = 0;
-  void *q[4], *u2b[4], *u1b[4], *pbase[4], *fx[8], *fy[8], *ub[4], *pb[4];
+  void *q[4], *u2b[4], *u1b[4], *pbase[4], *fx[8], *fy[8], *ub[4], *pb[4], *f1[8], *f2[8];
+  void *sx[16], *sy[16];
+  void *stage[4];                 // the state a graph-captured step reads
+  double *d_dt = nullptr;         // dt of the step being reversed
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // by cotangent buffer parity
+  void *graph_ub[2] = {nullptr, nullptr};
+  double graph_scalars[2][3] = {};  // cfl, dR0, dR1 each graph was captured with
   double *partials = nullptr;
   unsigned long long *argmin = nullptr;
   int nparts = 0;
@@ -392,6 +443,9 @@ struct AdjointScratch {
 
 static void free_scratch(AdjointScratch *s) {
   if (!s) return;
+  for (int k = 0; k < 2; ++k)
+    if (s->graph[k]) cudaGraphExecDestroy(s->graph[k]);
+  cudaFree(s->d_dt);
   for (void *p : s->all) cudaFree(p);
   cudaFree(s->partials);
   cudaFree(s->argmin);
@@ -411,9 +465,10 @@ static om_status get_scratch(Handle *h, int fp64, AdjointScratch **out) {
   s->fp64 = fp64;
   s->cells = h->memory_size_total();
   const size_t bytes = s->cells * (fp64 ? 8 : 4);
-  void **groups[8] = {s->q, s->u2b, s->u1b, s->pbase, s->ub, s->pb, s->fx, s->fy};
-  const int sizes[8] = {4, 4, 4, 4, 4, 4, 8, 8};
-  for (int gi = 0; gi < 8; ++gi)
+  void **groups[13] = {s->q,  s->u2b, s->u1b, s->pbase, s->ub, s->pb,   s->fx,
+                       s->fy, s->f1,  s->f2,  s->sx,    s->sy, s->stage};
+  const int sizes[13] = {4, 4, 4, 4, 4, 4, 8, 8, 8, 8, 16, 16, 4};
+  for (int gi = 0; gi < 13; ++gi)
     for (int k = 0; k < sizes[gi]; ++k) {
       void *p = nullptr;
       if (cudaMalloc(&p, bytes) != cudaSuccess) {
@@ -427,6 +482,7 @@ static om_status get_scratch(Handle *h, int fp64, AdjointScratch **out) {
     }
   s->nparts = 2 * sm_count(h->device) * 4;
   if (cudaMalloc(&s->partials, sizeof(double) * 2 * s->nparts) != cudaSuccess ||
+      cudaMalloc(&s->d_dt, sizeof(double)) != cudaSuccess ||
       cudaMalloc(&s->argmin, 2 * sizeof(unsigned long long)) != cudaSuccess) {
     cudaGetLastError();
     free_scratch(s);
@@ -457,34 +513,104 @@ template <class R> static adj::FaceBar<R> F8(void *const *p) {
   return f;
 }
 
+template <class R> static adj::SlotBar<R> S16(void *const *p) {
+  adj::SlotBar<R> f;
+  for (int k = 0; k < 16; ++k) f.f[k] = (R *)p[k];
+  return f;
+}
+
+template <class R> static adj::FluxStore<R> FS(void *const *p) {
+  adj::FluxStore<R> f;
+  for (int k = 0; k < 8; ++k) f.f[k] = (R *)p[k];
+  return f;
+}
+
 // One adjoint step at state `state` (4 device arrays) with step dt (in R)
 // and CFL minimum bits: ub (4 device arrays, cotangent of the next state)
 // -> pb_out (4 device arrays).  Returns the dt cotangent when dtb_out.
 template <class R>
-static om_status vjp_step(Handle *h, AdjointScratch *s, void *const *state, void *const *ub,
-                          void *const *pb_out, double dt, double cfl, unsigned long long tsbits,
-                          double *dtb_dev) {
+static om_status vjp_kernels(Handle *h, AdjointScratch *s, void *const *state, void *const *ub,
+                             void *const *pb_out, double cfl, unsigned long long tsbits,
+                             double *dtb_dev) {
   const cudaStream_t st = h->stream;
   const HydroScalars *hs_ = (const HydroScalars *)h->h_scalars;
-  adj::Geo<R> G{h->size[0], h->size[1], (R)h->cfg.gamma, (R)hs_->dR0, (R)hs_->dR1, (R)dt};
+  adj::Geo<R> G{h->size[0], h->size[1], (R)h->cfg.gamma, (R)hs_->dR0, (R)hs_->dR1, R(0), s->d_dt};
   const int grid = s->nparts;
   const auto P = F4<R>(state), Q = F4<R>(s->q), U = F4<R>(ub), U2b = F4<R>(s->u2b),
              U1b = F4<R>(s->u1b), Pbase = F4<R>(s->pbase), Pb = F4<R>(pb_out);
   const auto FX = F8<R>(s->fx), FY = F8<R>(s->fy);
-  adj::adj_stage1<R><<<grid, 256, 0, st>>>(P, Q, G);
-  adj::adj_stage2_cells<R><<<grid, 256, 0, st>>>(P, Q, U, U2b, Pbase, G, s->partials);
-  adj::adj_stage2_faces<R><<<grid, 256, 0, st>>>(Q, U2b, FX, FY, G);
-  adj::adj_stage1_cells<R><<<grid, 256, 0, st>>>(P, Q, FX, FY, U1b, Pbase, G,
+  const auto F1 = FS<R>(s->f1), F2 = FS<R>(s->f2);
+  const auto SX = S16<R>(s->sx), SY = S16<R>(s->sy);
+  (void)tsbits;
+  OM_CUDA_CHECK(cudaMemsetAsync(s->argmin, 0xFF, 2 * sizeof(unsigned long long), st));
+  adj::adj_walls1<R><<<grid, 256, 0, st>>>(P, F1, G, s->argmin + 1);
+  adj::adj_stage1<R><<<grid, 256, 0, st>>>(P, F1, Q, G, s->argmin + 1, s->argmin);
+  adj::adj_walls2<R><<<grid, 256, 0, st>>>(Q, F2, G);
+  adj::adj_stage2_cells<R><<<grid, 256, 0, st>>>(P, F2, U, U2b, Pbase, G, s->partials);
+  adj::adj_stage2_faces<R><<<grid, 256, 0, st>>>(Q, U2b, SX, SY, G);
+  adj::adj_stage1_cells<R><<<grid, 256, 0, st>>>(P, F1, SX, SY, U1b, Pbase, G,
                                                  s->partials + grid);
   adj::adj_stage1_faces<R><<<grid, 256, 0, st>>>(P, U1b, FX, FY, G);
   adj::adj_gather<R><<<grid, 256, 0, st>>>(Pbase, FX, FY, Pb, G);
-  (void)tsbits;
-  OM_CUDA_CHECK(cudaMemsetAsync(s->argmin, 0xFF, 2 * sizeof(unsigned long long), st));
-  adj::adj_min_bits<R><<<grid, 256, 0, st>>>(P, G, s->argmin + 1);
-  adj::adj_argmin<R><<<grid, 256, 0, st>>>(P, G, s->argmin + 1, s->argmin);
-  adj::adj_dt<R><<<1, 32, 0, st>>>(P, Pb, G, s->partials, 2 * grid, (R)cfl, s->argmin, dtb_dev);
+  adj::adj_dt<R><<<1, 256, 0, st>>>(P, Pb, G, s->partials, 2 * grid, (R)cfl, s->argmin, dtb_dev);
   OM_CUDA_CHECK(cudaGetLastError());
-  h->launches += 10;
+  return OM_OK;
+}
+
+// One adjoint step on caller buffers without a graph (synchronous dt upload)
+template <class R>
+static om_status vjp_kernels_direct(Handle *h, AdjointScratch *s, void *const *state,
+                                    void *const *ub, void *const *pb_out, double dt, double cfl,
+                                    unsigned long long tsbits) {
+  OM_CUDA_CHECK(cudaMemcpyAsync(s->d_dt, &dt, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  OM_CUDA_CHECK(cudaStreamSynchronize(h->stream));
+  OM_TRY(vjp_kernels<R>(h, s, state, ub, pb_out, cfl, tsbits, nullptr));
+  h->launches += 9;
+  return OM_OK;
+}
+
+// One adjoint step: the step's dt (from host memory that stays untouched
+// until the stream has read it) and the state go to fixed device buffers,
+// then the kernel sequence runs from a CUDA graph captured once per
+// cotangent buffer pair.
+template <class R>
+static om_status vjp_step(Handle *h, AdjointScratch *s, void *const *state, void *const *ub,
+                          void *const *pb_out, const double *dt_host, double cfl,
+                          unsigned long long tsbits, double *dtb_dev) {
+  const cudaStream_t st = h->stream;
+  const size_t bytes = s->cells * sizeof(R);
+  OM_CUDA_CHECK(cudaMemcpyAsync(s->d_dt, dt_host, sizeof(double), cudaMemcpyHostToDevice, st));
+  for (int k = 0; k < 4; ++k)
+    if (state[k] != s->stage[k])
+      OM_CUDA_CHECK(cudaMemcpyAsync(s->stage[k], state[k], bytes, cudaMemcpyDeviceToDevice, st));
+  const int key = ub[0] == s->ub[0] ? 0 : 1;
+  // scalars baked into the captured kernel arguments
+  const HydroScalars *hs_ = (const HydroScalars *)h->h_scalars;
+  const double baked[3] = {cfl, hs_->dR0, hs_->dR1};
+  if (!s->graph[key] || s->graph_ub[key] != ub[0] ||
+      std::memcmp(baked, s->graph_scalars[key], sizeof(baked)) != 0) {
+    if (s->graph[key]) cudaGraphExecDestroy(s->graph[key]);
+    s->graph[key] = nullptr;
+    cudaGraph_t g = nullptr;
+    OM_CUDA_CHECK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    om_status r = vjp_kernels<R>(h, s, s->stage, ub, pb_out, cfl, tsbits, dtb_dev);
+    cudaError_t ce = cudaStreamEndCapture(st, &g);
+    if (r != OM_OK) { if (g) cudaGraphDestroy(g); return r; }
+    if (ce != cudaSuccess) {
+      set_error(std::string("adjoint graph capture: ") + cudaGetErrorString(ce));
+      return OM_ERR_CUDA;
+    }
+    ce = cudaGraphInstantiate(&s->graph[key], g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) {
+      set_error(std::string("adjoint graph instantiate: ") + cudaGetErrorString(ce));
+      return OM_ERR_CUDA;
+    }
+    s->graph_ub[key] = ub[0];
+    std::memcpy(s->graph_scalars[key], baked, sizeof(baked));
+  }
+  OM_CUDA_CHECK(cudaGraphLaunch(s->graph[key], st));
+  h->launches += 9;
   return OM_OK;
 }
 
@@ -508,8 +634,8 @@ extern "C" om_status om_hydro_vjp(om_handle H, void *const *cot_next, void *cons
   OM_TRY(hydro_current_dt(h, &dt, &bits));
   void *state[4] = {h->arrays[0].d(), h->arrays[1].d(), h->arrays[2].d(), h->arrays[3].d()};
   const double cfl = ((HydroScalars *)h->h_scalars)->cfl;
-  om_status st = fp64 ? vjp_step<double>(h, s, state, cot_next, cot_prev, dt, cfl, bits, nullptr)
-                      : vjp_step<float>(h, s, state, cot_next, cot_prev, dt, cfl, bits, nullptr);
+  om_status st = fp64 ? vjp_kernels_direct<double>(h, s, state, cot_next, cot_prev, dt, cfl, bits)
+                      : vjp_kernels_direct<float>(h, s, state, cot_next, cot_prev, dt, cfl, bits);
   OM_TRY(st);
   OM_CUDA_CHECK(cudaStreamSynchronize(h->stream));
   return OM_OK;
@@ -605,9 +731,9 @@ extern "C" om_status om_hydro_adjoint_run(om_handle H, int steps, const void *ta
       if ((status = om_run(H, kid)) != OM_OK) return fail(status);
     }
     for (int m = len - 1; m >= 0; --m) {
-      status = fp64 ? vjp_step<double>(h, sc, segst[m].f, ub, pb, seg_dt[m], cfl, seg_bits[m],
+      status = fp64 ? vjp_step<double>(h, sc, segst[m].f, ub, pb, &seg_dt[m], cfl, seg_bits[m],
                                        nullptr)
-                    : vjp_step<float>(h, sc, segst[m].f, ub, pb, seg_dt[m], cfl, seg_bits[m],
+                    : vjp_step<float>(h, sc, segst[m].f, ub, pb, &seg_dt[m], cfl, seg_bits[m],
                                       nullptr);
       if (status != OM_OK) return fail(status);
       for (int k = 0; k < 4; ++k) std::swap(ub[k], pb[k]);
@@ -652,8 +778,8 @@ extern "C" om_status om_hydro_time_vjp(om_handle H, int reps, float *ms) {
   OM_CUDA_CHECK(cudaEventCreate(&e1));
   OM_CUDA_CHECK(cudaEventRecord(e0, h->stream));
   for (int r = 0; r < reps; ++r) {
-    om_status st = fp64 ? vjp_step<double>(h, s, state, s->ub, s->pb, dt, cfl, bits, nullptr)
-                        : vjp_step<float>(h, s, state, s->ub, s->pb, dt, cfl, bits, nullptr);
+    om_status st = fp64 ? vjp_step<double>(h, s, state, s->ub, s->pb, &dt, cfl, bits, nullptr)
+                        : vjp_step<float>(h, s, state, s->ub, s->pb, &dt, cfl, bits, nullptr);
     OM_TRY(st);
   }
   OM_CUDA_CHECK(cudaEventRecord(e1, h->stream));

@@ -49,7 +49,7 @@ def loss_of(h, st, steps, target):
     return float(((r - target) ** 2).mean())
 
 
-@pytest.mark.parametrize("precision,steps,tol", [(64, 12, 1e-5), (32, 12, 2e-3)])
+@pytest.mark.parametrize("precision,steps,tol", [(64, 12, 1e-4), (32, 12, 2e-3)])
 def test_gradient_vs_finite_differences(om_lib, oracle, precision, steps, tol):
     # The loss is piecewise smooth (the CFL arg-min, wave-speed cases and
     # limiter picks switch): a perturbation of 1e-6 already crosses such
