@@ -237,8 +237,9 @@ def life_workload(args, dist: Dist) -> dict:
                                f"{gens} generations per step, population reduce every generation",
                    "n0": n, "n1": n, "generations_per_step": gens,
                    "parallelism": f"replicas x{dist.world}",
-                   "l2": "inputs larger than L2 (2 x 1 GiB int32 buffers)" if n >= 8192
-                   else "grid resident in shared memory (launch-bound case)"},
+                   "l2": f"inputs larger than L2 (2 x {cells * 4 / 2**20:.0f} MiB int32 buffers)"
+                   if cells * 4 > 129 * 2**20
+                   else "grid fits in L2; no flush (launch-bound case)"},
         "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
     }
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:

@@ -81,6 +81,11 @@ __device__ __forceinline__ int wrap(int i, int n) {
   return i < 0 ? i + n : i;
 }
 
+// periodic index for -n <= i < 2n (one add or subtract, no division)
+__device__ __forceinline__ int wrap_near(int i, int n) {
+  return i < 0 ? i + n : (i >= n ? i - n : i);
+}
+
 // dt of this step in the OM's Real type: dtG = cfl * reduce Min dts
 template <class R> __device__ __forceinline__ R step_dt(const HydroStepArgs &a) {
   const R tsmin = ts_from_bits<R>(a.sc->tsmin[a.read_slot]);
@@ -144,10 +149,13 @@ __device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
   const R *rho = (const R *)a.rho, *vx = (const R *)a.v0, *vy = (const R *)a.v1,
           *pr = (const R *)a.p;
 
-  // phase 0: load primitives and sound speeds
+  // phase 0: load primitives and sound speeds.  Box indices run from -3 to
+  // n + T + 1 (T the tile extent), inside [-n, 2n) once n >= T + 8.
+  const bool near = n0 >= TX + 8 && n1 >= TY + 8;
   for (int i = tid; i < S::PY * S::PX; i += NT) {
     const int py = i / S::PX, px = i - py * S::PX;
-    const int gy = hk::wrap<R>(Y0 + py - 3, n1), gx = hk::wrap<R>(X0 + px - 3, n0);
+    const int gy = near ? hk::wrap_near(Y0 + py - 3, n1) : hk::wrap<R>(Y0 + py - 3, n1);
+    const int gx = near ? hk::wrap_near(X0 + px - 3, n0) : hk::wrap<R>(X0 + px - 3, n0);
     const size_t gi = (size_t)gy * n0 + gx;
     const R r = rho[gi], u = vx[gi], v = vy[gi], q = pr[gi];
     s.P[0][py][px] = r;

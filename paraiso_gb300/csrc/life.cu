@@ -39,12 +39,16 @@ struct LifeScalars {  // device/host scalar block
 struct LifeState {
   bool binary = true;           // every cell is known to be 0 or 1
   uint32_t *d_pop = nullptr;    // populations of the last run, per generation
+  uint32_t *d_flag = nullptr;   // raised by the cell-value check
   int pop_cap = 0;
   int last_n = 0;
   int depth = 0, tile_w = 0, tile_h = 0;  // tuned or configured
 };
 
 static LifeState *life_state(Handle *h) { return (LifeState *)h->impl; }
+
+cudaError_t life_check_cells_into(const int32_t *cells, size_t n, uint32_t *flag,
+                                  cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // device code
@@ -1041,18 +1045,70 @@ static void life_after_replay(Handle *h, int kernel_id, int n) {
 
 static void life_restore_key(Handle *h, uint64_t key) { life_state(h)->binary = key != 0; }
 
+// New cell contents came from the host.  The packed kernels need every cell
+// in {0, 1}; one read-only pass (HBM speed, a fraction of one generation)
+// settles that here, outside any stream capture, so that only grids that do
+// hold other values pay for a generation of the general integer kernel.
 static void life_array_written(Handle *h, Array *a) {
-  (void)a;
-  life_state(h)->binary = false;
+  LifeState *st = life_state(h);
+  st->binary = false;
+  const bool packed_ok = h->cyclic && (h->size[0] % 32 == 0) && h->cfg.variant == 0;
+  if (!packed_ok || !st->d_flag || h->capturing) return;
+  uint32_t bad = 1;
+  if (cudaMemsetAsync(st->d_flag, 0, sizeof(uint32_t), h->stream) != cudaSuccess ||
+      life_check_cells_into((const int32_t *)a->d(), a->count, st->d_flag, h->stream) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(&bad, st->d_flag, sizeof(bad), cudaMemcpyDeviceToHost, h->stream) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(h->stream) != cudaSuccess)
+    return;  // binary stays false: the general kernel handles any values
+  st->binary = bad == 0;
 }
 
 static void life_free(Handle *h) {
   LifeState *st = life_state(h);
   if (st) {
     if (st->d_pop) cudaFree(st->d_pop);
+    if (st->d_flag) cudaFree(st->d_flag);
     delete st;
   }
   h->impl = nullptr;
+}
+
+// Raises *flag when any of the n cells is outside {0, 1}.  128-bit loads when
+// the array is 16-byte aligned; a value v is outside {0, 1} iff v & ~1 != 0,
+// so the OR of four cells is tested at once.
+__global__ void __launch_bounds__(256)
+life_check_kernel(const int32_t *__restrict__ cells, size_t n, uint32_t *flag) {
+  bool bad = false;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const size_t i0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t tail = 0;
+  if ((reinterpret_cast<uintptr_t>(cells) & 15) == 0) {
+    const int4 *v = reinterpret_cast<const int4 *>(cells);
+    const size_t nv = n / 4;
+    for (size_t i = i0; i < nv; i += stride) {
+      const int4 c = __ldcs(v + i);
+      bad |= ((c.x | c.y | c.z | c.w) & ~1) != 0;
+    }
+    tail = nv * 4;
+  }
+  for (size_t i = tail + i0; i < n; i += stride) bad |= (cells[i] & ~1) != 0;
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1u);
+}
+
+// Launches the cell-value check on stream s (allocates nothing; *flag must
+// be cleared by the caller).
+cudaError_t life_check_cells_into(const int32_t *cells, size_t n, uint32_t *flag,
+                                  cudaStream_t s) {
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  const size_t want = (n / 4 + 255) / 256;
+  const unsigned grid = (unsigned)std::max<size_t>(1, std::min<size_t>(want, 8 * (size_t)sms));
+  life_check_kernel<<<grid, 256, 0, s>>>(cells, n, flag);
+  return cudaGetLastError();
 }
 
 // One launch of the temporally blocked tile kernel from `cur` into `next`
@@ -1094,6 +1150,10 @@ om_status life_setup(Handle *h) {
   h->ops.array_written = life_array_written;
   h->ops.reserve = life_reserve;
   OM_TRY(alloc_array(h, "cell", sizeof(int32_t)));
+  if (cudaMalloc(&st->d_flag, sizeof(uint32_t)) != cudaSuccess) {
+    set_error("Life: cannot allocate the cell-value flag");
+    return OM_ERR_NOMEM;
+  }
   h->scalars.push_back({"population", kInt, offsetof(LifeScalars, population)});
   h->scalars.push_back({"generation", kInt, offsetof(LifeScalars, generation)});
   h->scalar_bytes = sizeof(LifeScalars);

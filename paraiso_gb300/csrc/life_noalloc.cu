@@ -24,19 +24,11 @@ namespace om {
 
 cudaError_t life_tb_launch_into(const int32_t *cur, int32_t *next, int n0, int n1, int gens,
                                 uint32_t *pop, cudaStream_t s);
+cudaError_t life_check_cells_into(const int32_t *cells, size_t n, uint32_t *flag,
+                                  cudaStream_t s);
 
 static __device__ __align__(256) uint32_t
     g_life_noalloc_scratch[OM_LIFE_NOALLOC_MAX_GENERATIONS + 1];
-
-// Raises the flag word when any cell is outside {0, 1}.
-__global__ void __launch_bounds__(256)
-life_noalloc_check_kernel(const int32_t *__restrict__ cells, size_t n, uint32_t *flag) {
-  bool bad = false;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x)
-    bad |= (cells[i] & ~1) != 0;
-  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1u);
-}
 
 // Device address of the scratch array, looked up once per device with that
 // device current.  A host-side reference to g_life_noalloc_scratch is only
@@ -100,11 +92,7 @@ extern "C" om_status om_life_proceed_noalloc(const int32_t *cells_in, int32_t *c
   OM_CUDA_CHECK(cudaMemsetAsync(scratch, 0, bytes, s));
   const size_t n = (size_t)n0 * n1;
   uint32_t *flag = scratch + OM_LIFE_NOALLOC_MAX_GENERATIONS;
-  int dev = 0, sms = 0;
-  OM_CUDA_CHECK(cudaGetDevice(&dev));
-  OM_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  life_noalloc_check_kernel<<<2 * (sms > 0 ? sms : 1), 256, 0, s>>>(cells_in, n, flag);
-  OM_CUDA_CHECK(cudaGetLastError());
+  OM_CUDA_CHECK(life_check_cells_into(cells_in, n, flag, s));
   OM_CUDA_CHECK(life_tb_launch_into(cells_in, cells_out, n0, n1, generations, scratch, s));
   uint32_t bad = 0;
   OM_CUDA_CHECK(cudaMemcpyAsync(&bad, flag, sizeof(bad), cudaMemcpyDeviceToHost, s));

@@ -93,6 +93,20 @@ def test_life_nonbinary_first_step(om_lib, oracle):
     assert np.array_equal(pops, rp)
 
 
+def test_life_host_write_checks_cell_values(om_lib, oracle):
+    # a host write of 0/1 cells keeps every generation on the packed kernels;
+    # any other value costs exactly one generation of the general kernel
+    init = oracle.life_bernoulli(256, 96, 3, 0.3)
+    rc, rp = oracle.life_run(init, 30, cyclic=True)
+    cells, pops, _, _, packed_launches = run_gpu(om_lib, (256, 96), init, 30)
+    assert np.array_equal(cells, rc) and np.array_equal(pops, rp)
+    init[5, 7] = 2
+    rc, rp = oracle.life_run(init, 30, cyclic=True)
+    cells, pops, _, _, launches = run_gpu(om_lib, (256, 96), init, 30)
+    assert np.array_equal(cells, rc) and np.array_equal(pops, rp)
+    assert launches == packed_launches + 1
+
+
 def test_life_host_mirror_and_graph_replay(om_lib, oracle):
     pg = om_lib
     life = pg.Life((512, 256))
