@@ -6,7 +6,10 @@
 //
 // Real is double as in examples/Hydro/Hydro.hs:37; define OM_HYDRO_FP32 to
 // store the arrays in float and run the FP32 fused kernel (scalars stay
-// double: time is accumulated and dt is reduced in FP64).
+// double: time is accumulated in FP64).  The default mesh is the generated
+// one: 1024 x 1024 with the open boundary of the generator's default setup
+// (Language/Paraiso/Generator/Native.hs:36): 3-cell margins that take the
+// jet state every step (HydroMain.hs:105-131).
 #pragma once
 
 #include "om_shim.hpp"
@@ -18,10 +21,10 @@ class Hydro : public om_shim::machine {
 #else
   typedef double Real;
 #endif
-  // the example's mesh (HydroMain.hs:290-302), periodic, gamma 5/3
+  // the example's mesh (HydroMain.hs:290-302), open, gamma 5/3
   Hydro() : Hydro(1024, 1024) {}
-  Hydro(int n0, int n1, double gamma = 5.0 / 3.0)
-      : om_shim::machine(OM_KIND_HYDRO, n0, n1, config(gamma)),
+  Hydro(int n0, int n1, double gamma = 5.0 / 3.0, int boundary = OM_BOUNDARY_OPEN)
+      : om_shim::machine(OM_KIND_HYDRO, n0, n1, config(gamma, boundary)),
         density_(h_, "density"), velocity0_(h_, "velocity0"),
         velocity1_(h_, "velocity1"), pressure_(h_, "pressure") {}
 
@@ -46,10 +49,11 @@ class Hydro : public om_shim::machine {
   void proceed() { run("proceed"); }
 
  private:
-  static om_config config(double gamma) {
+  static om_config config(double gamma, int boundary) {
     om_config c;
     om_config_default(&c);
     c.gamma = gamma;
+    c.boundary = boundary;
 #ifdef OM_HYDRO_FP32
     c.precision = 32;
 #else

@@ -161,6 +161,19 @@ om_status om_hydro_dt_history(om_handle h, double *out, int n, int *written);
  * through both stages, MUSCL-minmod, HLLC, the clamps and the step's CFL dt
  * (routed to the arg-min cell of the timescale). */
 om_status om_hydro_vjp(om_handle h, void *const *cot_next, void *const *cot_prev);
+/* Checkpointed forward/backward pair.  om_hydro_forward runs `steps` proceed
+ * steps from the current state and keeps the state every `checkpoint_every`
+ * steps (0: ceil(sqrt(steps))) in a tape; the handle ends at the final
+ * state.  om_hydro_backward maps dL/d(final state) (cot_final[4]: density,
+ * velocity0, velocity1, pressure; host or device arrays of om_memory_size
+ * elements) to dL/d(start state) in grad[4] (host or device), recomputing
+ * each segment from its checkpoint; the handle is left at the final state
+ * and the tape serves any number of cotangents until om_hydro_tape_free. */
+typedef struct om_hydro_tape_s *om_hydro_tape;
+om_status om_hydro_forward(om_handle h, int steps, int checkpoint_every, om_hydro_tape *tape);
+om_status om_hydro_backward(om_handle h, om_hydro_tape tape, const void *const *cot_final,
+                            void *const *grad);
+om_status om_hydro_tape_free(om_hydro_tape tape);
 /* Gradient of loss = mean((density_T - target)^2) over `steps` proceed
  * steps from the current state, w.r.t. that state (grad[4]: host or device
  * arrays), with checkpoints every `checkpoint_every` steps (0: sqrt(steps)).

@@ -6,15 +6,16 @@
 // cotangent of the state before it, through both stages, both axes, the
 // MUSCL-minmod reconstruction, the HLLC fluxes, the clamps and the dt of the
 // step (dt = cfl * min timescale: its cotangent is routed to the arg-min
-// cell).  The step is a sequence of gather kernels over cells and faces, so
-// every cotangent is written by exactly one thread:
-//   A  stage-1 state Q (forward recompute)
-//   B  per cell: stage-2 update reverse -> conserved cotangent U2b, base part
-//   C  per face: stage-2 flux cotangent -> HLLC and reconstruction inputs
-//   D  per cell: gather into Qb; stage-1 update reverse -> U1b, base part
-//   E  per face: stage-1 flux cotangent -> HLLC inputs
-//   F  per cell: gather the stage-1 face cotangents into the base cotangent
-//   G  the dt cotangent (block partials summed in order) to the arg-min cell
+// cell).  Four launches, each over TX x TY tiles whose face work lives in
+// shared memory, so every cotangent is written by exactly one thread:
+//   A+B  forward recompute of the tile (as the fused forward step); stage-1
+//        state and walls stored; stage-2 update reverse per cell -> U2b,
+//        base part, dt partial; minimum CFL timescale
+//   C+D  stage-2 walls reverse (HLLC, MUSCL, per stencil slot in shared
+//        memory), gather into the stage-1 cotangent, stage-1 update reverse
+//   E+F  stage-1 walls reverse and gather into the previous-state cotangent;
+//        arg-min of the timescale
+//   G    dt cotangent (partials summed in a fixed order) to the arg-min cell
 // Multi-step gradients use sqrt(T) checkpointing: the forward keeps every
 // s-th state, the backward recomputes each segment and walks it backwards.
 #include <cuda_runtime.h>
@@ -46,13 +47,31 @@ template <class R> struct Fields {
   }
 };
 
+// Indices reach at most a tile (32 x 16) plus 3 cells beyond the mesh; with
+// both extents at least this, a single add or subtract wraps them.
+constexpr int kCheapWrap = 40;
+
+// What changes from one adjoint step to the next, read by the kernels from
+// device memory so that one captured graph serves every step: the step's dt
+// and the four arrays of the state before the step.
+struct StepIn {
+  double dt;
+  void *state[4];
+};
+
 template <class R> struct Geo {
   int n0, n1;
   R g, dR0, dR1, dt;
-  const double *dtp;  // the step's dt in device memory (read at kernel start)
-  // periodic index of a cell at most 4 cells outside the mesh
+  const StepIn *in;   // this step's dt and state (device memory)
+  int cheap;          // n0, n1 >= kCheapWrap: one add or subtract wraps an index
+  __device__ __forceinline__ Fields<R> state() const {
+    return Fields<R>{{(R *)in->state[0], (R *)in->state[1], (R *)in->state[2],
+                      (R *)in->state[3]}};
+  }
+  // periodic index of a cell at most 4 cells (or one tile plus 3 cells)
+  // outside the mesh
   __device__ __forceinline__ size_t at(int x, int y) const {
-    if (n0 >= 8 && n1 >= 8) {
+    if (cheap) {
       x += x < 0 ? n0 : 0;
       x -= x >= n0 ? n0 : 0;
       y += y < 0 ? n1 : 0;
@@ -76,34 +95,6 @@ template <class R> struct FluxStore {
   }
 };
 
-// order-1 stage-1 wall along AX at cell (x, y): between (x,y)-e and (x,y)
-template <int AX, class R>
-__device__ __forceinline__ Flux<R> wall1(const Fields<R> &P, const Geo<R> &G, int x, int y) {
-  const Prim<R> L = AX == 0 ? P.get(G.at(x - 1, y)) : P.get(G.at(x, y - 1));
-  const Prim<R> Rt = P.get(G.at(x, y));
-  return hs::hllc<AX>(G.g, L, hs::sound(G.g, L.rho, L.p), Rt, hs::sound(G.g, Rt.rho, Rt.p));
-}
-
-// MUSCL face states of the stage-2 wall along AX at (x, y)
-template <int AX, class R>
-__device__ __forceinline__ void face2_states(const Fields<R> &Q, const Geo<R> &G, int x, int y,
-                                             Prim<R> &L, Prim<R> &Rt, Prim<R> st[4]) {
-#pragma unroll
-  for (int k = 0; k < 4; ++k)
-    st[k] = AX == 0 ? Q.get(G.at(x - 2 + k, y)) : Q.get(G.at(x, y - 2 + k));
-  hs::muscl(st[0].rho, st[1].rho, st[2].rho, st[3].rho, L.rho, Rt.rho);
-  hs::muscl(st[0].v0, st[1].v0, st[2].v0, st[3].v0, L.v0, Rt.v0);
-  hs::muscl(st[0].v1, st[1].v1, st[2].v1, st[3].v1, L.v1, Rt.v1);
-  hs::muscl(st[0].p, st[1].p, st[2].p, st[3].p, L.p, Rt.p);
-}
-
-template <int AX, class R>
-__device__ __forceinline__ Flux<R> wall2(const Fields<R> &Q, const Geo<R> &G, int x, int y) {
-  Prim<R> L, Rt, st[4];
-  face2_states<AX>(Q, G, x, y, L, Rt, st);
-  return hs::hllc<AX>(G.g, L, hs::sound(G.g, L.rho, L.p), Rt, hs::sound(G.g, Rt.rho, Rt.p));
-}
-
 __device__ __forceinline__ double block_sum(double v, double *sh) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -116,202 +107,344 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
   return t;
 }
 
-// A1: stage-1 walls, one per face and axis (face i: left wall of cell i)
-template <class R>
-__global__ void __launch_bounds__(256)
-adj_walls1(Fields<R> P, FluxStore<R> F1, Geo<R> G, unsigned long long *minbits) {
-  const size_t n = (size_t)G.n0 * G.n1;
-  unsigned long long best = ~0ull;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x) {
-    const int y = (int)(i / G.n0), x = (int)(i - (size_t)y * G.n0);
-    F1.set(0, i, wall1<0>(P, G, x, y));
-    F1.set(1, i, wall1<1>(P, G, x, y));
-    const Prim<R> q = P.get(i);
-    const unsigned long long b = hk::ts_bits<R>(hs::timescale(G.g, G.dR0, G.dR1, q.rho, q.v0,
-                                                              q.v1, q.p));
-    best = b < best ? b : best;
-  }
+// Tile shapes of the fused kernels (A+B, C+D and E+F below)
+template <class R> struct AdjTile;
+template <> struct AdjTile<float> { static constexpr int TX = 32, TY = 16; };
+template <> struct AdjTile<double> { static constexpr int TX = 32, TY = 8; };
+
+__device__ __forceinline__ unsigned long long warp_min(unsigned long long v) {
   for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long w = __shfl_xor_sync(0xffffffffu, best, o);
-    best = w < best ? w : best;
+    const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w < v ? w : v;
   }
-  if ((threadIdx.x & 31) == 0) atomicMin(minbits, best);
+  return v;
 }
 
-// A2: stage-1 state from the stored walls
-template <class R>
+// A+B on one TX x TY tile: the forward recompute of the step in the layout
+// of the fused forward kernel (state box with a 3-cell halo, stage-1 walls,
+// stage-1 cells with a 2-cell halo, stage-2 walls of the tile), storing the
+// stage-1 state Q and the stage-1 walls F1 of the tile cells; then per tile
+// cell the stage-2 update reverse (conserved cotangent U2b, base part of the
+// previous-state cotangent, the dt partial) and the CFL timescale minimum of
+// the state.
+template <class R, int TX, int TY>
 __global__ void __launch_bounds__(256)
-adj_stage1(Fields<R> P, FluxStore<R> F1, Fields<R> Q, Geo<R> G,
-           const unsigned long long *minbits, unsigned long long *argmin) {
-  G.dt = (R)*G.dtp;
-  const size_t n = (size_t)G.n0 * G.n1;
-  const R h = G.dt / R(2);
-  const R d0 = h / G.dR0, d1 = h / G.dR1;
-  const unsigned long long mb = *minbits;
-  unsigned long long best = ~0ull;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x) {
-    const int y = (int)(i / G.n0), x = (int)(i - (size_t)y * G.n0);
-    const Prim<R> b = P.get(i);
-    Q.set(i, hs::update(G.g, b, d0, d1, F1.get(0, i), F1.get(0, G.at(x + 1, y)),
-                        F1.get(1, i), F1.get(1, G.at(x, y + 1))));
-    const R t = hs::timescale(G.g, G.dR0, G.dR1, b.rho, b.v0, b.v1, b.p);
-    if (hk::ts_bits<R>(t) == mb && i < best) best = i;
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long w = __shfl_xor_sync(0xffffffffu, best, o);
-    best = w < best ? w : best;
-  }
-  if ((threadIdx.x & 31) == 0 && best != ~0ull) atomicMin(argmin, best);
-}
-
-// A3: stage-2 walls (MUSCL on the stage-1 state), one per face and axis
-template <class R>
-__global__ void __launch_bounds__(256) adj_walls2(Fields<R> Q, FluxStore<R> F2, Geo<R> G) {
-  const size_t n = (size_t)G.n0 * G.n1;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x) {
-    const int y = (int)(i / G.n0), x = (int)(i - (size_t)y * G.n0);
-    F2.set(0, i, wall2<0>(Q, G, x, y));
-    F2.set(1, i, wall2<1>(Q, G, x, y));
-  }
-}
-
-// B: stage-2 update reverse per cell
-template <class R>
-__global__ void __launch_bounds__(256)
-adj_stage2_cells(Fields<R> P, FluxStore<R> F2, Fields<R> Ub, Fields<R> U2b, Fields<R> Pbase,
-                 Geo<R> G, double *partial) {
-  G.dt = (R)*G.dtp;
+adj_forward_tile(Fields<R> Ub, Fields<R> Q, FluxStore<R> F1, Fields<R> U2b, Fields<R> Pbase,
+                 Geo<R> G, double *partial, unsigned long long *minbits) {
+  using S = FusedSmem<R, TX, TY>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  S &s = *reinterpret_cast<S *>(smem_raw);
   __shared__ double sh[8];
-  const size_t n = (size_t)G.n0 * G.n1;
+  G.dt = (R)G.in->dt;
+  const Fields<R> P = G.state();
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int nt0 = (G.n0 + TX - 1) / TX;
+  const int X0 = (int)(blockIdx.x % nt0) * TX, Y0 = (int)(blockIdx.x / nt0) * TY;
+  const R g = G.g;
+  // state box (origin X0-3, Y0-3) with sound speeds
+  for (int i = tid; i < S::PY * S::PX; i += nthr) {
+    const int py = i / S::PX, px = i - py * S::PX;
+    const size_t gi = G.at(X0 + px - 3, Y0 + py - 3);
+    const R r = P.f[0][gi], u = P.f[1][gi], v = P.f[2][gi], q = P.f[3][gi];
+    s.P[0][py][px] = r;
+    s.P[1][py][px] = u;
+    s.P[2][py][px] = v;
+    s.P[3][py][px] = q;
+    s.C[py][px] = hs::sound(g, r, q);
+  }
+  __syncthreads();
+  // stage-1 walls: x wall fx of box row fy+1 is the left wall of box cell
+  // (fx+1, fy+1); y wall (fx, fy) is the lower wall of box cell (fx+1, fy+1)
+  {
+    constexpr int NX = S::FXY * S::FXX, NY = S::FYY * S::FYX;
+    for (int i = tid; i < NX + NY; i += nthr) {
+      if (i < NX) {
+        const int fy = i / S::FXX, fx = i - fy * S::FXX;
+        const int py = fy + 1;
+        const Prim<R> L{s.P[0][py][fx], s.P[1][py][fx], s.P[2][py][fx], s.P[3][py][fx]};
+        const Prim<R> Rt{s.P[0][py][fx + 1], s.P[1][py][fx + 1], s.P[2][py][fx + 1],
+                         s.P[3][py][fx + 1]};
+        s.fx[i] = hs::hllc<0>(g, L, s.C[py][fx], Rt, s.C[py][fx + 1]);
+      } else {
+        const int j = i - NX;
+        const int fy = j / S::FYX, fx = j - fy * S::FYX;
+        const int px = fx + 1;
+        const Prim<R> L{s.P[0][fy][px], s.P[1][fy][px], s.P[2][fy][px], s.P[3][fy][px]};
+        const Prim<R> Rt{s.P[0][fy + 1][px], s.P[1][fy + 1][px], s.P[2][fy + 1][px],
+                         s.P[3][fy + 1][px]};
+        s.fy[j] = hs::hllc<1>(g, L, s.C[fy][px], Rt, s.C[fy + 1][px]);
+      }
+    }
+  }
+  __syncthreads();
+  // stage-1 cells (Q box cell (qx, qy) is state box cell (qx+1, qy+1))
+  {
+    const R h = G.dt / R(2);
+    const R dtdx0 = h / G.dR0, dtdx1 = h / G.dR1;
+    for (int i = tid; i < S::QY * S::QX; i += nthr) {
+      const int qy = i / S::QX, qx = i - qy * S::QX;
+      const int py = qy + 1, px = qx + 1;
+      const Prim<R> b{s.P[0][py][px], s.P[1][py][px], s.P[2][py][px], s.P[3][py][px]};
+      const Prim<R> q = hs::update(g, b, dtdx0, dtdx1, s.fx[qy * S::FXX + qx],
+                                   s.fx[qy * S::FXX + qx + 1], s.fy[qy * S::FYX + qx],
+                                   s.fy[(qy + 1) * S::FYX + qx]);
+      s.Q[0][qy][qx] = q.rho;
+      s.Q[1][qy][qx] = q.v0;
+      s.Q[2][qy][qx] = q.v1;
+      s.Q[3][qy][qx] = q.p;
+    }
+  }
+  __syncthreads();
+  // the tile's stage-1 state and its cells' own (left / lower) stage-1 walls
+  for (int i = tid; i < TX * TY; i += nthr) {
+    const int ty = i / TX, tx = i - ty * TX;
+    const int x = X0 + tx, y = Y0 + ty;
+    if (x >= G.n0 || y >= G.n1) continue;
+    const size_t gi = (size_t)y * G.n0 + x;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) Q.f[c][gi] = s.Q[c][ty + 2][tx + 2];
+    F1.set(0, gi, s.fx[(ty + 2) * S::FXX + tx + 2]);
+    F1.set(1, gi, s.fy[(ty + 2) * S::FYX + tx + 2]);
+  }
+  __syncthreads();
+  // stage-2 walls of the tile (MUSCL on the stage-1 state)
+  {
+    constexpr int NX = TY * (TX + 1), NY = (TY + 1) * TX;
+    for (int i = tid; i < NX + NY; i += nthr) {
+      hs::Prim<R> L, Rt;
+      if (i < NX) {
+        const int sy = i / (TX + 1), sx = i - sy * (TX + 1);
+        const int qy = sy + 2;
+#pragma unroll
+        for (int f = 0; f < 4; ++f) {
+          R l, r;
+          hs::muscl(s.Q[f][qy][sx], s.Q[f][qy][sx + 1], s.Q[f][qy][sx + 2], s.Q[f][qy][sx + 3],
+                    l, r);
+          (&L.rho)[f] = l;
+          (&Rt.rho)[f] = r;
+        }
+        s.fx[i] = hs::hllc<0>(g, L, hs::sound(g, L.rho, L.p), Rt, hs::sound(g, Rt.rho, Rt.p));
+      } else {
+        const int j = i - NX;
+        const int sy = j / TX, sx = j - sy * TX;
+        const int qx = sx + 2;
+#pragma unroll
+        for (int f = 0; f < 4; ++f) {
+          R l, r;
+          hs::muscl(s.Q[f][sy][qx], s.Q[f][sy + 1][qx], s.Q[f][sy + 2][qx], s.Q[f][sy + 3][qx],
+                    l, r);
+          (&L.rho)[f] = l;
+          (&Rt.rho)[f] = r;
+        }
+        s.fy[j] = hs::hllc<1>(g, L, hs::sound(g, L.rho, L.p), Rt, hs::sound(g, Rt.rho, Rt.p));
+      }
+    }
+  }
+  __syncthreads();
+  // stage-2 update reverse per tile cell
   const R d0 = G.dt / G.dR0, d1 = G.dt / G.dR1;
   const R rdR0 = R(1) / G.dR0, rdR1 = R(1) / G.dR1;
   double dtb = 0;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x) {
-    const int y = (int)(i / G.n0), x = (int)(i - (size_t)y * G.n0);
-    const Flux<R> l0 = F2.get(0, i), r0 = F2.get(0, G.at(x + 1, y));
-    const Flux<R> l1 = F2.get(1, i), r1 = F2.get(1, G.at(x, y + 1));
-    const Prim<R> b = P.get(i);
+  unsigned long long best = ~0ull;
+  for (int i = tid; i < TX * TY; i += nthr) {
+    const int ty = i / TX, tx = i - ty * TX;
+    const int x = X0 + tx, y = Y0 + ty;
+    if (x >= G.n0 || y >= G.n1) continue;
+    const size_t gi = (size_t)y * G.n0 + x;
+    const Flux<R> l0 = s.fx[ty * (TX + 1) + tx], r0 = s.fx[ty * (TX + 1) + tx + 1];
+    const Flux<R> l1 = s.fy[ty * TX + tx], r1 = s.fy[(ty + 1) * TX + tx];
+    const Prim<R> b{s.P[0][ty + 3][tx + 3], s.P[1][ty + 3][tx + 3], s.P[2][ty + 3][tx + 3],
+                    s.P[3][ty + 3][tx + 3]};
     R u[4];
-    ha::update_cons(G.g, b, d0, d1, l0, r0, l1, r1, u);
-    const Prim<R> qb_ = Ub.get(i);
+    ha::update_cons(g, b, d0, d1, l0, r0, l1, r1, u);
+    const Prim<R> qb_ = Ub.get(gi);
     const PrimBar<R> qb{qb_.rho, qb_.v0, qb_.v1, qb_.p};
     R U[4];
-    ha::cons_from_prim_rev(G.g, u[0], u[1], u[2], u[3], qb, U);
-    U2b.set(i, Prim<R>{U[0], U[1], U[2], U[3]});
+    ha::cons_from_prim_rev(g, u[0], u[1], u[2], u[3], qb, U);
+    U2b.set(gi, Prim<R>{U[0], U[1], U[2], U[3]});
     PrimBar<R> bb;
     ha::zero(bb);
-    ha::cons_of_prim_rev(G.g, b, U, bb);
-    Pbase.set(i, Prim<R>{bb.rho, bb.v0, bb.v1, bb.p});
+    ha::cons_of_prim_rev(g, b, U, bb);
+    Pbase.set(gi, Prim<R>{bb.rho, bb.v0, bb.v1, bb.p});
     const R t0 = U[0] * (l0.fd - r0.fd) + U[1] * (l0.fm0 - r0.fm0) + U[2] * (l0.fm1 - r0.fm1) +
                  U[3] * (l0.fe - r0.fe);
     const R t1 = U[0] * (l1.fd - r1.fd) + U[1] * (l1.fm0 - r1.fm0) + U[2] * (l1.fm1 - r1.fm1) +
                  U[3] * (l1.fe - r1.fe);
     dtb += (double)(t0 * rdR0 + t1 * rdR1);
+    const unsigned long long tb =
+        hk::ts_bits<R>(hs::timescale(g, G.dR0, G.dR1, b.rho, b.v0, b.v1, b.p));
+    best = tb < best ? tb : best;
   }
-  const double s = block_sum(dtb, sh);
-  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+  best = warp_min(best);
+  if ((tid & 31) == 0) atomicMin(minbits, best);
+  const double sum = block_sum(dtb, sh);
+  if (tid == 0) partial[blockIdx.x] = sum;
 }
 
-// face cotangents of one axis: 8 arrays (L rho,v0,v1,p, R rho,v0,v1,p)
-template <class R> struct FaceBar {
-  R *f[8];
+// C+D on one TX x TY tile.  Stage-1 state box with a 3-cell halo (origin
+// X0-3, Y0-3), stage-2 conserved-cotangent box with a 2-cell halo (origin
+// X0-2, Y0-2), and per stencil slot the reconstruction cotangents of the
+// faces whose stencils reach a tile cell: first the x faces X0-1 .. X0+TX+1
+// of each tile row, then (in the same buffer) the y faces Y0-1 .. Y0+TY+1 of
+// each tile column; the x part of the gather waits in qx.
+template <class R, int TX, int TY> struct Stage2Smem {
+  static constexpr int QX = TX + 6, QY = TY + 6;
+  static constexpr int UX = TX + 4, UY = TY + 4;
+  static constexpr int XF = TX + 3, YF = TY + 3;
+  static constexpr int SLOTS = (TY * XF > YF * TX) ? TY * XF : YF * TX;
+  R q[4][QY][QX];
+  R u[4][UY][UX];
+  R slot[16][SLOTS];  // [slot * 4 + field][face]
+  R qx[4][TY][TX];
 };
 
-// reconstruction cotangents of one axis: slot k (0..3) of the stencil of
-// face f (cells f-2 .. f+1), per field: 16 arrays
-template <class R> struct SlotBar {
-  R *f[16];  // [k * 4 + field]
-};
+template <class R> struct AdjOcc;  // CTAs per SM the tile kernels are built for
+template <> struct AdjOcc<float> { static constexpr int stage2 = 3, stage1 = 3; };
+template <> struct AdjOcc<double> { static constexpr int stage2 = 2, stage1 = 2; };
 
-// C: stage-2 walls reverse; face i along AX is the left wall of cell i and
-// the right wall of cell i - e.  The HLLC reverse gives the cotangents of the
-// reconstructed face states; the MUSCL reverse spreads them over the four
-// stencil cells, stored per stencil slot for the gather in D.
+// MUSCL reverse of the four fields of one face into its 16 slot values
 template <class R>
-__global__ void __launch_bounds__(256, 3)
-adj_stage2_faces(Fields<R> Q, Fields<R> U2b, SlotBar<R> SX, SlotBar<R> SY, Geo<R> G) {
-  G.dt = (R)*G.dtp;
-  const size_t n = (size_t)G.n0 * G.n1;
+__device__ __forceinline__ void face_slots(const Prim<R> st[4], const PrimBar<R> &Lb,
+                                           const PrimBar<R> &Rb, R out[16]) {
+  const R lb[4] = {Lb.rho, Lb.v0, Lb.v1, Lb.p}, rb[4] = {Rb.rho, Rb.v0, Rb.v1, Rb.p};
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    R xb[4] = {0, 0, 0, 0};
+    ha::muscl_rev((&st[0].rho)[c], (&st[1].rho)[c], (&st[2].rho)[c], (&st[3].rho)[c], lb[c],
+                  rb[c], xb[0], xb[1], xb[2], xb[3]);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) out[k * 4 + c] = xb[k];
+  }
+}
+
+// HLLC and MUSCL reverse of one stage-2 face along AX: stencil st[4] (the
+// stage-1 states of cells f-2 .. f+1), wall-flux cotangent fb -> 16 slots
+template <int AX, class R>
+__device__ __forceinline__ void face2_rev(R g, const Prim<R> st[4], const Flux<R> &fb,
+                                          R out[16]) {
+  Prim<R> L, Rt;
+  hs::muscl(st[0].rho, st[1].rho, st[2].rho, st[3].rho, L.rho, Rt.rho);
+  hs::muscl(st[0].v0, st[1].v0, st[2].v0, st[3].v0, L.v0, Rt.v0);
+  hs::muscl(st[0].v1, st[1].v1, st[2].v1, st[3].v1, L.v1, Rt.v1);
+  hs::muscl(st[0].p, st[1].p, st[2].p, st[3].p, L.p, Rt.p);
+  PrimBar<R> Lb, Rb;
+  ha::zero(Lb);
+  ha::zero(Rb);
+  ha::hllc_rev<AX>(g, L, Rt, fb, Lb, Rb);
+  face_slots(st, Lb, Rb, out);
+}
+
+// C+D: stage-2 walls reverse (HLLC and MUSCL of the faces around the tile,
+// cotangents kept per stencil slot in shared memory), then per tile cell the
+// gather into Qb (face f = q + df holds the cell in slot 2 - df) and the
+// stage-1 update reverse.
+template <class R, int TX, int TY>
+__global__ void __launch_bounds__(256, AdjOcc<R>::stage2)
+adj_stage2_tile(Fields<R> Q, Fields<R> U2b, FluxStore<R> F1, Fields<R> U1b, Fields<R> Pbase,
+                Geo<R> G, double *partial) {
+  using S = Stage2Smem<R, TX, TY>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  S &s = *reinterpret_cast<S *>(smem_raw);
+  __shared__ double sh[8];
+  G.dt = (R)G.in->dt;
+  const Fields<R> P = G.state();
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int nt0 = (G.n0 + TX - 1) / TX;
+  const int X0 = (int)(blockIdx.x % nt0) * TX, Y0 = (int)(blockIdx.x / nt0) * TY;
+  for (int i = tid; i < S::QY * S::QX; i += nthr) {
+    const int by = i / S::QX, bx = i - by * S::QX;
+    const size_t gi = G.at(X0 - 3 + bx, Y0 - 3 + by);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) s.q[c][by][bx] = Q.f[c][gi];
+  }
+  for (int i = tid; i < S::UY * S::UX; i += nthr) {
+    const int by = i / S::UX, bx = i - by * S::UX;
+    const size_t gi = G.at(X0 - 2 + bx, Y0 - 2 + by);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) s.u[c][by][bx] = U2b.f[c][gi];
+  }
+  __syncthreads();
   const R d0 = G.dt / G.dR0, d1 = G.dt / G.dR1;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x) {
-    const int y = (int)(i / G.n0), x = (int)(i - (size_t)y * G.n0);
+  // x faces: face X0-1+j of row Y0+r has stencil box columns j..j+3 of box
+  // row r+3 and cells (right, left) at U2b box columns j+1, j of row r+2
+  for (int i = tid; i < TY * S::XF; i += nthr) {
+    const int r = i / S::XF, j = i - r * S::XF;
+    Prim<R> st[4];
 #pragma unroll
-    for (int ax = 0; ax < 2; ++ax) {
-      const size_t im = ax == 0 ? G.at(x - 1, y) : G.at(x, y - 1);
-      const R dd = ax == 0 ? d0 : d1;
-      const Prim<R> a = U2b.get(i), c = U2b.get(im);
-      const Flux<R> fb{dd * (a.rho - c.rho), dd * (a.v0 - c.v0), dd * (a.v1 - c.v1),
-                       dd * (a.p - c.p)};
-      Prim<R> L, Rt, st[4];
-      PrimBar<R> Lb, Rb;
-      ha::zero(Lb);
-      ha::zero(Rb);
-      if (ax == 0) {
-        face2_states<0>(Q, G, x, y, L, Rt, st);
-        ha::hllc_rev<0>(G.g, L, Rt, fb, Lb, Rb);
-      } else {
-        face2_states<1>(Q, G, x, y, L, Rt, st);
-        ha::hllc_rev<1>(G.g, L, Rt, fb, Lb, Rb);
-      }
-      SlotBar<R> &S = ax == 0 ? SX : SY;
-      const R lb[4] = {Lb.rho, Lb.v0, Lb.v1, Lb.p}, rb[4] = {Rb.rho, Rb.v0, Rb.v1, Rb.p};
+    for (int k = 0; k < 4; ++k)
+      st[k] = Prim<R>{s.q[0][r + 3][j + k], s.q[1][r + 3][j + k], s.q[2][r + 3][j + k],
+                      s.q[3][r + 3][j + k]};
+    const Flux<R> fb{d0 * (s.u[0][r + 2][j + 1] - s.u[0][r + 2][j]),
+                     d0 * (s.u[1][r + 2][j + 1] - s.u[1][r + 2][j]),
+                     d0 * (s.u[2][r + 2][j + 1] - s.u[2][r + 2][j]),
+                     d0 * (s.u[3][r + 2][j + 1] - s.u[3][r + 2][j])};
+    R out[16];
+    face2_rev<0>(G.g, st, fb, out);
 #pragma unroll
-      for (int c4 = 0; c4 < 4; ++c4) {
-        R xb[4] = {0, 0, 0, 0};
-        const R *xs = &st[0].rho;
-        ha::muscl_rev((&st[0].rho)[c4], (&st[1].rho)[c4], (&st[2].rho)[c4], (&st[3].rho)[c4],
-                      lb[c4], rb[c4], xb[0], xb[1], xb[2], xb[3]);
-        (void)xs;
+    for (int k = 0; k < 16; ++k) s.slot[k][i] = out[k];
+  }
+  __syncthreads();
+  for (int i = tid; i < TX * TY; i += nthr) {
+    const int ty = i / TX, tx = i - ty * TX;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) S.f[k * 4 + c4][i] = xb[k];
-      }
+    for (int c = 0; c < 4; ++c) {
+      R acc = R(0);
+#pragma unroll
+      for (int df = -1; df <= 2; ++df) acc += s.slot[(2 - df) * 4 + c][ty * S::XF + tx + df + 1];
+      s.qx[c][ty][tx] = acc;
     }
   }
-}
-
-// D: gather the reconstruction cotangents into Qb (face f = q + df holds this
-// cell in stencil slot 2 - df), then stage-1 update reverse
-template <class R>
-__global__ void __launch_bounds__(256)
-adj_stage1_cells(Fields<R> P, FluxStore<R> F1, SlotBar<R> SX, SlotBar<R> SY, Fields<R> U1b,
-                 Fields<R> Pbase, Geo<R> G, double *partial) {
-  G.dt = (R)*G.dtp;
-  __shared__ double sh[8];
-  const size_t n = (size_t)G.n0 * G.n1;
+  __syncthreads();
+  // y faces: face Y0-1+j of column X0+r has stencil box rows j..j+3 of box
+  // column r+3 and cells at U2b box rows j+1, j of column r+2
+  for (int i = tid; i < S::YF * TX; i += nthr) {
+    const int j = i / TX, r = i - j * TX;
+    Prim<R> st[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      st[k] = Prim<R>{s.q[0][j + k][r + 3], s.q[1][j + k][r + 3], s.q[2][j + k][r + 3],
+                      s.q[3][j + k][r + 3]};
+    const Flux<R> fb{d1 * (s.u[0][j + 1][r + 2] - s.u[0][j][r + 2]),
+                     d1 * (s.u[1][j + 1][r + 2] - s.u[1][j][r + 2]),
+                     d1 * (s.u[2][j + 1][r + 2] - s.u[2][j][r + 2]),
+                     d1 * (s.u[3][j + 1][r + 2] - s.u[3][j][r + 2])};
+    R out[16];
+    face2_rev<1>(G.g, st, fb, out);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) s.slot[k][i] = out[k];
+  }
+  __syncthreads();
   const R h = G.dt / R(2);
-  const R d0 = h / G.dR0, d1 = h / G.dR1;
+  const R e0 = h / G.dR0, e1 = h / G.dR1;
   const R rdR0 = R(1) / G.dR0, rdR1 = R(1) / G.dR1;
   double dtb = 0;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x) {
-    const int y = (int)(i / G.n0), x = (int)(i - (size_t)y * G.n0);
-    R qb[4] = {0, 0, 0, 0};
+  for (int i = tid; i < TX * TY; i += nthr) {
+    const int ty = i / TX, tx = i - ty * TX;
+    const int x = X0 + tx, y = Y0 + ty;
+    if (x >= G.n0 || y >= G.n1) continue;
+    R qb[4];
 #pragma unroll
-    for (int df = -1; df <= 2; ++df) {
-      const size_t fx = G.at(x + df, y), fy = G.at(x, y + df);
-      const int k = 2 - df;
+    for (int c = 0; c < 4; ++c) {
+      R acc = R(0);
 #pragma unroll
-      for (int c = 0; c < 4; ++c) qb[c] += SX.f[k * 4 + c][fx] + SY.f[k * 4 + c][fy];
+      for (int df = -1; df <= 2; ++df) acc += s.slot[(2 - df) * 4 + c][(ty + df + 1) * TX + tx];
+      qb[c] = s.qx[c][ty][tx] + acc;
     }
-    const Flux<R> l0 = F1.get(0, i), r0 = F1.get(0, G.at(x + 1, y));
-    const Flux<R> l1 = F1.get(1, i), r1 = F1.get(1, G.at(x, y + 1));
-    const Prim<R> b = P.get(i);
+    const size_t gi = (size_t)y * G.n0 + x;
+    const Flux<R> l0 = F1.get(0, gi), r0 = F1.get(0, G.at(x + 1, y));
+    const Flux<R> l1 = F1.get(1, gi), r1 = F1.get(1, G.at(x, y + 1));
+    const Prim<R> b = P.get(gi);
     R u[4];
-    ha::update_cons(G.g, b, d0, d1, l0, r0, l1, r1, u);
+    ha::update_cons(G.g, b, e0, e1, l0, r0, l1, r1, u);
     const PrimBar<R> qbar{qb[0], qb[1], qb[2], qb[3]};
     R U[4];
     ha::cons_from_prim_rev(G.g, u[0], u[1], u[2], u[3], qbar, U);
-    U1b.set(i, Prim<R>{U[0], U[1], U[2], U[3]});
+    U1b.set(gi, Prim<R>{U[0], U[1], U[2], U[3]});
     PrimBar<R> bb;
-    const Prim<R> pb0 = Pbase.get(i);
+    const Prim<R> pb0 = Pbase.get(gi);
     bb.rho = pb0.rho; bb.v0 = pb0.v0; bb.v1 = pb0.v1; bb.p = pb0.p;
     ha::cons_of_prim_rev(G.g, b, U, bb);
-    Pbase.set(i, Prim<R>{bb.rho, bb.v0, bb.v1, bb.p});
+    Pbase.set(gi, Prim<R>{bb.rho, bb.v0, bb.v1, bb.p});
     const R t0 = U[0] * (l0.fd - r0.fd) + U[1] * (l0.fm0 - r0.fm0) + U[2] * (l0.fm1 - r0.fm1) +
                  U[3] * (l0.fe - r0.fe);
     const R t1 = U[0] * (l1.fd - r1.fd) + U[1] * (l1.fm0 - r1.fm0) + U[2] * (l1.fm1 - r1.fm1) +
@@ -319,58 +452,85 @@ adj_stage1_cells(Fields<R> P, FluxStore<R> F1, SlotBar<R> SX, SlotBar<R> SY, Fie
     // dtdx = (dt / 2) / dR
     dtb += (double)(R(0.5) * (t0 * rdR0 + t1 * rdR1));
   }
-  const double s = block_sum(dtb, sh);
-  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+  const double sum = block_sum(dtb, sh);
+  if (tid == 0) partial[blockIdx.x] = sum;
 }
 
-// E: stage-1 walls reverse
-template <class R>
-__global__ void __launch_bounds__(256, 3)
-adj_stage1_faces(Fields<R> P, Fields<R> U1b, FaceBar<R> FX, FaceBar<R> FY, Geo<R> G) {
-  G.dt = (R)*G.dtp;
-  const size_t n = (size_t)G.n0 * G.n1;
+// E+F on one TX x TY tile: the face cotangents (left-state part 0..3,
+// right-state part 4..7) of x faces X0 .. X0+TX of each tile row and y faces
+// Y0 .. Y0+TY of each tile column, then per tile cell the previous-state
+// cotangent = base part + its own walls (right state) + the next walls
+// (left state), and the lowest index whose CFL timescale equals the minimum
+// (the arg-min that receives the dt cotangent; ties go to the lowest index).
+template <class R, int TX, int TY> struct Stage1Smem {
+  static constexpr int XF = TX + 1, YF = TY + 1;
+  R fx[8][TY][XF];
+  R fy[8][YF][TX];
+};
+
+template <class R, int TX, int TY>
+__global__ void __launch_bounds__(256, AdjOcc<R>::stage1)
+adj_stage1_tile(Fields<R> U1b, Fields<R> Pbase, Fields<R> Pb, Geo<R> G,
+                const unsigned long long *minbits, unsigned long long *argmin) {
+  using S = Stage1Smem<R, TX, TY>;
+  __shared__ S s;
+  G.dt = (R)G.in->dt;
+  const Fields<R> P = G.state();
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int nt0 = (G.n0 + TX - 1) / TX;
+  const int X0 = (int)(blockIdx.x % nt0) * TX, Y0 = (int)(blockIdx.x / nt0) * TY;
   const R h = G.dt / R(2);
   const R d0 = h / G.dR0, d1 = h / G.dR1;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x) {
-    const int y = (int)(i / G.n0), x = (int)(i - (size_t)y * G.n0);
-#pragma unroll
-    for (int ax = 0; ax < 2; ++ax) {
-      const size_t im = ax == 0 ? G.at(x - 1, y) : G.at(x, y - 1);
-      const R dd = ax == 0 ? d0 : d1;
-      const Prim<R> a = U1b.get(i), c = U1b.get(im);
-      const Flux<R> fb{dd * (a.rho - c.rho), dd * (a.v0 - c.v0), dd * (a.v1 - c.v1),
-                       dd * (a.p - c.p)};
-      const Prim<R> L = P.get(im), Rt = P.get(i);
-      PrimBar<R> Lb, Rb;
-      ha::zero(Lb);
-      ha::zero(Rb);
-      if (ax == 0) ha::hllc_rev<0>(G.g, L, Rt, fb, Lb, Rb);
-      else ha::hllc_rev<1>(G.g, L, Rt, fb, Lb, Rb);
-      FaceBar<R> &F = ax == 0 ? FX : FY;
-      F.f[0][i] = Lb.rho; F.f[1][i] = Lb.v0; F.f[2][i] = Lb.v1; F.f[3][i] = Lb.p;
-      F.f[4][i] = Rb.rho; F.f[5][i] = Rb.v0; F.f[6][i] = Rb.v1; F.f[7][i] = Rb.p;
+  constexpr int NXF = TY * S::XF, NYF = S::YF * TX;
+  for (int i = tid; i < NXF + NYF; i += nthr) {
+    PrimBar<R> Lb, Rb;
+    ha::zero(Lb);
+    ha::zero(Rb);
+    int r, j;
+    if (i < NXF) {
+      r = i / S::XF;
+      j = i - r * S::XF;
+      const size_t ic = G.at(X0 + j, Y0 + r), im = G.at(X0 + j - 1, Y0 + r);
+      const Prim<R> a = U1b.get(ic), c = U1b.get(im);
+      const Flux<R> fb{d0 * (a.rho - c.rho), d0 * (a.v0 - c.v0), d0 * (a.v1 - c.v1),
+                       d0 * (a.p - c.p)};
+      ha::hllc_rev<0>(G.g, P.get(im), P.get(ic), fb, Lb, Rb);
+      s.fx[0][r][j] = Lb.rho; s.fx[1][r][j] = Lb.v0; s.fx[2][r][j] = Lb.v1; s.fx[3][r][j] = Lb.p;
+      s.fx[4][r][j] = Rb.rho; s.fx[5][r][j] = Rb.v0; s.fx[6][r][j] = Rb.v1; s.fx[7][r][j] = Rb.p;
+    } else {
+      const int i2 = i - NXF;
+      j = i2 / TX;
+      r = i2 - j * TX;
+      const size_t ic = G.at(X0 + r, Y0 + j), im = G.at(X0 + r, Y0 + j - 1);
+      const Prim<R> a = U1b.get(ic), c = U1b.get(im);
+      const Flux<R> fb{d1 * (a.rho - c.rho), d1 * (a.v0 - c.v0), d1 * (a.v1 - c.v1),
+                       d1 * (a.p - c.p)};
+      ha::hllc_rev<1>(G.g, P.get(im), P.get(ic), fb, Lb, Rb);
+      s.fy[0][j][r] = Lb.rho; s.fy[1][j][r] = Lb.v0; s.fy[2][j][r] = Lb.v1; s.fy[3][j][r] = Lb.p;
+      s.fy[4][j][r] = Rb.rho; s.fy[5][j][r] = Rb.v0; s.fy[6][j][r] = Rb.v1; s.fy[7][j][r] = Rb.p;
     }
   }
-}
-
-// F: previous-state cotangent = base part + stage-1 walls (the cell is the
-// right state of its own wall and the left state of the next wall)
-template <class R>
-__global__ void __launch_bounds__(256)
-adj_gather(Fields<R> Pbase, FaceBar<R> FX, FaceBar<R> FY, Fields<R> Pb, Geo<R> G) {
-  const size_t n = (size_t)G.n0 * G.n1;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x) {
-    const int y = (int)(i / G.n0), x = (int)(i - (size_t)y * G.n0);
-    const size_t ix = G.at(x + 1, y), iy = G.at(x, y + 1);
-    Prim<R> b = Pbase.get(i);
-    b.rho += FX.f[4][i] + FX.f[0][ix] + FY.f[4][i] + FY.f[0][iy];
-    b.v0 += FX.f[5][i] + FX.f[1][ix] + FY.f[5][i] + FY.f[1][iy];
-    b.v1 += FX.f[6][i] + FX.f[2][ix] + FY.f[6][i] + FY.f[2][iy];
-    b.p += FX.f[7][i] + FX.f[3][ix] + FY.f[7][i] + FY.f[3][iy];
-    Pb.set(i, b);
+  __syncthreads();
+  const unsigned long long mb = *minbits;
+  unsigned long long best = ~0ull;
+  for (int i = tid; i < TX * TY; i += nthr) {
+    const int ty = i / TX, tx = i - ty * TX;
+    const int x = X0 + tx, y = Y0 + ty;
+    if (x >= G.n0 || y >= G.n1) continue;
+    const size_t gi = (size_t)y * G.n0 + x;
+    const Prim<R> q = P.get(gi);
+    if (hk::ts_bits<R>(hs::timescale(G.g, G.dR0, G.dR1, q.rho, q.v0, q.v1, q.p)) == mb &&
+        gi < best)
+      best = gi;
+    Prim<R> b = Pbase.get(gi);
+    b.rho += s.fx[4][ty][tx] + s.fx[0][ty][tx + 1] + s.fy[4][ty][tx] + s.fy[0][ty + 1][tx];
+    b.v0 += s.fx[5][ty][tx] + s.fx[1][ty][tx + 1] + s.fy[5][ty][tx] + s.fy[1][ty + 1][tx];
+    b.v1 += s.fx[6][ty][tx] + s.fx[2][ty][tx + 1] + s.fy[6][ty][tx] + s.fy[2][ty + 1][tx];
+    b.p += s.fx[7][ty][tx] + s.fx[3][ty][tx + 1] + s.fy[7][ty][tx] + s.fy[3][ty + 1][tx];
+    Pb.set(gi, b);
   }
+  best = warp_min(best);
+  if ((tid & 31) == 0 && best != ~0ull) atomicMin(argmin, best);
 }
 
 // G: dt cotangent to the arg-min cell.  The block partials are summed by one
@@ -378,7 +538,7 @@ adj_gather(Fields<R> Pbase, FaceBar<R> FX, FaceBar<R> FY, Fields<R> Pb, Geo<R> G
 // result does not depend on scheduling.
 template <class R>
 __global__ void __launch_bounds__(256)
-adj_dt(Fields<R> P, Fields<R> Pb, Geo<R> G, const double *partials, int nparts, R cfl,
+adj_dt(Fields<R> Pb, Geo<R> G, const double *partials, int nparts, R cfl,
        const unsigned long long *argmin, double *dtb_out) {
   __shared__ double sh[256];
   double acc = 0;
@@ -397,7 +557,7 @@ adj_dt(Fields<R> P, Fields<R> Pb, Geo<R> G, const double *partials, int nparts, 
   const R tb = (R)(dtb * (double)cfl);
   PrimBar<R> xb;
   ha::zero(xb);
-  ha::timescale_rev(G.g, G.dR0, G.dR1, P.get(j), tb, xb);
+  ha::timescale_rev(G.g, G.dR0, G.dR1, G.state().get(j), tb, xb);
   Prim<R> b = Pb.get(j);
   b.rho += xb.rho; b.v0 += xb.v0; b.v1 += xb.v1; b.p += xb.p;
   Pb.set(j, b);
@@ -428,16 +588,16 @@ adj_loss(const R *rho, const R *target, R *rhob, size_t n, double *partial) {
 struct AdjointScratch {
   int fp64 = -1;
   size_t cells = 0;
-  void *q[4], *u2b[4], *u1b[4], *pbase[4], *fx[8], *fy[8], *ub[4], *pb[4], *f1[8], *f2[8];
-  void *sx[16], *sy[16];
-  void *stage[4];                 // the state a graph-captured step reads
-  double *d_dt = nullptr;         // dt of the step being reversed
+  void *q[4], *u2b[4], *u1b[4], *pbase[4], *ub[4], *pb[4], *f1[8];
+  adj::StepIn *d_in = nullptr;    // the step being reversed (device)
+  adj::StepIn *h_in1 = nullptr;   // pinned slot for single steps
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // by cotangent buffer parity
-  void *graph_ub[2] = {nullptr, nullptr};
+  void *graph_io[2][8] = {};        // ub[4], pb[4] each graph was captured with
   double graph_scalars[2][3] = {};  // cfl, dR0, dR1 each graph was captured with
   double *partials = nullptr;
   unsigned long long *argmin = nullptr;
-  int nparts = 0;
+  int nparts = 0;   // blocks of the grid-stride kernels
+  int ntiles = 0;   // tiles of the fused reverse kernels
   std::vector<void *> all;
 };
 
@@ -445,7 +605,8 @@ static void free_scratch(AdjointScratch *s) {
   if (!s) return;
   for (int k = 0; k < 2; ++k)
     if (s->graph[k]) cudaGraphExecDestroy(s->graph[k]);
-  cudaFree(s->d_dt);
+  cudaFree(s->d_in);
+  cudaFreeHost(s->h_in1);
   for (void *p : s->all) cudaFree(p);
   cudaFree(s->partials);
   cudaFree(s->argmin);
@@ -455,7 +616,22 @@ static void free_scratch(AdjointScratch *s) {
 // scratch hangs off the handle's kind state through a small registry
 static std::vector<std::pair<Handle *, AdjointScratch *>> g_scratch;
 
+template <class R> static cudaError_t allow_tile_smem() {
+  constexpr int TX = adj::AdjTile<R>::TX, TY = adj::AdjTile<R>::TY;
+  cudaError_t e = cudaFuncSetAttribute(adj::adj_forward_tile<R, TX, TY>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)sizeof(FusedSmem<R, TX, TY>));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(adj::adj_stage2_tile<R, TX, TY>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)sizeof(adj::Stage2Smem<R, TX, TY>));
+}
+
 static om_status get_scratch(Handle *h, int fp64, AdjointScratch **out) {
+  if (!h->cyclic) {
+    set_error("Hydro adjoint: periodic grids only");
+    return OM_ERR_UNSUPPORTED;
+  }
   for (auto &kv : g_scratch)
     if (kv.first == h) {
       *out = kv.second;
@@ -465,10 +641,9 @@ static om_status get_scratch(Handle *h, int fp64, AdjointScratch **out) {
   s->fp64 = fp64;
   s->cells = h->memory_size_total();
   const size_t bytes = s->cells * (fp64 ? 8 : 4);
-  void **groups[13] = {s->q,  s->u2b, s->u1b, s->pbase, s->ub, s->pb,   s->fx,
-                       s->fy, s->f1,  s->f2,  s->sx,    s->sy, s->stage};
-  const int sizes[13] = {4, 4, 4, 4, 4, 4, 8, 8, 8, 8, 16, 16, 4};
-  for (int gi = 0; gi < 13; ++gi)
+  void **groups[7] = {s->q, s->u2b, s->u1b, s->pbase, s->ub, s->pb, s->f1};
+  const int sizes[7] = {4, 4, 4, 4, 4, 4, 8};
+  for (int gi = 0; gi < 7; ++gi)
     for (int k = 0; k < sizes[gi]; ++k) {
       void *p = nullptr;
       if (cudaMalloc(&p, bytes) != cudaSuccess) {
@@ -481,8 +656,15 @@ static om_status get_scratch(Handle *h, int fp64, AdjointScratch **out) {
       s->all.push_back(p);
     }
   s->nparts = 2 * sm_count(h->device) * 4;
-  if (cudaMalloc(&s->partials, sizeof(double) * 2 * s->nparts) != cudaSuccess ||
-      cudaMalloc(&s->d_dt, sizeof(double)) != cudaSuccess ||
+  const int tx = fp64 ? adj::AdjTile<double>::TX : adj::AdjTile<float>::TX;
+  const int ty = fp64 ? adj::AdjTile<double>::TY : adj::AdjTile<float>::TY;
+  s->ntiles = ((h->size[0] + tx - 1) / tx) * ((h->size[1] + ty - 1) / ty);
+  const cudaError_t ea = fp64 ? allow_tile_smem<double>() : allow_tile_smem<float>();
+  if (ea != cudaSuccess ||
+      cudaMalloc(&s->partials, sizeof(double) * std::max(s->nparts, 2 * s->ntiles)) !=
+          cudaSuccess ||
+      cudaMalloc(&s->d_in, sizeof(adj::StepIn)) != cudaSuccess ||
+      cudaMallocHost(&s->h_in1, sizeof(adj::StepIn)) != cudaSuccess ||
       cudaMalloc(&s->argmin, 2 * sizeof(unsigned long long)) != cudaSuccess) {
     cudaGetLastError();
     free_scratch(s);
@@ -507,93 +689,65 @@ template <class R> static adj::Fields<R> F4(void *const *p) {
   return adj::Fields<R>{{(R *)p[0], (R *)p[1], (R *)p[2], (R *)p[3]}};
 }
 
-template <class R> static adj::FaceBar<R> F8(void *const *p) {
-  adj::FaceBar<R> f;
-  for (int k = 0; k < 8; ++k) f.f[k] = (R *)p[k];
-  return f;
-}
-
-template <class R> static adj::SlotBar<R> S16(void *const *p) {
-  adj::SlotBar<R> f;
-  for (int k = 0; k < 16; ++k) f.f[k] = (R *)p[k];
-  return f;
-}
-
 template <class R> static adj::FluxStore<R> FS(void *const *p) {
   adj::FluxStore<R> f;
   for (int k = 0; k < 8; ++k) f.f[k] = (R *)p[k];
   return f;
 }
 
-// One adjoint step at state `state` (4 device arrays) with step dt (in R)
-// and CFL minimum bits: ub (4 device arrays, cotangent of the next state)
-// -> pb_out (4 device arrays).  Returns the dt cotangent when dtb_out.
+// kernels of one adjoint step (the three tile kernels and the dt kernel)
+constexpr int kVjpLaunches = 4;
+
+// The kernels of one adjoint step, reading the step's dt and state from
+// s->d_in: ub (4 device arrays, cotangent of the state after the step) ->
+// pb_out (4 device arrays, cotangent of the state before it).
 template <class R>
-static om_status vjp_kernels(Handle *h, AdjointScratch *s, void *const *state, void *const *ub,
-                             void *const *pb_out, double cfl, unsigned long long tsbits,
-                             double *dtb_dev) {
+static om_status vjp_kernels(Handle *h, AdjointScratch *s, void *const *ub, void *const *pb_out,
+                             double cfl) {
   const cudaStream_t st = h->stream;
   const HydroScalars *hs_ = (const HydroScalars *)h->h_scalars;
-  adj::Geo<R> G{h->size[0], h->size[1], (R)h->cfg.gamma, (R)hs_->dR0, (R)hs_->dR1, R(0), s->d_dt};
-  const int grid = s->nparts;
-  const auto P = F4<R>(state), Q = F4<R>(s->q), U = F4<R>(ub), U2b = F4<R>(s->u2b),
-             U1b = F4<R>(s->u1b), Pbase = F4<R>(s->pbase), Pb = F4<R>(pb_out);
-  const auto FX = F8<R>(s->fx), FY = F8<R>(s->fy);
-  const auto F1 = FS<R>(s->f1), F2 = FS<R>(s->f2);
-  const auto SX = S16<R>(s->sx), SY = S16<R>(s->sy);
-  (void)tsbits;
+  const int cheap = h->size[0] >= adj::kCheapWrap && h->size[1] >= adj::kCheapWrap;
+  adj::Geo<R> G{h->size[0], h->size[1], (R)h->cfg.gamma, (R)hs_->dR0, (R)hs_->dR1, R(0),
+                s->d_in,    cheap};
+  const int nt = s->ntiles;
+  constexpr int TX = adj::AdjTile<R>::TX, TY = adj::AdjTile<R>::TY;
+  const auto Q = F4<R>(s->q), U = F4<R>(ub), U2b = F4<R>(s->u2b), U1b = F4<R>(s->u1b),
+             Pbase = F4<R>(s->pbase), Pb = F4<R>(pb_out);
+  const auto F1 = FS<R>(s->f1);
+  // argmin[0]: arg-min cell, argmin[1]: minimum timescale bits
   OM_CUDA_CHECK(cudaMemsetAsync(s->argmin, 0xFF, 2 * sizeof(unsigned long long), st));
-  adj::adj_walls1<R><<<grid, 256, 0, st>>>(P, F1, G, s->argmin + 1);
-  adj::adj_stage1<R><<<grid, 256, 0, st>>>(P, F1, Q, G, s->argmin + 1, s->argmin);
-  adj::adj_walls2<R><<<grid, 256, 0, st>>>(Q, F2, G);
-  adj::adj_stage2_cells<R><<<grid, 256, 0, st>>>(P, F2, U, U2b, Pbase, G, s->partials);
-  adj::adj_stage2_faces<R><<<grid, 256, 0, st>>>(Q, U2b, SX, SY, G);
-  adj::adj_stage1_cells<R><<<grid, 256, 0, st>>>(P, F1, SX, SY, U1b, Pbase, G,
-                                                 s->partials + grid);
-  adj::adj_stage1_faces<R><<<grid, 256, 0, st>>>(P, U1b, FX, FY, G);
-  adj::adj_gather<R><<<grid, 256, 0, st>>>(Pbase, FX, FY, Pb, G);
-  adj::adj_dt<R><<<1, 256, 0, st>>>(P, Pb, G, s->partials, 2 * grid, (R)cfl, s->argmin, dtb_dev);
+  adj::adj_forward_tile<R, TX, TY><<<nt, 256, sizeof(FusedSmem<R, TX, TY>), st>>>(
+      U, Q, F1, U2b, Pbase, G, s->partials, s->argmin + 1);
+  adj::adj_stage2_tile<R, TX, TY><<<nt, 256, sizeof(adj::Stage2Smem<R, TX, TY>), st>>>(
+      Q, U2b, F1, U1b, Pbase, G, s->partials + nt);
+  adj::adj_stage1_tile<R, TX, TY><<<nt, 256, 0, st>>>(U1b, Pbase, Pb, G, s->argmin + 1,
+                                                      s->argmin);
+  adj::adj_dt<R><<<1, 256, 0, st>>>(Pb, G, s->partials, 2 * nt, (R)cfl, s->argmin, nullptr);
   OM_CUDA_CHECK(cudaGetLastError());
   return OM_OK;
 }
 
-// One adjoint step on caller buffers without a graph (synchronous dt upload)
+// One adjoint step.  `slot` (pinned host memory, left untouched until the
+// stream has passed this step) holds the step's dt and state; it is copied
+// to s->d_in, then the kernel sequence runs from a CUDA graph captured once
+// per pair of cotangent buffers (and per cfl, dR0, dR1).
 template <class R>
-static om_status vjp_kernels_direct(Handle *h, AdjointScratch *s, void *const *state,
-                                    void *const *ub, void *const *pb_out, double dt, double cfl,
-                                    unsigned long long tsbits) {
-  OM_CUDA_CHECK(cudaMemcpyAsync(s->d_dt, &dt, sizeof(double), cudaMemcpyHostToDevice, h->stream));
-  OM_CUDA_CHECK(cudaStreamSynchronize(h->stream));
-  OM_TRY(vjp_kernels<R>(h, s, state, ub, pb_out, cfl, tsbits, nullptr));
-  h->launches += 9;
-  return OM_OK;
-}
-
-// One adjoint step: the step's dt (from host memory that stays untouched
-// until the stream has read it) and the state go to fixed device buffers,
-// then the kernel sequence runs from a CUDA graph captured once per
-// cotangent buffer pair.
-template <class R>
-static om_status vjp_step(Handle *h, AdjointScratch *s, void *const *state, void *const *ub,
-                          void *const *pb_out, const double *dt_host, double cfl,
-                          unsigned long long tsbits, double *dtb_dev) {
+static om_status vjp_step(Handle *h, AdjointScratch *s, const adj::StepIn *slot,
+                          void *const *ub, void *const *pb_out, double cfl) {
   const cudaStream_t st = h->stream;
-  const size_t bytes = s->cells * sizeof(R);
-  OM_CUDA_CHECK(cudaMemcpyAsync(s->d_dt, dt_host, sizeof(double), cudaMemcpyHostToDevice, st));
-  for (int k = 0; k < 4; ++k)
-    if (state[k] != s->stage[k])
-      OM_CUDA_CHECK(cudaMemcpyAsync(s->stage[k], state[k], bytes, cudaMemcpyDeviceToDevice, st));
+  OM_CUDA_CHECK(
+      cudaMemcpyAsync(s->d_in, slot, sizeof(adj::StepIn), cudaMemcpyHostToDevice, st));
   const int key = ub[0] == s->ub[0] ? 0 : 1;
-  // scalars baked into the captured kernel arguments
+  void *io[8] = {ub[0], ub[1], ub[2], ub[3], pb_out[0], pb_out[1], pb_out[2], pb_out[3]};
   const HydroScalars *hs_ = (const HydroScalars *)h->h_scalars;
   const double baked[3] = {cfl, hs_->dR0, hs_->dR1};
-  if (!s->graph[key] || s->graph_ub[key] != ub[0] ||
+  if (!s->graph[key] || std::memcmp(io, s->graph_io[key], sizeof(io)) != 0 ||
       std::memcmp(baked, s->graph_scalars[key], sizeof(baked)) != 0) {
     if (s->graph[key]) cudaGraphExecDestroy(s->graph[key]);
     s->graph[key] = nullptr;
     cudaGraph_t g = nullptr;
     OM_CUDA_CHECK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    om_status r = vjp_kernels<R>(h, s, s->stage, ub, pb_out, cfl, tsbits, dtb_dev);
+    om_status r = vjp_kernels<R>(h, s, ub, pb_out, cfl);
     cudaError_t ce = cudaStreamEndCapture(st, &g);
     if (r != OM_OK) { if (g) cudaGraphDestroy(g); return r; }
     if (ce != cudaSuccess) {
@@ -606,17 +760,37 @@ static om_status vjp_step(Handle *h, AdjointScratch *s, void *const *state, void
       set_error(std::string("adjoint graph instantiate: ") + cudaGetErrorString(ce));
       return OM_ERR_CUDA;
     }
-    s->graph_ub[key] = ub[0];
+    std::memcpy(s->graph_io[key], io, sizeof(io));
     std::memcpy(s->graph_scalars[key], baked, sizeof(baked));
   }
   OM_CUDA_CHECK(cudaGraphLaunch(s->graph[key], st));
-  h->launches += 9;
+  h->launches += kVjpLaunches;
   return OM_OK;
+}
+
+static om_status run_vjp_step(Handle *h, AdjointScratch *s, const adj::StepIn *slot,
+                              void *const *ub, void *const *pb, double cfl) {
+  return s->fp64 ? vjp_step<double>(h, s, slot, ub, pb, cfl)
+                 : vjp_step<float>(h, s, slot, ub, pb, cfl);
 }
 
 }  // namespace om
 
 using namespace om;
+
+// The record of a checkpointed forward run, consumed by om_hydro_backward.
+struct om_hydro_tape_s {
+  Handle *h = nullptr;
+  int steps = 0, seg = 0, nck = 0;
+  std::vector<HydroCheckpoint> ck;     // state before segment j, and the final state
+  std::vector<HydroCheckpoint> segst;  // states of one recomputed segment
+  adj::StepIn *h_in = nullptr;         // pinned: one record per step
+  ~om_hydro_tape_s() {
+    for (auto &c : ck) hydro_checkpoint_free(&c);
+    for (auto &c : segst) hydro_checkpoint_free(&c);
+    if (h_in) cudaFreeHost(h_in);
+  }
+};
 
 extern "C" om_status om_hydro_vjp(om_handle H, void *const *cot_next, void *const *cot_prev) {
   Handle *h = handle_of(H);
@@ -629,22 +803,142 @@ extern "C" om_status om_hydro_vjp(om_handle H, void *const *cot_next, void *cons
   AdjointScratch *s;
   OM_TRY(get_scratch(h, fp64, &s));
   for (int i = 0; i < 4; ++i) OM_TRY(bring_device(h, h->arrays[i]));
-  double dt;
+  // the pinned slot may still feed a step in flight
+  OM_CUDA_CHECK(cudaStreamSynchronize(h->stream));
   unsigned long long bits;
-  OM_TRY(hydro_current_dt(h, &dt, &bits));
-  void *state[4] = {h->arrays[0].d(), h->arrays[1].d(), h->arrays[2].d(), h->arrays[3].d()};
+  OM_TRY(hydro_current_dt(h, &s->h_in1->dt, &bits));
+  for (int k = 0; k < 4; ++k) s->h_in1->state[k] = h->arrays[k].d();
   const double cfl = ((HydroScalars *)h->h_scalars)->cfl;
-  om_status st = fp64 ? vjp_kernels_direct<double>(h, s, state, cot_next, cot_prev, dt, cfl, bits)
-                      : vjp_kernels_direct<float>(h, s, state, cot_next, cot_prev, dt, cfl, bits);
+  OM_CUDA_CHECK(cudaMemcpyAsync(s->d_in, s->h_in1, sizeof(adj::StepIn), cudaMemcpyHostToDevice,
+                                h->stream));
+  om_status st = fp64 ? vjp_kernels<double>(h, s, cot_next, cot_prev, cfl)
+                      : vjp_kernels<float>(h, s, cot_next, cot_prev, cfl);
   OM_TRY(st);
+  h->launches += kVjpLaunches;
   OM_CUDA_CHECK(cudaStreamSynchronize(h->stream));
   return OM_OK;
 }
 
-// Gradient of loss = mean((density_T - target)^2) with respect to the state
-// at the start, over `steps` proceed steps of the handle (which ends at
-// step T).  sqrt(T) checkpointing: every s-th state is kept, each segment is
-// recomputed once and walked backwards.
+extern "C" om_status om_hydro_tape_free(om_hydro_tape tape) {
+  delete tape;
+  return OM_OK;
+}
+
+extern "C" om_status om_hydro_forward(om_handle H, int steps, int checkpoint_every,
+                                      om_hydro_tape *out) {
+  Handle *h = handle_of(H);
+  if (!h || h->kind != OM_KIND_HYDRO || steps < 1 || !out) {
+    set_error("om_hydro_forward: needs a Hydro handle, steps >= 1 and a tape pointer");
+    return OM_ERR_ARG;
+  }
+  if (!h->cyclic) {
+    set_error("Hydro adjoint: periodic grids only");
+    return OM_ERR_UNSUPPORTED;
+  }
+  *out = nullptr;
+  OM_CUDA_CHECK(cudaSetDevice(h->device));
+  om_hydro_tape t = new om_hydro_tape_s();
+  t->h = h;
+  t->steps = steps;
+  t->seg = checkpoint_every > 0 ? checkpoint_every
+                                : std::max(1, (int)std::ceil(std::sqrt((double)steps)));
+  t->seg = std::min(t->seg, steps);
+  t->nck = (steps + t->seg - 1) / t->seg;
+  t->ck.resize(t->nck + 1);
+  t->segst.resize(t->seg);
+  om_status status = OM_OK;
+  auto fail = [&](om_status s2) {
+    delete t;
+    return s2;
+  };
+  for (auto &c : t->ck)
+    if ((status = hydro_checkpoint_alloc(h, &c)) != OM_OK) return fail(status);
+  for (auto &c : t->segst)
+    if ((status = hydro_checkpoint_alloc(h, &c)) != OM_OK) return fail(status);
+  if (cudaMallocHost(&t->h_in, sizeof(adj::StepIn) * (size_t)steps) != cudaSuccess) {
+    cudaGetLastError();
+    t->h_in = nullptr;
+    set_error("om_hydro_forward: allocation failed");
+    return fail(OM_ERR_NOMEM);
+  }
+  int kid = -1;
+  if ((status = om_kernel_id(H, "proceed", &kid)) != OM_OK) return fail(status);
+  for (int j = 0; j < t->nck; ++j) {
+    if ((status = hydro_save(h, &t->ck[j])) != OM_OK) return fail(status);
+    const int len = std::min(t->seg, steps - j * t->seg);
+    if ((status = om_run_n(H, kid, len)) != OM_OK) return fail(status);
+  }
+  if ((status = hydro_save(h, &t->ck[t->nck])) != OM_OK) return fail(status);
+  *out = t;
+  return OM_OK;
+}
+
+// Backward over the tape from the final-state cotangent already in s->ub.
+// On return result[4] holds the arrays (s->ub or s->pb) with the cotangent
+// of the tape's start state; the handle is at the final state.  Every copy
+// and kernel runs on the handle's stream, so a segment buffer is refilled
+// only after the steps that read it.
+static om_status backward_core(om_handle H, om_hydro_tape t, AdjointScratch *s, void **result) {
+  Handle *h = t->h;
+  int kid = -1;
+  OM_TRY(om_kernel_id(H, "proceed", &kid));
+  void *ub[4], *pb[4];
+  for (int k = 0; k < 4; ++k) {
+    ub[k] = s->ub[k];
+    pb[k] = s->pb[k];
+  }
+  const double cfl = ((HydroScalars *)h->h_scalars)->cfl;
+  for (int j = t->nck - 1; j >= 0; --j) {
+    const int len = std::min(t->seg, t->steps - j * t->seg);
+    // recompute the segment from its checkpoint, keeping every state
+    OM_TRY(hydro_restore(h, &t->ck[j]));
+    for (int m = 0; m < len; ++m) {
+      adj::StepIn &in = t->h_in[j * t->seg + m];
+      unsigned long long bits;
+      OM_TRY(hydro_save(h, &t->segst[m]));
+      OM_TRY(hydro_current_dt(h, &in.dt, &bits));
+      for (int k = 0; k < 4; ++k) in.state[k] = t->segst[m].f[k];
+      OM_TRY(om_run(H, kid));
+    }
+    for (int m = len - 1; m >= 0; --m) {
+      OM_TRY(run_vjp_step(h, s, &t->h_in[j * t->seg + m], ub, pb, cfl));
+      for (int k = 0; k < 4; ++k) std::swap(ub[k], pb[k]);
+    }
+  }
+  OM_TRY(hydro_restore(h, &t->ck[t->nck]));
+  for (int k = 0; k < 4; ++k) result[k] = ub[k];
+  return OM_OK;
+}
+
+extern "C" om_status om_hydro_backward(om_handle H, om_hydro_tape t, const void *const *cot_final,
+                                       void *const *grad) {
+  Handle *h = handle_of(H);
+  if (!h || !t || t->h != h || !cot_final || !grad) {
+    set_error("om_hydro_backward: needs the tape's own handle, 4 cotangents and 4 outputs");
+    return OM_ERR_ARG;
+  }
+  OM_CUDA_CHECK(cudaSetDevice(h->device));
+  const int fp64 = h->cfg.precision == 64;
+  const size_t bytes = h->memory_size_total() * (fp64 ? 8 : 4);
+  AdjointScratch *s;
+  OM_TRY(get_scratch(h, fp64, &s));
+  for (int k = 0; k < 4; ++k)
+    OM_CUDA_CHECK(cudaMemcpyAsync(s->ub[k], cot_final[k], bytes, cudaMemcpyDefault, h->stream));
+  void *res[4];
+  om_status status = backward_core(H, t, s, res);
+  if (status != OM_OK) {
+    hydro_restore(h, &t->ck[t->nck]);
+    return status;
+  }
+  for (int k = 0; k < 4; ++k)
+    OM_CUDA_CHECK(cudaMemcpyAsync(grad[k], res[k], bytes, cudaMemcpyDefault, h->stream));
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess) {
+    set_error(std::string("om_hydro_backward: ") + cudaGetErrorString(cudaGetLastError()));
+    return OM_ERR_CUDA;
+  }
+  return OM_OK;
+}
+
 extern "C" om_status om_hydro_adjoint_run(om_handle H, int steps, const void *target,
                                           int checkpoint_every, double *loss,
                                           void *const *grad) {
@@ -659,42 +953,24 @@ extern "C" om_status om_hydro_adjoint_run(om_handle H, int steps, const void *ta
   const size_t bytes = cells * (fp64 ? 8 : 4);
   AdjointScratch *sc;
   OM_TRY(get_scratch(h, fp64, &sc));
-  const int seg = checkpoint_every > 0 ? checkpoint_every
-                                       : std::max(1, (int)std::ceil(std::sqrt((double)steps)));
-  const int nck = (steps + seg - 1) / seg;
-  int kid = -1;
-  OM_TRY(om_kernel_id(H, "proceed", &kid));
-  std::vector<HydroCheckpoint> ck(nck + 1), segst(seg);
-  std::vector<double> seg_dt(seg);
-  std::vector<unsigned long long> seg_bits(seg);
   void *dtarget = nullptr;
-  om_status status = OM_OK;
-  auto fail = [&](om_status s2) {
-    for (auto &c : ck) hydro_checkpoint_free(&c);
-    for (auto &c : segst) hydro_checkpoint_free(&c);
-    cudaFree(dtarget);
-    return s2;
-  };
-  for (auto &c : ck)
-    if ((status = hydro_checkpoint_alloc(h, &c)) != OM_OK) return fail(status);
-  for (auto &c : segst)
-    if ((status = hydro_checkpoint_alloc(h, &c)) != OM_OK) return fail(status);
   if (cudaMalloc(&dtarget, bytes) != cudaSuccess) {
     cudaGetLastError();
     set_error("om_hydro_adjoint_run: allocation failed");
-    return fail(OM_ERR_NOMEM);
+    return OM_ERR_NOMEM;
   }
+  om_hydro_tape t = nullptr;
+  auto done = [&](om_status s2) {
+    if (t) om_hydro_tape_free(t);
+    cudaFree(dtarget);
+    return s2;
+  };
   if (cudaMemcpy(dtarget, target, bytes, cudaMemcpyDefault) != cudaSuccess) {
     set_error("om_hydro_adjoint_run: target copy failed");
-    return fail(OM_ERR_CUDA);
+    return done(OM_ERR_CUDA);
   }
-  // forward with checkpoints
-  for (int j = 0; j < nck; ++j) {
-    if ((status = hydro_save(h, &ck[j])) != OM_OK) return fail(status);
-    const int len = std::min(seg, steps - j * seg);
-    if ((status = om_run_n(H, kid, len)) != OM_OK) return fail(status);
-  }
-  if ((status = hydro_save(h, &ck[nck])) != OM_OK) return fail(status);
+  om_status status = om_hydro_forward(H, steps, checkpoint_every, &t);
+  if (status != OM_OK) return done(status);
   // loss and its cotangent at the final state
   {
     const int grid = sc->nparts;
@@ -712,49 +988,32 @@ extern "C" om_status om_hydro_adjoint_run(om_handle H, int steps, const void *ta
                     h->stream);
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) {
       set_error(std::string("adjoint loss: ") + cudaGetErrorString(cudaGetLastError()));
-      return fail(OM_ERR_CUDA);
+      return done(OM_ERR_CUDA);
     }
     double l = 0;
     for (double v : part) l += v;
     if (loss) *loss = l / (double)cells;
   }
-  // backward, segment by segment
-  void *ub[4] = {sc->ub[0], sc->ub[1], sc->ub[2], sc->ub[3]};
-  void *pb[4] = {sc->pb[0], sc->pb[1], sc->pb[2], sc->pb[3]};
-  const double cfl = ((HydroScalars *)h->h_scalars)->cfl;
-  for (int j = nck - 1; j >= 0; --j) {
-    const int len = std::min(seg, steps - j * seg);
-    if ((status = hydro_restore(h, &ck[j])) != OM_OK) return fail(status);
-    for (int m = 0; m < len; ++m) {
-      if ((status = hydro_save(h, &segst[m])) != OM_OK) return fail(status);
-      if ((status = hydro_current_dt(h, &seg_dt[m], &seg_bits[m])) != OM_OK) return fail(status);
-      if ((status = om_run(H, kid)) != OM_OK) return fail(status);
-    }
-    for (int m = len - 1; m >= 0; --m) {
-      status = fp64 ? vjp_step<double>(h, sc, segst[m].f, ub, pb, &seg_dt[m], cfl, seg_bits[m],
-                                       nullptr)
-                    : vjp_step<float>(h, sc, segst[m].f, ub, pb, &seg_dt[m], cfl, seg_bits[m],
-                                      nullptr);
-      if (status != OM_OK) return fail(status);
-      for (int k = 0; k < 4; ++k) std::swap(ub[k], pb[k]);
-    }
+  void *res[4];
+  if ((status = backward_core(H, t, sc, res)) != OM_OK) {
+    hydro_restore(h, &t->ck[t->nck]);
+    return done(status);
   }
   for (int k = 0; k < 4; ++k)
-    if (cudaMemcpyAsync(grad[k], ub[k], bytes, cudaMemcpyDefault, h->stream) != cudaSuccess) {
+    if (cudaMemcpyAsync(grad[k], res[k], bytes, cudaMemcpyDefault, h->stream) != cudaSuccess) {
       set_error("om_hydro_adjoint_run: gradient copy failed");
-      return fail(OM_ERR_CUDA);
+      return done(OM_ERR_CUDA);
     }
-  // leave the handle at the final state of the forward run
-  if ((status = hydro_restore(h, &ck[nck])) != OM_OK) return fail(status);
   if (cudaStreamSynchronize(h->stream) != cudaSuccess) {
     set_error(std::string("om_hydro_adjoint_run: ") + cudaGetErrorString(cudaGetLastError()));
-    return fail(OM_ERR_CUDA);
+    return done(OM_ERR_CUDA);
   }
-  return fail(OM_OK);
+  return done(OM_OK);
 }
 
 // device time (ms) of one adjoint step at the handle's current state, for
-// measurement (cotangent input: the density cotangent of the loss)
+// measurement (cotangent input: zero arrays; the kernels' work does not
+// depend on the values)
 extern "C" om_status om_hydro_time_vjp(om_handle H, int reps, float *ms) {
   Handle *h = handle_of(H);
   if (!h || h->kind != OM_KIND_HYDRO || reps < 1 || !ms) {
@@ -766,27 +1025,32 @@ extern "C" om_status om_hydro_time_vjp(om_handle H, int reps, float *ms) {
   AdjointScratch *s;
   OM_TRY(get_scratch(h, fp64, &s));
   for (int i = 0; i < 4; ++i) OM_TRY(bring_device(h, h->arrays[i]));
-  double dt;
+  OM_CUDA_CHECK(cudaStreamSynchronize(h->stream));
   unsigned long long bits;
-  OM_TRY(hydro_current_dt(h, &dt, &bits));
+  OM_TRY(hydro_current_dt(h, &s->h_in1->dt, &bits));
+  for (int k = 0; k < 4; ++k) s->h_in1->state[k] = h->arrays[k].d();
   const size_t bytes = h->memory_size_total() * (fp64 ? 8 : 4);
   for (int k = 0; k < 4; ++k) OM_CUDA_CHECK(cudaMemsetAsync(s->ub[k], 0, bytes, h->stream));
-  void *state[4] = {h->arrays[0].d(), h->arrays[1].d(), h->arrays[2].d(), h->arrays[3].d()};
   const double cfl = ((HydroScalars *)h->h_scalars)->cfl;
-  cudaEvent_t e0, e1;
-  OM_CUDA_CHECK(cudaEventCreate(&e0));
-  OM_CUDA_CHECK(cudaEventCreate(&e1));
-  OM_CUDA_CHECK(cudaEventRecord(e0, h->stream));
-  for (int r = 0; r < reps; ++r) {
-    om_status st = fp64 ? vjp_step<double>(h, s, state, s->ub, s->pb, &dt, cfl, bits, nullptr)
-                        : vjp_step<float>(h, s, state, s->ub, s->pb, &dt, cfl, bits, nullptr);
-    OM_TRY(st);
+  // one step outside the timed region captures the graph
+  OM_TRY(run_vjp_step(h, s, s->h_in1, s->ub, s->pb, cfl));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  om_status st = OM_OK;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess ||
+      cudaEventRecord(e0, h->stream) != cudaSuccess) {
+    set_error("om_hydro_time_vjp: event setup failed");
+    st = OM_ERR_CUDA;
   }
-  OM_CUDA_CHECK(cudaEventRecord(e1, h->stream));
-  OM_CUDA_CHECK(cudaEventSynchronize(e1));
-  cudaEventElapsedTime(ms, e0, e1);
-  *ms /= reps;
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  return OM_OK;
+  for (int r = 0; st == OM_OK && r < reps; ++r)
+    st = run_vjp_step(h, s, s->h_in1, s->ub, s->pb, cfl);
+  if (st == OM_OK && (cudaEventRecord(e1, h->stream) != cudaSuccess ||
+                      cudaEventSynchronize(e1) != cudaSuccess ||
+                      cudaEventElapsedTime(ms, e0, e1) != cudaSuccess)) {
+    set_error("om_hydro_time_vjp: timing failed");
+    st = OM_ERR_CUDA;
+  }
+  if (st == OM_OK) *ms /= reps;
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  return st;
 }

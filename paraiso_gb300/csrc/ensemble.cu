@@ -86,6 +86,9 @@ static om_status ens_upload_args(om_ensemble E) {
       x.sc = E->d_sc + k;
       x.read_slot = p;
       x.dt_hist = &E->d_sc[k].dt_last;
+      x.lm = 0;
+      x.ms0 = E->n0[k];
+      x.margin_min = nullptr;
     }
     OM_CUDA_CHECK(cudaMemcpyAsync(E->d_args[p], a.data(), sizeof(HydroStepArgs) * E->count,
                                   cudaMemcpyHostToDevice, E->stream));
@@ -452,7 +455,7 @@ om_status om_ensemble_totals(om_ensemble E, int k, double *out) {
   const size_t off = E->offset[k] * E->es;
   OM_CUDA_CHECK(hydro_totals(E->fp64, (char *)E->field[0][E->cur] + off,
                              (char *)E->field[1][E->cur] + off, (char *)E->field[2][E->cur] + off,
-                             (char *)E->field[3][E->cur] + off, (size_t)E->n0[k] * E->n1[k],
+                             (char *)E->field[3][E->cur] + off, E->n0[k], E->n1[k], 0,
                              E->gamma, E->d_partials, E->totals_blocks, E->d_totals, E->stream));
   OM_CUDA_CHECK(cudaMemcpyAsync(E->h_totals, E->d_totals, sizeof(double) * 4,
                                 cudaMemcpyDeviceToHost, E->stream));

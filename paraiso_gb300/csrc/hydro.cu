@@ -33,6 +33,9 @@ struct HydroState {
   bool ts_valid = false;       // sc->tsmin[slot] holds the min of the current state
   int slot = 0;
   double ts_dR0 = 0, ts_dR1 = 0;  // dR the cached minimum was computed with
+  double ts_ext1 = 0;             // extent1 it was computed with (open grids)
+  int lm = 0;                     // margin width: 3 on an open grid, else 0
+  unsigned long long *d_margin = nullptr;  // open grid: margin cells' CFL minimum
   double *d_dt = nullptr;      // dt history of the last run
   int dt_cap = 0;
   int last_n = 0;
@@ -70,7 +73,7 @@ static om_status hydro_init(Handle *h, int n) {
   (void)n;
   HydroState *st = hst(h);
   OM_CUDA_CHECK(hydro_init_jet(st->fp64, h->arrays[0].d(), h->arrays[1].d(), h->arrays[2].d(),
-                               h->arrays[3].d(), h->size[0], h->size[1], h->cfg.gamma,
+                               h->arrays[3].d(), h->size[0], h->size[1], st->lm, h->cfg.gamma,
                                hsc_dev(h), h->stream));
   h->launches++;
   st->ts_valid = false;
@@ -78,22 +81,45 @@ static om_status hydro_init(Handle *h, int n) {
   return OM_OK;
 }
 
-// ensure sc->tsmin[slot] holds the CFL minimum of the current state
-static om_status ensure_tsmin(Handle *h) {
+// the cached minimum (and on an open grid the margin minimum, a function of
+// dR and extent1) still belongs to the current scalars
+static bool ts_current(Handle *h) {
+  const HydroState *st = hst(h);
+  const HydroScalars *hs_ = hsc_host(h);
+  return st->ts_valid && st->ts_dR0 == hs_->dR0 && st->ts_dR1 == hs_->dR1 &&
+         (st->lm == 0 || st->ts_ext1 == hs_->extent1);
+}
+
+static void ts_mark_current(Handle *h) {
   HydroState *st = hst(h);
   const HydroScalars *hs_ = hsc_host(h);
-  if (st->ts_valid && st->ts_dR0 == hs_->dR0 && st->ts_dR1 == hs_->dR1) return OM_OK;
-  OM_CUDA_CHECK(cudaMemsetAsync(&hsc_dev(h)->tsmin[st->slot], 0xFF, sizeof(unsigned long long),
-                                h->stream));
-  cudaEvent_t ev = prof_begin(h);
-  OM_CUDA_CHECK(hydro_tsmin(st->fp64, h->arrays[0].d(), h->arrays[1].d(), h->arrays[2].d(),
-                            h->arrays[3].d(), h->memory_size_total(), h->cfg.gamma, hsc_dev(h),
-                            st->slot, reduce_grid(h), h->stream));
-  prof_end(h, ev, "hydro_tsmin_kernel", (double)h->memory_size_total());
-  h->launches++;
   st->ts_valid = true;
   st->ts_dR0 = hs_->dR0;
   st->ts_dR1 = hs_->dR1;
+  st->ts_ext1 = hs_->extent1;
+}
+
+// ensure sc->tsmin[slot] holds the CFL minimum of the current state
+static om_status ensure_tsmin(Handle *h) {
+  HydroState *st = hst(h);
+  if (ts_current(h)) return OM_OK;
+  OM_CUDA_CHECK(cudaMemsetAsync(&hsc_dev(h)->tsmin[st->slot], 0xFF, sizeof(unsigned long long),
+                                h->stream));
+  cudaEvent_t ev = prof_begin(h);
+  if (st->lm > 0) {
+    OM_CUDA_CHECK(hydro_tsmin_open(st->fp64, h->arrays[0].d(), h->arrays[1].d(),
+                                   h->arrays[2].d(), h->arrays[3].d(), h->size[0], h->size[1],
+                                   st->lm, h->cfg.gamma, hsc_dev(h), st->slot, st->d_margin,
+                                   reduce_grid(h), h->stream));
+    h->launches += 2;
+  } else {
+    OM_CUDA_CHECK(hydro_tsmin(st->fp64, h->arrays[0].d(), h->arrays[1].d(), h->arrays[2].d(),
+                              h->arrays[3].d(), h->memory_size_total(), h->cfg.gamma,
+                              hsc_dev(h), st->slot, reduce_grid(h), h->stream));
+    h->launches++;
+  }
+  prof_end(h, ev, "hydro_tsmin_kernel", (double)h->memory_size_total());
+  ts_mark_current(h);
   return OM_OK;
 }
 
@@ -118,6 +144,9 @@ static om_status proceed_fused(Handle *h, int n) {
     a.sc = hsc_dev(h);
     a.read_slot = st->slot;
     a.dt_hist = st->d_dt + k;
+    a.lm = st->lm;
+    a.ms0 = (int)h->memory_size(0);
+    a.margin_min = st->d_margin;
     cudaEvent_t ev = prof_begin(h);
     cudaError_t e = st->fp64 ? hydro_fused_f64(a, st->tile, h->stream, nullptr)
                              : hydro_fused_f32(a, st->tile, st->variant == 2, h->stream, nullptr);
@@ -195,19 +224,14 @@ static om_status hydro_proceed(Handle *h, int n) {
 
 static uint64_t hydro_state_key(Handle *h) {
   HydroState *st = hst(h);
-  const HydroScalars *hs_ = hsc_host(h);
-  const bool valid = st->ts_valid && st->ts_dR0 == hs_->dR0 && st->ts_dR1 == hs_->dR1;
-  return (valid ? 1 : 0) | (uint64_t)st->slot << 1;
+  return (ts_current(h) ? 1 : 0) | (uint64_t)st->slot << 1;
 }
 
 static void hydro_restore_key(Handle *h, uint64_t key) {
   HydroState *st = hst(h);
   st->ts_valid = (key & 1) != 0;
   st->slot = (int)((key >> 1) & 1);
-  if (st->ts_valid) {
-    st->ts_dR0 = hsc_host(h)->dR0;
-    st->ts_dR1 = hsc_host(h)->dR1;
-  }
+  if (st->ts_valid) ts_mark_current(h);
 }
 
 static bool hydro_graph_ok(Handle *h, int kernel_id) {
@@ -218,10 +242,7 @@ static bool hydro_graph_ok(Handle *h, int kernel_id) {
 static void hydro_after_replay(Handle *h, int kernel_id, int n) {
   HydroState *st = hst(h);
   if (h->kernels[kernel_id].name == "proceed") {
-    const HydroScalars *hs_ = hsc_host(h);
-    st->ts_valid = true;
-    st->ts_dR0 = hs_->dR0;
-    st->ts_dR1 = hs_->dR1;
+    ts_mark_current(h);
     st->slot ^= (n & 1);
     st->last_n = n;
   } else {
@@ -244,6 +265,7 @@ static void hydro_free(Handle *h) {
   cudaFree(st->d_dt);
   cudaFree(st->d_ts);
   cudaFree(st->d_min);
+  cudaFree(st->d_margin);
   if (st->h_min) cudaFreeHost(st->h_min);
   cudaFree(st->d_partials);
   cudaFree(st->d_totals);
@@ -281,7 +303,7 @@ om_status hydro_current_dt(Handle *h, double *dt, unsigned long long *bits) {
 struct HydroCkState {
   bool ts_valid;
   int slot;
-  double ts_dR0, ts_dR1;
+  double ts_dR0, ts_dR1, ts_ext1;
 };
 static_assert(sizeof(HydroCkState) <= 64, "checkpoint bookkeeping size");
 
@@ -312,7 +334,7 @@ om_status hydro_save(Handle *h, HydroCheckpoint *c) {
   }
   std::memcpy(c->sc, h->h_scalars, sizeof(HydroScalars));
   HydroState *st = hst(h);
-  HydroCkState k{st->ts_valid, st->slot, st->ts_dR0, st->ts_dR1};
+  HydroCkState k{st->ts_valid, st->slot, st->ts_dR0, st->ts_dR1, st->ts_ext1};
   std::memcpy(c->state, &k, sizeof(k));
   return OM_OK;
 }
@@ -333,12 +355,13 @@ om_status hydro_restore(Handle *h, const HydroCheckpoint *c) {
   st->slot = k.slot;
   st->ts_dR0 = k.ts_dR0;
   st->ts_dR1 = k.ts_dR1;
+  st->ts_ext1 = k.ts_ext1;
   return OM_OK;
 }
 
 om_status hydro_setup(Handle *h) {
-  if (!h->cyclic) {
-    set_error("Hydro: only the cyclic (periodic) boundary is implemented on the GPU");
+  if (!h->cyclic && h->cfg.variant == 1) {
+    set_error("Hydro: the open boundary runs on the fused path (variant 0 or 2), not plain");
     return OM_ERR_UNSUPPORTED;
   }
   if (h->cfg.precision != 32 && h->cfg.precision != 64) {
@@ -353,9 +376,17 @@ om_status hydro_setup(Handle *h) {
     set_error("Hydro: gamma must be > 1");
     return OM_ERR_ARG;
   }
+  // open grids keep 3-cell margins (the stencil radius of both stages,
+  // Hydro.hpp:12-13 of the generated class); periodic grids none
+  const int lm = h->cyclic ? 0 : 3;
+  for (int ax = 0; ax < 2; ++ax) {
+    h->lower_margin[ax] = lm;
+    h->upper_margin[ax] = lm;
+  }
   HydroState *st = new HydroState();
   st->fp64 = h->cfg.precision == 64;
   st->variant = h->cfg.variant;
+  st->lm = lm;
   st->tile = (h->cfg.tile_x == 64) ? kTile64x16 : (h->cfg.tile_y == 8 ? kTile32x8 : kTile32x16);
   h->impl = st;
   h->impl_free = hydro_free;
@@ -383,6 +414,7 @@ om_status hydro_setup(Handle *h) {
   const size_t cells = h->memory_size_total();
   if (cudaMalloc(&st->d_ts, cells * es) != cudaSuccess ||
       cudaMalloc(&st->d_min, sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc(&st->d_margin, sizeof(unsigned long long)) != cudaSuccess ||
       cudaMallocHost(&st->h_min, sizeof(unsigned long long)) != cudaSuccess ||
       cudaMalloc(&st->d_partials, sizeof(double) * 8 * st->totals_blocks) != cudaSuccess ||
       cudaMalloc(&st->d_totals, sizeof(double) * 4) != cudaSuccess ||
@@ -411,6 +443,10 @@ extern "C" om_status om_hydro_init_kh(om_handle H, uint64_t seed) {
   Handle *h;
   OM_TRY(hydro_handle(H, &h));
   HydroState *st = hst(h);
+  if (st->lm > 0) {
+    set_error("om_hydro_init_kh: the Kelvin-Helmholtz start is periodic (open grids use init)");
+    return OM_ERR_UNSUPPORTED;
+  }
   OM_CUDA_CHECK(hydro_init_kh(st->fp64, h->arrays[0].d(), h->arrays[1].d(), h->arrays[2].d(),
                               h->arrays[3].d(), h->size[0], h->size[1], mix64(seed), h->stream));
   OM_CUDA_CHECK(cudaStreamSynchronize(h->stream));
@@ -436,7 +472,7 @@ extern "C" om_status om_hydro_totals(om_handle H, double *out) {
   HydroState *st = hst(h);
   for (int i = 0; i < 4; ++i) OM_TRY(bring_device(h, h->arrays[i]));
   OM_CUDA_CHECK(hydro_totals(st->fp64, h->arrays[0].d(), h->arrays[1].d(), h->arrays[2].d(),
-                             h->arrays[3].d(), h->memory_size_total(), h->cfg.gamma,
+                             h->arrays[3].d(), h->size[0], h->size[1], st->lm, h->cfg.gamma,
                              st->d_partials, st->totals_blocks, st->d_totals, h->stream));
   OM_CUDA_CHECK(cudaMemcpyAsync(st->h_totals, st->d_totals, sizeof(double) * 4,
                                 cudaMemcpyDeviceToHost, h->stream));

@@ -18,28 +18,53 @@ void hydro_tile_dims(int tile, int *tx, int *ty) {
   }
 }
 
-template <class R, int TX, int TY, int NT>
+template <class R, int TX, int TY, int NT, bool OPEN>
 static cudaError_t launch_fused(const HydroStepArgs &a0, cudaStream_t s, int *grid_out) {
   HydroStepArgs a = a0;
   a.nt0 = (a.n0 + TX - 1) / TX;
   const int nt1 = (a.n1 + TY - 1) / TY;
   const size_t smem = sizeof(FusedSmem<R, TX, TY>);
-  cudaError_t e = cudaFuncSetAttribute(hydro_fused_kernel<R, TX, TY, NT>,
+  cudaError_t e = cudaFuncSetAttribute(hydro_fused_kernel<R, TX, TY, NT, OPEN>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  hydro_fused_kernel<R, TX, TY, NT><<<a.nt0 * nt1, NT, smem, s>>>(a);
+  hydro_fused_kernel<R, TX, TY, NT, OPEN><<<a.nt0 * nt1, NT, smem, s>>>(a);
   if (grid_out) *grid_out = a.nt0 * nt1;
   return cudaGetLastError();
 }
 
+// a.lm > 0: open grid (margins, jet boundary condition)
 cudaError_t hydro_fused_f64(const HydroStepArgs &a, int tile, cudaStream_t s, int *grid_out) {
   (void)tile;  // one shape in FP64: 32x16 (104 KB of shared memory)
-  return launch_fused<double, 32, 16, 256>(a, s, grid_out);
+  return a.lm > 0 ? launch_fused<double, 32, 16, 256, true>(a, s, grid_out)
+                  : launch_fused<double, 32, 16, 256, false>(a, s, grid_out);
 }
 
 // exact FP32 variant (the fast build lives in hydro_fast.cu)
 cudaError_t hydro_fused_f32_exact(const HydroStepArgs &a, cudaStream_t s, int *grid_out) {
-  return launch_fused<float, 32, 16, 256>(a, s, grid_out);
+  return a.lm > 0 ? launch_fused<float, 32, 16, 256, true>(a, s, grid_out)
+                  : launch_fused<float, 32, 16, 256, false>(a, s, grid_out);
+}
+
+// CFL minimum of an open grid: margin cells (jet state) into *margin_min,
+// then the interior cells and the margin minimum into sc->tsmin[slot]
+cudaError_t hydro_tsmin_open(int fp64, const void *rho, const void *v0, const void *v1,
+                             const void *p, int n0, int n1, int lm, double gamma,
+                             HydroScalars *sc, int slot, unsigned long long *margin_min, int grid,
+                             cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(margin_min, 0xFF, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  if (fp64) {
+    hydro_margin_min_kernel<double><<<grid, 256, 0, s>>>(n0, n1, lm, gamma, sc, margin_min);
+    hydro_tsmin_open_kernel<double><<<grid, 256, 0, s>>>(
+        (const double *)rho, (const double *)v0, (const double *)v1, (const double *)p, n0, n1,
+        lm, gamma, sc, slot, margin_min);
+  } else {
+    hydro_margin_min_kernel<float><<<grid, 256, 0, s>>>(n0, n1, lm, gamma, sc, margin_min);
+    hydro_tsmin_open_kernel<float><<<grid, 256, 0, s>>>(
+        (const float *)rho, (const float *)v0, (const float *)v1, (const float *)p, n0, n1, lm,
+        gamma, sc, slot, margin_min);
+  }
+  return cudaGetLastError();
 }
 
 template <class R, int TX, int TY, int NT>
@@ -149,17 +174,20 @@ cudaError_t hydro_scalar_advance(HydroScalars *sc, double dt, double *dt_hist, c
   return cudaGetLastError();
 }
 
-// buildInit (HydroMain.hs:79-102) with the cyclic codec: loadIndex is the
-// cell index, so the jet region (x < 0) is empty on a periodic mesh.
+// buildInit (HydroMain.hs:79-102) over the memory array: loadIndex is the
+// cell index minus the margin lm, so with the cyclic codec (lm 0) the jet
+// region (x < 0) is empty, and on an open grid it lies in the left margin.
 template <class R>
-__global__ void hydro_init_jet_kernel(R *rho, R *v0, R *v1, R *p, int n0, int n1, double gamma,
-                                      const HydroScalars *sc) {
-  const size_t n = (size_t)n0 * n1;
+__global__ void hydro_init_jet_kernel(R *rho, R *v0, R *v1, R *p, int n0, int n1, int lm,
+                                      double gamma, const HydroScalars *sc) {
+  const int ms0 = n0 + 2 * lm;
+  const size_t n = (size_t)ms0 * (n1 + 2 * lm);
   const R g = (R)gamma, dR0 = (R)sc->dR0, dR1 = (R)sc->dR1, ext1 = (R)sc->extent1;
   const R pi = (R)3.141592653589793;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
-    const int iy = (int)(i / n0), ix = (int)(i - (size_t)iy * n0);
+    const int y = (int)(i / ms0), x = (int)(i - (size_t)y * ms0);
+    const int iy = y - lm, ix = x - lm;
     const R cx = dR0 * (R)ix, cy = dR1 * (R)iy;
     const bool region = (cy > R(0.47) * ext1) && ((cy < R(0.53) * ext1) && (cx < R(0)));
     const R factor = R(1) + R(1e-3) * (R)sin((double)(R(6) * pi * cx));
@@ -171,15 +199,15 @@ __global__ void hydro_init_jet_kernel(R *rho, R *v0, R *v1, R *p, int n0, int n1
 }
 
 cudaError_t hydro_init_jet(int fp64, void *rho, void *v0, void *v1, void *p, int n0, int n1,
-                           double gamma, const HydroScalars *sc, cudaStream_t s) {
+                           int lm, double gamma, const HydroScalars *sc, cudaStream_t s) {
   const int grid = 1024;
   if (fp64)
     hydro_init_jet_kernel<double><<<grid, 256, 0, s>>>((double *)rho, (double *)v0,
-                                                       (double *)v1, (double *)p, n0, n1, gamma,
-                                                       sc);
+                                                       (double *)v1, (double *)p, n0, n1, lm,
+                                                       gamma, sc);
   else
     hydro_init_jet_kernel<float><<<grid, 256, 0, s>>>((float *)rho, (float *)v0, (float *)v1,
-                                                      (float *)p, n0, n1, gamma, sc);
+                                                      (float *)p, n0, n1, lm, gamma, sc);
   return cudaGetLastError();
 }
 
@@ -260,11 +288,16 @@ __device__ void block_merge(Neu (&v)[4], Neu (*sh)[4]) {
 template <class R>
 __global__ void __launch_bounds__(256)
 hydro_totals_kernel(const R *__restrict__ rho, const R *__restrict__ u, const R *__restrict__ v,
-                    const R *__restrict__ p, size_t n, double gamma, double *partials) {
+                    const R *__restrict__ p, int n0, int n1, int lm, double gamma,
+                    double *partials) {
   __shared__ Neu sh[8][4];
   Neu acc[4] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x) {
+  const size_t n = (size_t)n0 * n1;
+  const int ms0 = n0 + 2 * lm;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x) {
+    // interior cell k of the memory array
+    const size_t i = lm ? (size_t)((int)(k / n0) + lm) * ms0 + (int)(k % n0) + lm : k;
     const double r = rho[i], a = u[i], b = v[i], q = p[i];
     neu_add(acc[0], r);
     neu_add(acc[1], r * a);
@@ -290,16 +323,16 @@ __global__ void hydro_totals_final_kernel(const double *partials, int blocks, do
 }
 
 cudaError_t hydro_totals(int fp64, const void *rho, const void *v0, const void *v1,
-                         const void *p, size_t n, double gamma, double *partials, int blocks,
-                         double *out, cudaStream_t s) {
+                         const void *p, int n0, int n1, int lm, double gamma, double *partials,
+                         int blocks, double *out, cudaStream_t s) {
   if (fp64)
     hydro_totals_kernel<double><<<blocks, 256, 0, s>>>((const double *)rho, (const double *)v0,
-                                                       (const double *)v1, (const double *)p, n,
-                                                       gamma, partials);
+                                                       (const double *)v1, (const double *)p, n0,
+                                                       n1, lm, gamma, partials);
   else
     hydro_totals_kernel<float><<<blocks, 256, 0, s>>>((const float *)rho, (const float *)v0,
-                                                      (const float *)v1, (const float *)p, n,
-                                                      gamma, partials);
+                                                      (const float *)v1, (const float *)p, n0,
+                                                      n1, lm, gamma, partials);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   hydro_totals_final_kernel<<<1, 32, 0, s>>>(partials, blocks, out);

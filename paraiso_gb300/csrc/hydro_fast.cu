@@ -9,16 +9,16 @@ namespace om {
 
 cudaError_t hydro_fused_f32_exact(const HydroStepArgs &a, cudaStream_t s, int *grid_out);
 
-template <int TX, int TY, int NT>
+template <int TX, int TY, int NT, bool OPEN = false>
 static cudaError_t launch_fast(const HydroStepArgs &a0, cudaStream_t s, int *grid_out) {
   HydroStepArgs a = a0;
   a.nt0 = (a.n0 + TX - 1) / TX;
   const int nt1 = (a.n1 + TY - 1) / TY;
   const size_t smem = sizeof(FusedSmem<float, TX, TY>);
-  cudaError_t e = cudaFuncSetAttribute(hydro_fused_kernel<float, TX, TY, NT>,
+  cudaError_t e = cudaFuncSetAttribute(hydro_fused_kernel<float, TX, TY, NT, OPEN>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  hydro_fused_kernel<float, TX, TY, NT><<<a.nt0 * nt1, NT, smem, s>>>(a);
+  hydro_fused_kernel<float, TX, TY, NT, OPEN><<<a.nt0 * nt1, NT, smem, s>>>(a);
   if (grid_out) *grid_out = a.nt0 * nt1;
   return cudaGetLastError();
 }
@@ -73,6 +73,8 @@ int hydro_ensemble_occupancy(int fp64, int tile, bool exact) {
 cudaError_t hydro_fused_f32(const HydroStepArgs &a, int tile, bool exact, cudaStream_t s,
                             int *grid_out) {
   if (exact) return hydro_fused_f32_exact(a, s, grid_out);
+  // an open grid (margins, jet boundary condition) runs the 32x16 tile
+  if (a.lm > 0) return launch_fast<32, 16, 256, true>(a, s, grid_out);
   switch (tile) {
     case kTile32x8: return launch_fast<32, 8, 256>(a, s, grid_out);
     case kTile64x16: return launch_fast<64, 16, 512>(a, s, grid_out);

@@ -31,6 +31,10 @@ struct HydroStepArgs {
   HydroScalars *sc;
   int read_slot;                   // tsmin slot holding min of the current state
   double *dt_hist;                 // dt of this step is written to dt_hist[0]
+  // open boundary only (the OPEN kernels): margin width, memory row pitch
+  // (n0 + 2 lm) and the CFL timescale minimum of the margin cells
+  int lm, ms0;
+  const unsigned long long *margin_min;
 };
 
 namespace hk {
@@ -86,6 +90,21 @@ __device__ __forceinline__ int wrap_near(int i, int n) {
   return i < 0 ? i + n : (i >= n ? i - n : i);
 }
 
+// boundaryCondition (HydroMain.hs:105-131): a cell of an open grid whose
+// index (ix, iy) lies outside [0, n) holds the jet state, in the OM's Real
+// type and operation order
+template <class R>
+__device__ __forceinline__ hs::Prim<R> jet_state(R g, R dR0, R dR1, R ext1, int ix, int iy) {
+  const R cx = dR0 * R(ix), cy = dR1 * R(iy);
+  const bool region = (cy > R(0.47) * ext1) && ((cy < R(0.53) * ext1) && (cx < R(0)));
+  hs::Prim<R> q;
+  q.rho = g * g * (region ? R(1) : R(10));
+  q.v0 = region ? R(6) : R(0);
+  q.v1 = R(0);
+  q.p = R(0.6);
+  return q;
+}
+
 // dt of this step in the OM's Real type: dtG = cfl * reduce Min dts
 template <class R> __device__ __forceinline__ R step_dt(const HydroStepArgs &a) {
   const R tsmin = ts_from_bits<R>(a.sc->tsmin[a.read_slot]);
@@ -134,7 +153,10 @@ template <class R, int TX, int TY> struct FusedSmem {
 
 // One tile of the fused step (tile index `tile` of the grid described by a),
 // run by a whole block; the tile with index 0 advances the instance's time.
-template <class R, int TX, int TY, int NT>
+// OPEN: the grid has margins of width a.lm; box cells outside the interior
+// take the jet state of the boundary condition instead of a periodic image,
+// and the margin cells' timescale minimum joins the CFL minimum.
+template <class R, int TX, int TY, int NT, bool OPEN = false>
 __device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
                                            FusedSmem<R, TX, TY> &s, unsigned long long *red) {
   using S = FusedSmem<R, TX, TY>;
@@ -154,10 +176,22 @@ __device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
   const bool near = n0 >= TX + 8 && n1 >= TY + 8;
   for (int i = tid; i < S::PY * S::PX; i += NT) {
     const int py = i / S::PX, px = i - py * S::PX;
-    const int gy = near ? hk::wrap_near(Y0 + py - 3, n1) : hk::wrap<R>(Y0 + py - 3, n1);
-    const int gx = near ? hk::wrap_near(X0 + px - 3, n0) : hk::wrap<R>(X0 + px - 3, n0);
-    const size_t gi = (size_t)gy * n0 + gx;
-    const R r = rho[gi], u = vx[gi], v = vy[gi], q = pr[gi];
+    R r, u, v, q;
+    if (OPEN) {
+      const int ix = X0 + px - 3, iy = Y0 + py - 3;
+      if (ix < 0 || iy < 0 || ix >= n0 || iy >= n1) {
+        const hs::Prim<R> j = hk::jet_state<R>(g, dR0, dR1, (R)a.sc->extent1, ix, iy);
+        r = j.rho; u = j.v0; v = j.v1; q = j.p;
+      } else {
+        const size_t gi = (size_t)(iy + a.lm) * a.ms0 + (ix + a.lm);
+        r = rho[gi]; u = vx[gi]; v = vy[gi]; q = pr[gi];
+      }
+    } else {
+      const int gy = near ? hk::wrap_near(Y0 + py - 3, n1) : hk::wrap<R>(Y0 + py - 3, n1);
+      const int gx = near ? hk::wrap_near(X0 + px - 3, n0) : hk::wrap<R>(X0 + px - 3, n0);
+      const size_t gi = (size_t)gy * n0 + gx;
+      r = rho[gi]; u = vx[gi]; v = vy[gi]; q = pr[gi];
+    }
     s.P[0][py][px] = r;
     s.P[1][py][px] = u;
     s.P[2][py][px] = v;
@@ -257,7 +291,7 @@ __device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
       const hs::Prim<R> q =
           hs::update(g, b, dtdx0, dtdx1, s.fx[oy * (TX + 1) + ox], s.fx[oy * (TX + 1) + ox + 1],
                      s.fy[oy * TX + ox], s.fy[(oy + 1) * TX + ox]);
-      const size_t gi = (size_t)gy * n0 + gx;
+      const size_t gi = OPEN ? (size_t)(gy + a.lm) * a.ms0 + (gx + a.lm) : (size_t)gy * n0 + gx;
       orho[gi] = q.rho;
       ovx[gi] = q.v0;
       ovy[gi] = q.v1;
@@ -267,7 +301,28 @@ __device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
       m = bits < m ? bits : m;
     }
   }
+  if (OPEN) {
+    // the generated class copies whole manifests, whose margins are zero,
+    // into the statics: tiles on the grid edge clear the adjacent margins
+    const int lm = a.lm;
+    const int xa = X0 == 0 ? -lm : X0, xb = X0 + TX >= n0 ? n0 + lm : X0 + TX;
+    const int ya = Y0 == 0 ? -lm : Y0, yb = Y0 + TY >= n1 ? n1 + lm : Y0 + TY;
+    const int w = xb - xa, cnt = w * (yb - ya);
+    if (xa < 0 || ya < 0 || xb > n0 || yb > n1) {
+      R *orho = (R *)a.nrho, *ovx = (R *)a.nv0, *ovy = (R *)a.nv1, *opr = (R *)a.np;
+      for (int i = tid; i < cnt; i += NT) {
+        const int y = ya + i / w, x = xa + i % w;
+        if (x >= 0 && y >= 0 && x < n0 && y < n1) continue;
+        const size_t gi = (size_t)(y + lm) * a.ms0 + (x + lm);
+        orho[gi] = R(0);
+        ovx[gi] = R(0);
+        ovy[gi] = R(0);
+        opr[gi] = R(0);
+      }
+    }
+  }
   hk::block_min_to(m, &a.sc->tsmin[1 - a.read_slot], red);
+  if (OPEN && tile == 0 && tid == 0) atomicMin(&a.sc->tsmin[1 - a.read_slot], *a.margin_min);
   if (tile == 0 && tid == 0) {
     a.dt_hist[0] = (double)dtG;
     a.sc->dt_last = (double)dtG;
@@ -275,13 +330,62 @@ __device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
   }
 }
 
-template <class R, int TX, int TY, int NT>
+template <class R, int TX, int TY, int NT, bool OPEN = false>
 __global__ void __launch_bounds__(NT)
 hydro_fused_kernel(HydroStepArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned long long red[32];
-  fused_tile<R, TX, TY, NT>(a, blockIdx.x, *reinterpret_cast<FusedSmem<R, TX, TY> *>(smem_raw),
-                            red);
+  fused_tile<R, TX, TY, NT, OPEN>(a, blockIdx.x,
+                                  *reinterpret_cast<FusedSmem<R, TX, TY> *>(smem_raw), red);
+}
+
+// CFL timescale minimum of the margin cells of an open grid (the jet state
+// of the boundary condition; it depends only on the index, gamma, dR and
+// extent1)
+template <class R>
+__global__ void __launch_bounds__(256)
+hydro_margin_min_kernel(int n0, int n1, int lm, double gamma, const HydroScalars *sc,
+                        unsigned long long *out) {
+  __shared__ unsigned long long red[32];
+  const R g = (R)gamma, dR0 = (R)sc->dR0, dR1 = (R)sc->dR1, ext1 = (R)sc->extent1;
+  const int ms0 = n0 + 2 * lm, ms1 = n1 + 2 * lm;
+  const size_t total = (size_t)ms0 * ms1;
+  unsigned long long m = ~0ull;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int y = (int)(i / ms0), x = (int)(i - (size_t)y * ms0);
+    const int ix = x - lm, iy = y - lm;
+    if (ix >= 0 && iy >= 0 && ix < n0 && iy < n1) continue;
+    const hs::Prim<R> q = hk::jet_state<R>(g, dR0, dR1, ext1, ix, iy);
+    const unsigned long long b = hk::ts_bits<R>(hs::timescale(g, dR0, dR1, q.rho, q.v0, q.v1, q.p));
+    m = b < m ? b : m;
+  }
+  hk::block_min_to(m, out, red);
+}
+
+// CFL minimum of an open grid's current state: the interior cells, then
+// the margin cells' minimum
+template <class R>
+__global__ void __launch_bounds__(256)
+hydro_tsmin_open_kernel(const R *__restrict__ rho, const R *__restrict__ v0,
+                        const R *__restrict__ v1, const R *__restrict__ p, int n0, int n1, int lm,
+                        double gamma, HydroScalars *sc, int slot,
+                        const unsigned long long *margin_min) {
+  __shared__ unsigned long long red[32];
+  const R g = (R)gamma, dR0 = (R)sc->dR0, dR1 = (R)sc->dR1;
+  const int ms0 = n0 + 2 * lm;
+  const size_t n = (size_t)n0 * n1;
+  unsigned long long m = ~0ull;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int y = (int)(i / n0), x = (int)(i - (size_t)y * n0);
+    const size_t gi = (size_t)(y + lm) * ms0 + (x + lm);
+    const R t = hs::timescale(g, dR0, dR1, rho[gi], v0[gi], v1[gi], p[gi]);
+    const unsigned long long b = hk::ts_bits<R>(t);
+    m = b < m ? b : m;
+  }
+  hk::block_min_to(m, &sc->tsmin[slot], red);
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicMin(&sc->tsmin[slot], *margin_min);
 }
 
 // Ensemble step: every tile of every instance is one work item; the

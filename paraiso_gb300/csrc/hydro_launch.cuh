@@ -32,6 +32,12 @@ int hydro_ensemble_occupancy(int fp64, int tile, bool exact);
 cudaError_t hydro_tsmin(int fp64, const void *rho, const void *v0, const void *v1,
                         const void *p, size_t n, double gamma, HydroScalars *sc, int slot,
                         int grid, cudaStream_t s);
+// the same for an open grid with margins lm: the margin cells' (jet)
+// minimum into *margin_min, then interior and margin into sc->tsmin[slot]
+cudaError_t hydro_tsmin_open(int fp64, const void *rho, const void *v0, const void *v1,
+                             const void *p, int n0, int n1, int lm, double gamma,
+                             HydroScalars *sc, int slot, unsigned long long *margin_min, int grid,
+                             cudaStream_t s);
 
 // plain path pieces
 cudaError_t hydro_plain_timescale(int fp64, const void *rho, const void *v0, const void *v1,
@@ -47,14 +53,15 @@ cudaError_t hydro_scalar_advance(HydroScalars *sc, double dt, double *dt_hist, c
 
 // initial states
 cudaError_t hydro_init_jet(int fp64, void *rho, void *v0, void *v1, void *p, int n0, int n1,
-                           double gamma, const HydroScalars *sc, cudaStream_t s);
+                           int lm, double gamma, const HydroScalars *sc, cudaStream_t s);
 cudaError_t hydro_init_kh(int fp64, void *rho, void *v0, void *v1, void *p, int n0, int n1,
                           unsigned long long seed_mix, cudaStream_t s);
 
-// compensated FP64 totals: partials[blocks][8], then out[4] (device)
+// compensated FP64 totals over the n0 x n1 interior of memory arrays with
+// margins lm: partials[blocks][8], then out[4] (device)
 cudaError_t hydro_totals(int fp64, const void *rho, const void *v0, const void *v1,
-                         const void *p, size_t n, double gamma, double *partials, int blocks,
-                         double *out, cudaStream_t s);
+                         const void *p, int n0, int n1, int lm, double gamma, double *partials,
+                         int blocks, double *out, cudaStream_t s);
 
 // A saved Hydro state (hydro.cu): the four arrays (device copies), the
 // scalar block and the cached-minimum bookkeeping, so that a restore

@@ -41,6 +41,7 @@ EXPORTS = [
     "om_ensemble_scalar", "om_ensemble_set_scalar", "om_ensemble_totals",
     "om_ensemble_last_launch_count", "om_life_proceed_noalloc", "om_autotune",
     "om_autotune_ensemble", "om_hydro_vjp", "om_hydro_adjoint_run", "om_hydro_time_vjp",
+    "om_hydro_forward", "om_hydro_backward", "om_hydro_tape_free",
 ]
 
 
@@ -116,6 +117,9 @@ def load_library(path: str | None = None) -> C.CDLL:
         "om_hydro_vjp": (i, [vp, C.POINTER(vp), C.POINTER(vp)]),
         "om_hydro_adjoint_run": (i, [vp, i, vp, i, C.POINTER(C.c_double), C.POINTER(vp)]),
         "om_hydro_time_vjp": (i, [vp, i, C.POINTER(C.c_float)]),
+        "om_hydro_forward": (i, [vp, i, i, C.POINTER(vp)]),
+        "om_hydro_backward": (i, [vp, vp, C.POINTER(vp), C.POINTER(vp)]),
+        "om_hydro_tape_free": (i, [vp]),
         "om_profile_query": (i, [vp, C.c_char_p, C.POINTER(C.c_long), C.POINTER(C.c_double),
                                  C.POINTER(C.c_double)]),
     }
@@ -387,6 +391,26 @@ class Hydro(OrthotopeMachine):
                                             int(checkpoint_every), C.byref(loss), ptrs))
         return loss.value, tuple(grads)
 
+    def forward(self, steps: int, checkpoint_every: int = 0) -> "HydroTape":
+        """Run `steps` steps keeping checkpoints (om_hydro_forward); the tape
+        then maps any cotangent of the final state back (HydroTape.backward)."""
+        t = C.c_void_p()
+        _check(self._L.om_hydro_forward(self._h, int(steps), int(checkpoint_every), C.byref(t)))
+        return HydroTape(self, t)
+
+    def backward(self, tape: "HydroTape", cot_final):
+        """dL/d(start state) of a tape from dL/d(final state) (four
+        memory-sized arrays: density, velocity0, velocity1, pressure)."""
+        dt = self.array_dtypes["density"]
+        cots = [np.ascontiguousarray(c, dt) for c in cot_final]
+        if len(cots) != 4 or any(c.shape != tuple(self.memory_shape) for c in cots):
+            raise ValueError("backward: four arrays of the memory shape")
+        grads = [np.empty(self.memory_shape, dt) for _ in range(4)]
+        a = (C.c_void_p * 4)(*[c.ctypes.data for c in cots])
+        b = (C.c_void_p * 4)(*[g.ctypes.data for g in grads])
+        _check(self._L.om_hydro_backward(self._h, tape._t, a, b))
+        return tuple(grads)
+
     def time_vjp(self, reps: int = 5) -> float:
         ms = C.c_float()
         _check(self._L.om_hydro_time_vjp(self._h, int(reps), C.byref(ms)))
@@ -412,6 +436,36 @@ def ensemble_sizes(count: int, seed: int, lo: int = 256, hi: int = 2048, step: i
         h1 = mix(mix(seed) + (2 * k + 1) * 0x9E3779B97F4A7C15)
         out.append((lo + step * (h0 % m), lo + step * (h1 % m)))
     return out
+
+
+class HydroTape:
+    """Checkpoints of one om_hydro_forward run, for om_hydro_backward."""
+
+    def __init__(self, hydro: "Hydro", handle: C.c_void_p):
+        self._hydro = hydro
+        self._t = handle
+
+    def backward(self, cot_final):
+        if not self._t:
+            raise OMError(1, "tape is closed")
+        return self._hydro.backward(self, cot_final)
+
+    def close(self) -> None:
+        if self._t:
+            self._hydro._L.om_hydro_tape_free(self._t)
+            self._t = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Ensemble:

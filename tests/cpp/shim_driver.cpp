@@ -31,7 +31,7 @@ int main(int argc, char **argv) {
   }
   if (argc >= 4 && !std::strcmp(argv[1], "hydro")) {
     const int n = std::atoi(argv[2]);
-    Hydro sim(n, n, 1.4);
+    Hydro sim(n, n, 1.4, OM_BOUNDARY_CYCLIC);
     sim.time() = 0;
     sim.cfl() = 0.4;
     sim.extent0() = 1.0;
@@ -57,6 +57,29 @@ int main(int argc, char **argv) {
     std::printf("time %.17g\nmass0 %.17g\nmass %.17g\n", sim.time(), mass0, mass);
     return 0;
   }
-  std::fprintf(stderr, "usage: shim_driver life N0 N1 STEPS | hydro N STEPS\n");
+  if (argc >= 4 && !std::strcmp(argv[1], "hydro_open")) {
+    // the generated class's defaults: open boundary, gamma 5/3, jet init
+    const int n = std::atoi(argv[2]);
+    Hydro sim(n, n);
+    sim.time() = 0;
+    sim.cfl() = 0.5;
+    sim.extent0() = 1.0;
+    sim.extent1() = 1.0;
+    sim.dR0() = sim.extent0() / n;
+    sim.dR1() = sim.extent1() / n;
+    sim.init();
+    for (int t = 0; t < std::atoi(argv[3]); ++t) sim.proceed();
+    double mass = 0, px = 0;
+    for (int y = 0; y < n; ++y)
+      for (int x = 0; x < n; ++x) {
+        mass += sim.density(x, y);
+        px += sim.density(x, y) * sim.velocity0(x, y);
+      }
+    std::printf("time %.17g\nmass %.17g\npx %.17g\nmargin %d\n", sim.time(), mass, px,
+                sim.om_lower_margin_0());
+    return 0;
+  }
+  std::fprintf(stderr,
+               "usage: shim_driver life N0 N1 STEPS | hydro N STEPS | hydro_open N STEPS\n");
   return 2;
 }

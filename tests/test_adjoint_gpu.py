@@ -117,3 +117,52 @@ def test_multistep_gradient_vs_tangent_linear(om_lib, oracle, ck):
         ad = sum(float((g * b).sum()) for g, b in zip(grad, d))
         assert abs(ad - tl) <= 1e-12 * abs(tl), (ad, tl)
     h.close()
+
+
+def test_forward_backward_pair(om_lib, oracle):
+    # om_hydro_forward / om_hydro_backward with an arbitrary cotangent on all
+    # four fields: <cot, TL(d)> == <backward(cot), d>; the same tape serves a
+    # second cotangent, and the loss cotangent reproduces adjoint_run
+    size = (48, 40)
+    steps = 7
+    st = noisy_kh(oracle, size, 11)
+    h = make(om_lib, size, 64)
+    h.set_state(st)
+    rng = np.random.default_rng(17)
+    with h.forward(steps, checkpoint_every=3) as tape:
+        ref, _, _ = oracle.hydro_run(st, steps, cyclic=True, gamma=GAMMA, cfl=CFL)
+        for a, b in zip(h.state(), ref):
+            assert np.array_equal(a, b)
+        d = tuple(rng.standard_normal(a.shape) * s for a, s in zip(st, (0.1, 0.05, 0.05, 0.1)))
+        _, dfin, _ = oracle.hydro_tl_run(st, d, steps, gamma=GAMMA, cfl=CFL)
+        for _ in range(2):
+            cot = tuple(rng.standard_normal(a.shape) for a in st)
+            grad = tape.backward(cot)
+            tl = sum(float((c * t).sum()) for c, t in zip(cot, dfin))
+            ad = sum(float((g * b).sum()) for g, b in zip(grad, d))
+            assert abs(ad - tl) <= 1e-12 * abs(tl), (ad, tl)
+        for a, b in zip(h.state(), ref):     # left at the final state
+            assert np.array_equal(a, b)
+        target = np.full(st[0].shape, 1.5)
+        loss_cot = (2 * (ref[0] - target) / ref[0].size, np.zeros_like(ref[0]),
+                    np.zeros_like(ref[0]), np.zeros_like(ref[0]))
+        g1 = tape.backward(loss_cot)
+    h.set_state(st)
+    h.set_scalar("time", 0.0)
+    _, g2 = h.adjoint_run(steps, target, checkpoint_every=3)
+    for a, b in zip(g1, g2):
+        assert np.array_equal(a, b)
+    h.close()
+
+
+def test_backward_rejects_foreign_tape(om_lib, oracle):
+    size = (32, 32)
+    st = noisy_kh(oracle, size, 2)
+    a, b = make(om_lib, size, 64), make(om_lib, size, 64)
+    a.set_state(st)
+    b.set_state(st)
+    with a.forward(2) as tape:
+        with pytest.raises(om_lib.OMError):
+            b.backward(tape, [np.zeros(st[0].shape)] * 4)
+    a.close()
+    b.close()

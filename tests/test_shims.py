@@ -55,3 +55,20 @@ def test_shim_driver_hydro_conserves_mass(om_lib, tmp_path):
     vals = dict(l.split() for l in out if l)
     assert float(vals["time"]) > 0
     assert abs(float(vals["mass"]) - float(vals["mass0"])) < 1e-11 * float(vals["mass0"])
+
+
+@pytest.mark.gpu
+def test_shim_driver_hydro_open_default(om_lib, oracle, tmp_path):
+    # Hydro(n, n) is the generated class: open boundary, jet inflow, gamma 5/3
+    exe = compile_cpp(os.path.join(ROOT, "tests", "cpp", "shim_driver.cpp"), "shim_driver",
+                      tmp_path)
+    out = subprocess.run([exe, "hydro_open", "64", "6"], check=True, capture_output=True,
+                         text=True).stdout.split("\n")
+    vals = dict(l.split() for l in out if l)
+    assert int(vals["margin"]) == 3
+    st = oracle.hydro_init_jet(64, 64, cyclic=False, gamma=5 / 3, dtype=np.float64)
+    ref, t, _ = oracle.hydro_run(st, 6, cyclic=False, gamma=5 / 3, cfl=0.5, dtype=np.float64)
+    rho, vx = ref[0][3:-3, 3:-3], ref[1][3:-3, 3:-3]
+    assert abs(float(vals["time"]) - t) <= 1e-12 * t
+    assert abs(float(vals["mass"]) - rho.sum()) <= 1e-12 * rho.sum()
+    assert abs(float(vals["px"]) - (rho * vx).sum()) <= 1e-9 * abs(rho * vx).sum()
