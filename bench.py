@@ -579,6 +579,11 @@ def life_cpu_baseline(n: int, args) -> dict:
 def reference_arm(args, dist: Dist) -> dict | None:
     if dist.rank != 0:
         return None
+    if args.workload == "adjoint":
+        return {"impl": "reference",
+                "unavailable": "the reference has no adjoint of the Hydro step to time"}
+    if args.workload in ("hydro4k", "ensemble"):
+        return reference_hydro(args, dist)
     from oracle import pyoracle as O
     O.build()
     n = args.size or (128 if args.workload == "life128" else 16384)
@@ -611,6 +616,55 @@ def reference_arm(args, dist: Dist) -> dict | None:
                                    "generated Life loop, pinned bit-exact to the reference's "
                                    "pre-generated Life.cpp"},
         "e2e": {"value": round(value, 4), "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def reference_hydro(args, dist: Dist) -> dict:
+    """The oracle's FP32 Hydro step (the reference's generated Hydro is
+    float) on the host cores: one step of the 4096^2 grid, or one step of
+    every ensemble instance, per timed step."""
+    import paraiso_gb300 as pg
+    from oracle import pyoracle as O
+    O.build()
+    if args.workload == "hydro4k":
+        n = args.size or 4096
+        grids = [(n, n, 1)]
+        metric = "Hydro cell-updates/s (Gcell-updates/s), FP32 bulk, FP64 dt/totals"
+        workload = f"hydro {n}x{n} periodic Kelvin-Helmholtz, gamma 1.4, CFL 0.4"
+    else:
+        sizes = pg.ensemble_sizes(args.count, 1)
+        grids = [(a, b, 1000 + k) for k, (a, b) in enumerate(sizes)]
+        metric = "Hydro ensemble cell-updates/s (Gcell-updates/s), FP32, per-instance CFL dt"
+        workload = (f"{args.count} periodic Kelvin-Helmholtz instances, n0,n1 uniform over "
+                    "multiples of 32 in [256,2048] (seed 1)")
+    states = [tuple(a.astype(np.float32) for a in O.hydro_init_kh(a, b, seed))
+              for a, b, seed in grids]
+    cells = sum(a * b for a, b, _ in grids)
+    steps = max(1, min(args.steps, 3))
+    for k, st in enumerate(states):       # warm-up: one step
+        states[k], _, _ = O.hydro_run(st, 1, cyclic=True, gamma=1.4, cfl=0.4, dtype=np.float32)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for k, st in enumerate(states):
+            states[k], _, _ = O.hydro_run(st, 1, cyclic=True, gamma=1.4, cfl=0.4,
+                                          dtype=np.float32)
+    tot = time.perf_counter() - t0
+    value = cells * steps / tot / 1e9
+    cores = O.lib().oracle_num_threads()
+    return {
+        "impl": "reference", "metric": metric, "value": round(value, 5),
+        "unit": "Gcell-updates/s", "n_gpus": dist.world, "steps": steps, "warmup": args.warmup,
+        "ms_per_step": round(tot / steps * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": workload, "cells": cells},
+        "cpu_baseline": {"value": round(value, 5), "unit": "Gcell-updates/s", "cores": cores,
+                         "kind": "port",
+                         "sample": f"{steps} FP32 steps of {len(grids)} grid(s), {cells} cells; "
+                                   "CPU restatement (oracle/om_oracle.cpp, OpenMP) of the "
+                                   "generated Hydro step, pinned bit-exact to the reference's "
+                                   "pre-generated Hydro.cpp"},
+        "e2e": {"value": round(value, 5), "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
 

@@ -46,7 +46,7 @@ typedef enum {
   OM_ERR_STATE = 7         /* call not valid in the handle's current state */
 } om_status;
 
-typedef enum { OM_KIND_LIFE = 1, OM_KIND_HYDRO = 2 } om_kind;
+typedef enum { OM_KIND_LIFE = 1, OM_KIND_HYDRO = 2, OM_KIND_GRAPH = 3 } om_kind;
 typedef enum { OM_BOUNDARY_CYCLIC = 0, OM_BOUNDARY_OPEN = 1 } om_boundary;
 typedef enum { OM_SCALAR_INT = 0, OM_SCALAR_DOUBLE = 1 } om_scalar_type;
 
@@ -245,6 +245,35 @@ om_status om_ensemble_last_launch_count(om_ensemble e, int *launches);
 /* Autotune the ensemble's tile shape for these instance sizes. */
 om_status om_autotune_ensemble(int count, const int *sizes, const om_config *base,
                                om_config *best, double *best_rate);
+
+/* ---- general OM graphs ---------------------------------------------------
+ * The generator's input (Language/Paraiso/OM/Graph.hs:113-123: Load, Store,
+ * Shift, Imm, Arith, Reduce, Broadcast, LoadIndex, LoadSize) as text, one
+ * node per line, compiled at run time into CUDA kernels for this GPU:
+ *
+ *   om NAME NDIM N0 [N1] cyclic|open
+ *   static NAME array|scalar int|float|double|bool
+ *   kernel NAME
+ *   ID load REALM TYPE STATIC         ID imm REALM TYPE LITERAL
+ *   ID shift array TYPE NODE V0 [V1]  ID loadindex array int AXIS
+ *   ID loadsize scalar int AXIS       ID reduce scalar TYPE sum|min|max NODE
+ *   ID broadcast array TYPE NODE      ID OP REALM TYPE NODE...  (add sub mul
+ *     div mod neg inv not and or eq ne lt le gt ge select max min abs signum
+ *     sqrt exp log sin cos tan asin acos atan atan2 pow cast)
+ *   store STATIC NODE
+ *   end
+ *
+ * (paraiso_gb300/omgraph.py writes it from Builder-style Python.)  The
+ * handle then works as any other: kernels by name (om_kernel_id, om_run),
+ * statics through om_scalar_ptr / om_array_* with the margins an open mesh
+ * needs.  Scalar types: 0 int (and bool), 1 double, 2 float. */
+om_status om_create_graph(const char *text, const om_config *cfg, om_handle *out);
+/* The CUDA source generated for a graph handle (owned by the handle). */
+om_status om_graph_source(om_handle h, const char **source);
+/* Parse, plan, generate and compile a graph for sm_<major><minor>a without a
+ * device (no handle); *source, if given, receives the generated CUDA source
+ * (valid until the next call on this thread). */
+om_status om_graph_check(const char *text, int major, int minor, const char **source);
 
 /* ---- caller-owned buffers, no allocation -------------------------------- */
 

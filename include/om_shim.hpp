@@ -56,6 +56,10 @@ class machine {
     const int sizes[2] = {n0, n1};
     check(om_create(kind, 2, sizes, &cfg, &h_), "om_create");
   }
+  // a general OM graph (om_create_graph), compiled for this GPU
+  explicit machine(const char *graph_text) {
+    check(om_create_graph(graph_text, nullptr, &h_), "om_create_graph");
+  }
   ~machine() { om_destroy(h_); }
   machine(const machine &) = delete;
   machine &operator=(const machine &) = delete;

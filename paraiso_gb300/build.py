@@ -72,7 +72,7 @@ def build(verbose: bool = False, extra_flags: list[str] | None = None) -> str:
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         list(ex.map(run, jobs))
     if jobs or _stale(OUT, objs):
-        run([nvcc(), *ARCH, "-shared", "-o", OUT, *objs, "-lcudart"])
+        run([nvcc(), *ARCH, "-shared", "-o", OUT, *objs, "-lcudart", "-lnvrtc"])
     return OUT
 
 

@@ -169,6 +169,70 @@ namespace om {
 Handle *handle_of(om_handle H) { return H ? &H->h : nullptr; }
 }  // namespace om
 
+namespace om {
+
+om_status create_handle(int kind, const int sizes[2], const om_config &cfg,
+                        om_status (*setup)(Handle *, void *), void *ctx, om_handle *out) {
+  om_config c = cfg;
+  *out = nullptr;
+  if (c.boundary != OM_BOUNDARY_CYCLIC && c.boundary != OM_BOUNDARY_OPEN) {
+    set_error("om_create: boundary must be cyclic (0) or open (1)");
+    return OM_ERR_ARG;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    set_error("om_create: no CUDA device available");
+    return OM_ERR_CUDA;
+  }
+  if (c.device < 0 || c.device >= ndev) {
+    set_error("om_create: device ordinal out of range");
+    return OM_ERR_ARG;
+  }
+  OM_CUDA_CHECK(cudaSetDevice(c.device));
+  om_handle H = new om_handle_s();
+  Handle *h = &H->h;
+  h->kind = kind;
+  h->ndim = 2;
+  h->size[0] = sizes[0];
+  h->size[1] = sizes[1];
+  h->cyclic = c.boundary == OM_BOUNDARY_CYCLIC;
+  h->cfg = c;
+  h->device = c.device;
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    delete H;
+    set_error("om_create: cudaStreamCreate failed");
+    return OM_ERR_CUDA;
+  }
+  h->own_stream = true;
+  om_status s = setup(h, ctx);
+  if (s == OM_OK && h->scalar_bytes) {
+    if (cudaMallocHost(&h->h_scalars, h->scalar_bytes) != cudaSuccess ||
+        cudaMalloc(&h->d_scalars, h->scalar_bytes) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("om_create: scalar block allocation failed");
+      s = OM_ERR_NOMEM;
+    } else {
+      std::memset(h->h_scalars, 0, h->scalar_bytes);
+    }
+  }
+  if (s == OM_OK && cudaStreamSynchronize(h->stream) != cudaSuccess) {
+    set_error(std::string("om_create: ") + cudaGetErrorString(cudaGetLastError()));
+    s = OM_ERR_CUDA;
+  }
+  if (s != OM_OK) {
+    std::string keep = g_last_error;
+    om_destroy(H);
+    set_error(keep);
+    return s;
+  }
+  *out = H;
+  return OM_OK;
+}
+
+}  // namespace om
+
 extern "C" {
 
 void om_config_default(om_config *cfg) {
@@ -203,60 +267,12 @@ om_status om_create(int kind, int ndim, const int *sizes, const om_config *cfg,
   }
   om_config c;
   if (cfg) c = *cfg; else om_config_default(&c);
-  if (c.boundary != OM_BOUNDARY_CYCLIC && c.boundary != OM_BOUNDARY_OPEN) {
-    set_error("om_create: boundary must be cyclic (0) or open (1)");
-    return OM_ERR_ARG;
-  }
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
-    cudaGetLastError();
-    set_error("om_create: no CUDA device available");
-    return OM_ERR_CUDA;
-  }
-  if (c.device < 0 || c.device >= ndev) {
-    set_error("om_create: device ordinal out of range");
-    return OM_ERR_ARG;
-  }
-  OM_CUDA_CHECK(cudaSetDevice(c.device));
-  om_handle H = new om_handle_s();
-  Handle *h = &H->h;
-  h->kind = kind;
-  h->ndim = 2;
-  h->size[0] = sizes[0];
-  h->size[1] = sizes[1];
-  h->cyclic = c.boundary == OM_BOUNDARY_CYCLIC;
-  h->cfg = c;
-  h->device = c.device;
-  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
-    cudaGetLastError();
-    delete H;
-    set_error("om_create: cudaStreamCreate failed");
-    return OM_ERR_CUDA;
-  }
-  h->own_stream = true;
-  om_status s = kind == OM_KIND_LIFE ? life_setup(h) : hydro_setup(h);
-  if (s == OM_OK && h->scalar_bytes) {
-    if (cudaMallocHost(&h->h_scalars, h->scalar_bytes) != cudaSuccess ||
-        cudaMalloc(&h->d_scalars, h->scalar_bytes) != cudaSuccess) {
-      cudaGetLastError();
-      set_error("om_create: scalar block allocation failed");
-      s = OM_ERR_NOMEM;
-    } else {
-      std::memset(h->h_scalars, 0, h->scalar_bytes);
+  struct Kind {
+    static om_status setup(Handle *h, void *) {
+      return h->kind == OM_KIND_LIFE ? life_setup(h) : hydro_setup(h);
     }
-  }
-  if (s == OM_OK && cudaStreamSynchronize(h->stream) != cudaSuccess) {
-    set_error(std::string("om_create: ") + cudaGetErrorString(cudaGetLastError()));
-    s = OM_ERR_CUDA;
-  }
-  if (s != OM_OK) {
-    std::string keep = g_last_error;
-    om_destroy(H);
-    set_error(keep);
-    return s;
-  }
-  *out = H;
-  return OM_OK;
+  };
+  return create_handle(kind, sizes, c, Kind::setup, nullptr, out);
 }
 
 om_status om_destroy(om_handle H) {
@@ -340,6 +356,7 @@ static om_status finish(Handle *h) {
 static om_status run_plain(om_handle H, int kernel_id, int n) {
   Handle *h = &H->h;
   h->launches = 0;
+  h->current_kernel = kernel_id;
   om_status s = h->kernels[kernel_id].fn(h, n);
   H->last_launches = h->launches;
   return s;

@@ -51,7 +51,7 @@ struct Array {
   void swap() { cur = 1 - cur; }
 };
 
-enum ScalarType { kInt = 0, kDouble = 1 };
+enum ScalarType { kInt = 0, kDouble = 1, kFloat = 2 };
 
 struct Scalar {
   std::string name;
@@ -121,6 +121,7 @@ struct Handle {
   void (*impl_free)(Handle *) = nullptr;
   KindOps ops;
   int launches = 0;           // kernel launches issued by the current run
+  int current_kernel = -1;    // index of the kernel whose function is running
   bool profiling = false;
   bool capturing = false;
   std::vector<ProfPending> prof_pending;
@@ -133,6 +134,11 @@ struct Handle {
   Array *find_array(const char *n);
   Scalar *find_scalar(const char *n);
 };
+
+// Create a handle: stream, then `setup` (which adds arrays, scalars and
+// kernels), then the scalar block.  Used by om_create and om_create_graph.
+om_status create_handle(int kind, const int sizes[2], const om_config &cfg,
+                        om_status (*setup)(Handle *, void *), void *ctx, om_handle *out);
 
 // Allocate an OM array (double-buffered device storage, zero-filled).
 om_status alloc_array(Handle *h, const char *name, int elem_size);

@@ -1,0 +1,954 @@
+// omgraph.cu -- Orthotope Machine graphs compiled into GB300 kernels at run
+// time.  The reference's generator lowers an OM graph to a plan of
+// sub-kernels and prints C++/CUDA for them
+// (Language/Paraiso/Generator/OMTrans.hs:39-56, PlanTrans.hs:282-596).  Here
+// the graph arrives as text (the format of paraiso_gb300/omgraph.py), and
+// each OM kernel becomes a few CUDA kernels generated as source and compiled
+// with NVRTC for sm_103a:
+//   * one "stage" per reduce depth: a grid-stride pass over the memory array
+//     that writes every array store of that depth (its value on its valid
+//     region, zero elsewhere, into the static's other buffer) and folds every
+//     reduce of that depth into per-block partials; the last block combines
+//     the partials in a fixed order;
+//   * one "commit" thread that evaluates the scalar stores.
+// Values other than stores and reduces are recomputed where they are used
+// (the generator's Delayed allocation), once per (node, offset) per cell.
+// Semantics followed: valid regions (Optimization/BoundaryAnalysis.hs:33-94),
+// margins (OMTrans.hs:103-120), shift reads x[c - v] (PlanTrans.hs:561-562),
+// loadIndex / loadSize (PlanTrans.hs:455-466), Arith -> C (PlanTrans.hs:
+// 670-710), statics updated when the kernel ends (PlanTrans.hs:243-258).
+#include <cuda_runtime.h>
+#include <nvrtc.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "om_internal.cuh"
+
+namespace om {
+namespace og {
+
+enum Type { TInt = 0, TFloat, TDouble, TBool };
+
+static const char *ctype(Type t) {
+  switch (t) {
+    case TInt: return "int";
+    case TFloat: return "float";
+    case TDouble: return "double";
+    default: return "bool";
+  }
+}
+static int tsize(Type t) { return t == TDouble ? 8 : (t == TBool ? 1 : 4); }
+
+struct Node {
+  int id = -1;
+  std::string op;
+  bool array = true;
+  Type type = TInt;
+  std::vector<int> args;  // operand node ids
+  std::string sarg;       // static name, reduce operator or literal
+  int vec[2] = {0, 0};    // shift vector or axis
+};
+
+struct Store {
+  int stat;
+  int node;
+};
+
+struct KernelDef {
+  std::string name;
+  std::vector<Node> nodes;
+  std::map<int, int> at;  // node id -> index in nodes
+  std::vector<Store> stores;
+  const Node &node(int id) const { return nodes[at.at(id)]; }
+};
+
+struct StaticDef {
+  std::string name;
+  bool array;
+  Type type;
+  size_t offset = 0;  // scalar: byte offset in the scalar block
+};
+
+struct Graph {
+  std::string name;
+  int ndim = 2;
+  int size[2] = {1, 1};
+  bool open = false;
+  std::vector<StaticDef> statics;
+  std::vector<KernelDef> kernels;
+  int find_static(const std::string &n) const {
+    for (size_t i = 0; i < statics.size(); ++i)
+      if (statics[i].name == n) return (int)i;
+    return -1;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// parsing
+// ---------------------------------------------------------------------------
+
+static bool parse_type(const std::string &s, Type *t) {
+  if (s == "int") *t = TInt;
+  else if (s == "float") *t = TFloat;
+  else if (s == "double") *t = TDouble;
+  else if (s == "bool") *t = TBool;
+  else return false;
+  return true;
+}
+
+static const char *kArith[] = {"add", "sub", "mul", "div", "mod", "neg", "inv", "not",
+                               "and", "or", "eq", "ne", "lt", "le", "gt", "ge",
+                               "select", "max", "min", "abs", "signum", "sqrt", "exp",
+                               "log", "sin", "cos", "tan", "asin", "acos", "atan",
+                               "atan2", "pow", "cast"};
+
+static int arity(const std::string &op) {
+  static const char *one[] = {"neg", "inv", "not", "abs", "signum", "sqrt", "exp", "log",
+                              "sin", "cos", "tan", "asin", "acos", "atan", "cast"};
+  for (const char *o : one)
+    if (op == o) return 1;
+  if (op == "select") return 3;
+  return 2;
+}
+
+static bool is_arith(const std::string &op) {
+  for (const char *o : kArith)
+    if (op == o) return true;
+  return false;
+}
+
+static om_status perr(int line, const std::string &what) {
+  set_error("om_create_graph: line " + std::to_string(line) + ": " + what);
+  return OM_ERR_ARG;
+}
+
+static om_status parse(const char *text, Graph *g) {
+  std::istringstream in(text);
+  std::string l;
+  int ln = 0;
+  KernelDef *k = nullptr;
+  bool head = false;
+  while (std::getline(in, l)) {
+    ++ln;
+    std::istringstream ws(l);
+    std::vector<std::string> w;
+    for (std::string t; ws >> t;) w.push_back(t);
+    if (w.empty() || w[0][0] == '#') continue;
+    if (!head) {
+      if (w[0] != "om" || w.size() < 4) return perr(ln, "expected 'om NAME NDIM SIZES BOUNDARY'");
+      g->name = w[1];
+      g->ndim = std::atoi(w[2].c_str());
+      if (g->ndim < 1 || g->ndim > 2 || (int)w.size() != 4 + g->ndim)
+        return perr(ln, "1 or 2 dimensions");
+      for (int a = 0; a < g->ndim; ++a) {
+        g->size[a] = std::atoi(w[3 + a].c_str());
+        if (g->size[a] < 1 || g->size[a] > (1 << 20)) return perr(ln, "size out of range");
+      }
+      const std::string &b = w[3 + g->ndim];
+      if (b != "cyclic" && b != "open") return perr(ln, "boundary cyclic or open");
+      g->open = b == "open";
+      head = true;
+      continue;
+    }
+    if (w[0] == "static") {
+      if (k || w.size() != 4) return perr(ln, "static NAME array|scalar TYPE");
+      StaticDef s;
+      s.name = w[1];
+      if (w[2] != "array" && w[2] != "scalar") return perr(ln, "realm array or scalar");
+      s.array = w[2] == "array";
+      if (!parse_type(w[3], &s.type)) return perr(ln, "unknown type " + w[3]);
+      if (g->find_static(s.name) >= 0) return perr(ln, "duplicate static " + s.name);
+      g->statics.push_back(s);
+      continue;
+    }
+    if (w[0] == "kernel") {
+      if (k || w.size() != 2) return perr(ln, "kernel NAME (inside no other kernel)");
+      g->kernels.push_back(KernelDef());
+      k = &g->kernels.back();
+      k->name = w[1];
+      continue;
+    }
+    if (w[0] == "end") {
+      if (!k) return perr(ln, "end outside a kernel");
+      k = nullptr;
+      continue;
+    }
+    if (!k) return perr(ln, "node outside a kernel");
+    if (w[0] == "store") {
+      if (w.size() != 3) return perr(ln, "store STATIC NODE");
+      const int s = g->find_static(w[1]);
+      const int id = std::atoi(w[2].c_str());
+      if (s < 0) return perr(ln, "no static " + w[1]);
+      if (!k->at.count(id)) return perr(ln, "unknown node " + w[2]);
+      const Node &v = k->node(id);
+      if (v.array != g->statics[s].array || v.type != g->statics[s].type)
+        return perr(ln, "store of a value whose realm or type differs from " + w[1]);
+      k->stores.push_back(Store{s, id});
+      continue;
+    }
+    if (w.size() < 4) return perr(ln, "ID OP REALM TYPE ...");
+    Node n;
+    n.id = std::atoi(w[0].c_str());
+    n.op = w[1];
+    if (w[2] != "array" && w[2] != "scalar") return perr(ln, "realm array or scalar");
+    n.array = w[2] == "array";
+    if (!parse_type(w[3], &n.type)) return perr(ln, "unknown type " + w[3]);
+    if (k->at.count(n.id)) return perr(ln, "duplicate node id");
+    auto node_arg = [&](size_t i, int *out) -> bool {
+      if (i >= w.size()) return false;
+      const int id = std::atoi(w[i].c_str());
+      if (!k->at.count(id)) return false;
+      *out = id;
+      return true;
+    };
+    if (n.op == "load") {
+      if (w.size() != 5) return perr(ln, "load STATIC");
+      const int s = g->find_static(w[4]);
+      if (s < 0) return perr(ln, "no static " + w[4]);
+      if (g->statics[s].array != n.array || g->statics[s].type != n.type)
+        return perr(ln, "load realm/type differs from the static");
+      n.sarg = w[4];
+    } else if (n.op == "imm") {
+      if (w.size() != 5) return perr(ln, "imm LITERAL");
+      n.sarg = w[4];
+    } else if (n.op == "shift") {
+      if ((int)w.size() != 5 + g->ndim || !n.array) return perr(ln, "shift NODE V0 [V1]");
+      int a;
+      if (!node_arg(4, &a) || !k->node(a).array) return perr(ln, "shift of an array node");
+      n.args.push_back(a);
+      for (int d = 0; d < g->ndim; ++d) n.vec[d] = std::atoi(w[5 + d].c_str());
+      if (k->node(a).type != n.type) return perr(ln, "shift keeps the type");
+    } else if (n.op == "loadindex" || n.op == "loadsize") {
+      if (w.size() != 5) return perr(ln, n.op + " AXIS");
+      n.vec[0] = std::atoi(w[4].c_str());
+      if (n.vec[0] < 0 || n.vec[0] >= g->ndim) return perr(ln, "axis out of range");
+      if (n.type != TInt || n.array != (n.op == "loadindex"))
+        return perr(ln, "loadindex is an int array, loadsize an int scalar");
+    } else if (n.op == "reduce") {
+      if (w.size() != 6 || n.array) return perr(ln, "reduce OP NODE (a scalar)");
+      n.sarg = w[4];
+      if (n.sarg != "sum" && n.sarg != "min" && n.sarg != "max")
+        return perr(ln, "reduce sum|min|max");
+      int a;
+      if (!node_arg(5, &a) || !k->node(a).array || k->node(a).type != n.type ||
+          n.type == TBool)
+        return perr(ln, "reduce of a numeric array node of the same type");
+      n.args.push_back(a);
+    } else if (n.op == "broadcast") {
+      int a;
+      if (w.size() != 5 || !n.array || !node_arg(4, &a) || k->node(a).array ||
+          k->node(a).type != n.type)
+        return perr(ln, "broadcast of a scalar node of the same type");
+      n.args.push_back(a);
+    } else if (is_arith(n.op)) {
+      const int ar = arity(n.op);
+      if ((int)w.size() != 4 + ar) return perr(ln, n.op + " takes " + std::to_string(ar));
+      for (int i = 0; i < ar; ++i) {
+        int a;
+        if (!node_arg(4 + i, &a)) return perr(ln, "unknown operand");
+        if (k->node(a).array != n.array) return perr(ln, "operand realm differs");
+        n.args.push_back(a);
+      }
+      if (n.op == "mod" && n.type != TInt) return perr(ln, "mod of int values");
+    } else {
+      return perr(ln, "unknown operation " + n.op);
+    }
+    k->at[n.id] = (int)k->nodes.size();
+    k->nodes.push_back(n);
+  }
+  if (!head) return perr(ln, "empty graph");
+  if (k) return perr(ln, "kernel without end");
+  return OM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// valid regions and margins
+// ---------------------------------------------------------------------------
+
+struct Iv {
+  bool lo_inf = true, hi_inf = true;
+  int lo = 0, hi = 0;  // offsets from the lower / upper edge of the array
+};
+struct Region {
+  Iv ax[2];
+};
+
+static Region full_region() {
+  Region r;
+  for (auto &a : r.ax) { a.lo_inf = a.hi_inf = false; a.lo = a.hi = 0; }
+  return r;
+}
+
+static Region meet(const Region &a, const Region &b) {
+  Region r;
+  for (int d = 0; d < 2; ++d) {
+    const Iv &x = a.ax[d], &y = b.ax[d];
+    Iv &z = r.ax[d];
+    z.lo_inf = x.lo_inf && y.lo_inf;
+    z.lo = x.lo_inf ? y.lo : (y.lo_inf ? x.lo : std::max(x.lo, y.lo));
+    z.hi_inf = x.hi_inf && y.hi_inf;
+    z.hi = x.hi_inf ? y.hi : (y.hi_inf ? x.hi : std::min(x.hi, y.hi));
+  }
+  return r;
+}
+
+static std::vector<Region> regions(const KernelDef &k) {
+  std::vector<Region> reg(k.nodes.size());
+  for (size_t i = 0; i < k.nodes.size(); ++i) {
+    const Node &n = k.nodes[i];
+    if (!n.array || n.op == "imm" || n.op == "loadindex" || n.op == "broadcast") {
+      reg[i] = Region();
+    } else if (n.op == "load") {
+      reg[i] = full_region();
+    } else if (n.op == "shift") {
+      Region m = reg[k.at.at(n.args[0])];
+      for (int d = 0; d < 2; ++d) {
+        m.ax[d].lo += n.vec[d];
+        m.ax[d].hi += n.vec[d];
+      }
+      reg[i] = meet(m, full_region());
+    } else {
+      Region r;
+      for (int a : n.args) r = meet(r, reg[k.at.at(a)]);
+      reg[i] = r;
+    }
+  }
+  return reg;
+}
+
+// ---------------------------------------------------------------------------
+// code generation
+// ---------------------------------------------------------------------------
+
+struct Layout {
+  int ms[2];
+  int lm[2];
+  bool open;
+  int size[2];
+};
+
+static std::string lit(Type t, const std::string &s) {
+  if (t == TBool) return (s == "0" || s == "false") ? "false" : "true";
+  if (t == TInt) return "(" + std::to_string(std::strtoll(s.c_str(), nullptr, 10)) + ")";
+  const double v = std::strtod(s.c_str(), nullptr);
+  if (v != v) return t == TFloat ? "(om_inf_f() - om_inf_f())" : "(om_inf_d() - om_inf_d())";
+  if (v == 1.0 / 0.0) return t == TFloat ? "om_inf_f()" : "om_inf_d()";
+  if (v == -1.0 / 0.0) return t == TFloat ? "(-om_inf_f())" : "(-om_inf_d())";
+  char buf[64];
+  std::snprintf(buf, sizeof buf, "%a", v);
+  return t == TFloat ? std::string("((float)") + buf + ")" : std::string("(") + buf + ")";
+}
+
+// Emits the statements computing (node, offset) values of one kernel, each
+// once, into a block of code.
+class Emitter {
+ public:
+  Emitter(const Graph &g, const KernelDef &k, const Layout &L,
+          const std::map<int, int> &slot_of_reduce)
+      : g_(g), k_(k), L_(L), slots_(slot_of_reduce) {}
+
+  std::string code;
+
+  std::string value(int id, int o0, int o1) {
+    const Node &n = k_.node(id);
+    if (!n.array) o0 = o1 = 0;
+    const auto key = std::make_tuple(id, o0, o1);
+    auto it = memo_.find(key);
+    if (it != memo_.end()) return it->second;
+    std::string expr;
+    const std::string T = ctype(n.type);
+    if (n.op == "load") {
+      const int s = g_.find_static(n.sarg);
+      if (g_.statics[s].array)
+        expr = "((const " + T + " *)P.cur[" + std::to_string(array_index(s)) + "])[" +
+               addr(o0, o1) + "]";
+      else
+        expr = scalar_read(g_.statics[s]);
+    } else if (n.op == "imm") {
+      expr = lit(n.type, n.sarg);
+    } else if (n.op == "shift") {
+      return memo_[key] = value(n.args[0], o0 - n.vec[0], o1 - n.vec[1]);
+    } else if (n.op == "loadindex") {
+      const int ax = n.vec[0];
+      const std::string c = ax == 0 ? "c0" : "c1";
+      const int off = (ax == 0 ? o0 : o1) - L_.lm[ax];
+      if (L_.open)
+        expr = "(" + c + " + (" + std::to_string(off) + "))";
+      else
+        expr = wrap(c, ax == 0 ? o0 : o1, L_.ms[ax]);
+    } else if (n.op == "loadsize") {
+      expr = std::to_string(g_.size[n.vec[0]]);
+    } else if (n.op == "reduce") {
+      expr = "(*(const " + T + " *)(slots + " + std::to_string(8 * slots_.at(id)) + "))";
+    } else if (n.op == "broadcast") {
+      return memo_[key] = value(n.args[0], 0, 0);
+    } else {
+      std::vector<std::string> a;
+      for (int x : n.args) a.push_back(value(x, o0, o1));
+      expr = arith(n, a);
+    }
+    const std::string v = "v" + std::to_string(id) + "_" + off_name(o0) + "_" + off_name(o1);
+    code += "      const " + T + " " + v + " = " + expr + ";\n";
+    return memo_[key] = v;
+  }
+
+  int array_index(int s) const {
+    int k = 0;
+    for (int i = 0; i < s; ++i) k += g_.statics[i].array ? 1 : 0;
+    return k;
+  }
+
+ private:
+  static std::string off_name(int o) { return o < 0 ? "m" + std::to_string(-o) : std::to_string(o); }
+
+  std::string wrap(const std::string &c, int o, int n) const {
+    if (o == 0) return c;
+    const std::string x = "(" + c + " + (" + std::to_string(o) + "))";
+    return "((" + x + " % " + std::to_string(n) + " + " + std::to_string(n) + ") % " +
+           std::to_string(n) + ")";
+  }
+
+  std::string addr(int o0, int o1) const {
+    std::string x, y;
+    if (L_.open) {
+      x = "(c0 + (" + std::to_string(o0) + "))";
+      y = "(c1 + (" + std::to_string(o1) + "))";
+    } else {
+      x = wrap("c0", o0, L_.ms[0]);
+      y = wrap("c1", o1, L_.ms[1]);
+    }
+    return "(long long)" + y + " * " + std::to_string(L_.ms[0]) + " + " + x;
+  }
+
+  std::string scalar_read(const StaticDef &s) const {
+    const std::string off = std::to_string(s.offset);
+    if (s.type == TBool) return "(*(const int *)(SC + " + off + ") != 0)";
+    return "(*(const " + std::string(ctype(s.type)) + " *)(SC + " + off + "))";
+  }
+
+  std::string arith(const Node &n, const std::vector<std::string> &a) const {
+    const std::string &op = n.op;
+    const std::string T = ctype(n.type);
+    auto bin = [&](const char *o) { return "(" + a[0] + " " + o + " " + a[1] + ")"; };
+    if (op == "add") return bin("+");
+    if (op == "sub") return bin("-");
+    if (op == "mul") return bin("*");
+    if (op == "div") return bin("/");
+    if (op == "mod") return bin("%");
+    if (op == "neg") return "(-" + a[0] + ")";
+    if (op == "inv") return "(1 / " + a[0] + ")";
+    if (op == "not") return "(!" + a[0] + ")";
+    if (op == "and") return bin("&&");
+    if (op == "or") return bin("||");
+    if (op == "eq") return bin("==");
+    if (op == "ne") return bin("!=");
+    if (op == "lt") return bin("<");
+    if (op == "le") return bin("<=");
+    if (op == "gt") return bin(">");
+    if (op == "ge") return bin(">=");
+    if (op == "select") return "(" + a[0] + " ? " + a[1] + " : " + a[2] + ")";
+    // std::max(a, b) = (a < b) ? b : a;  std::min(a, b) = (b < a) ? b : a
+    if (op == "max") return "((" + a[0] + " < " + a[1] + ") ? " + a[1] + " : " + a[0] + ")";
+    if (op == "min") return "((" + a[1] + " < " + a[0] + ") ? " + a[1] + " : " + a[0] + ")";
+    if (op == "abs") return n.type == TInt ? "abs(" + a[0] + ")" : "fabs(" + a[0] + ")";
+    if (op == "signum")
+      return "((" + T + ")((" + a[0] + " > (" + T + ")0) - (" + a[0] + " < (" + T + ")0)))";
+    if (op == "cast") return "((" + T + ")(" + a[0] + "))";
+    if (op == "atan2" || op == "pow") return op + "(" + a[0] + ", " + a[1] + ")";
+    return op + "(" + a[0] + ")";  // sqrt exp log sin cos tan asin acos atan
+  }
+
+  const Graph &g_;
+  const KernelDef &k_;
+  const Layout &L_;
+  const std::map<int, int> &slots_;
+  std::map<std::tuple<int, int, int>, std::string> memo_;
+};
+
+static std::string region_test(const Region &r, const Layout &L) {
+  if (!L.open) return "true";
+  std::string t = "true";
+  for (int d = 0; d < 2; ++d) {
+    const std::string c = d == 0 ? "c0" : "c1";
+    const Iv &a = r.ax[d];
+    if (!a.lo_inf) t += " && " + c + " >= " + std::to_string(a.lo);
+    if (!a.hi_inf) t += " && " + c + " < " + std::to_string(L.ms[d] + a.hi);
+  }
+  return t;
+}
+
+static bool region_is_all(const Region &r, const Layout &L) {
+  if (!L.open) return true;
+  for (int d = 0; d < 2; ++d) {
+    const Iv &a = r.ax[d];
+    if (!a.lo_inf && a.lo > 0) return false;
+    if (!a.hi_inf && a.hi < 0) return false;
+  }
+  return true;
+}
+
+struct StagePlan {
+  std::vector<int> stores;   // indices into KernelDef::stores (array stores)
+  std::vector<int> reduces;  // reduce node ids
+  std::string fn;
+};
+
+struct KernelPlan {
+  std::vector<StagePlan> stages;
+  std::vector<int> scalar_stores;  // indices into KernelDef::stores
+  std::vector<int> stored_arrays;  // static indices of arrays written
+  std::string commit_fn;
+};
+
+static const char *kPrelude =
+    "struct OMPtrs { const void *cur[32]; void *nxt[32]; };\n"
+    "__device__ __forceinline__ float om_inf_f() { return __int_as_float(0x7f800000); }\n"
+    "__device__ __forceinline__ double om_inf_d() {\n"
+    "  return __longlong_as_double(0x7ff0000000000000LL); }\n";
+
+static std::string ident(Type t, const std::string &op) {
+  if (op == "sum") return std::string("(") + ctype(t) + ")0";
+  const bool mn = op == "min";
+  if (t == TInt) return mn ? "2147483647" : "(-2147483647 - 1)";
+  if (t == TFloat) return mn ? "om_inf_f()" : "(-om_inf_f())";
+  return mn ? "om_inf_d()" : "(-om_inf_d())";
+}
+
+static std::string combine(const std::string &op, const std::string &acc, const std::string &x) {
+  if (op == "sum") return acc + " + " + x;
+  // std::min(acc, x) = (x < acc) ? x : acc;  std::max(acc, x) = (acc < x) ? x : acc
+  if (op == "min") return "((" + x + " < " + acc + ") ? " + x + " : " + acc + ")";
+  return "((" + acc + " < " + x + ") ? " + x + " : " + acc + ")";
+}
+
+// Builds the plan and the CUDA source of every kernel of the graph.
+static std::string generate(const Graph &g, const Layout &L, std::vector<KernelPlan> *plans,
+                            std::map<std::pair<int, int>, int> *slot_map, int *nslots) {
+  std::ostringstream src;
+  src << kPrelude;
+  int slot = 0;
+  for (size_t ki = 0; ki < g.kernels.size(); ++ki) {
+    const KernelDef &k = g.kernels[ki];
+    KernelPlan kp;
+    const std::vector<Region> reg = regions(k);
+    // reduce depth of every node
+    std::vector<int> depth(k.nodes.size(), 0);
+    std::map<int, int> slots;
+    for (size_t i = 0; i < k.nodes.size(); ++i) {
+      const Node &n = k.nodes[i];
+      int d = 0;
+      for (int a : n.args) d = std::max(d, depth[k.at.at(a)]);
+      if (n.op == "reduce") {
+        d += 1;
+        slots[n.id] = slot;
+        (*slot_map)[{(int)ki, n.id}] = slot++;
+      }
+      depth[i] = d;
+    }
+    // the last store to each static wins (manifests are copied in order)
+    std::vector<int> last(g.statics.size(), -1);
+    for (size_t s = 0; s < k.stores.size(); ++s) last[k.stores[s].stat] = (int)s;
+    int nst = 0;
+    for (size_t s = 0; s < k.stores.size(); ++s) {
+      if (last[k.stores[s].stat] != (int)s) continue;
+      const int id = k.stores[s].node;
+      if (g.statics[k.stores[s].stat].array) {
+        nst = std::max(nst, depth[k.at.at(id)] + 1);
+        kp.stored_arrays.push_back(k.stores[s].stat);
+      } else {
+        kp.scalar_stores.push_back((int)s);
+      }
+    }
+    for (const Node &n : k.nodes)
+      if (n.op == "reduce") nst = std::max(nst, depth[k.at.at(n.args[0])] + 1);
+    kp.stages.resize(nst);
+    for (size_t s = 0; s < k.stores.size(); ++s)
+      if (last[k.stores[s].stat] == (int)s && g.statics[k.stores[s].stat].array)
+        kp.stages[depth[k.at.at(k.stores[s].node)]].stores.push_back((int)s);
+    for (const Node &n : k.nodes)
+      if (n.op == "reduce") kp.stages[depth[k.at.at(n.args[0])]].reduces.push_back(n.id);
+
+    for (int st = 0; st < nst; ++st) {
+      StagePlan &sp = kp.stages[st];
+      sp.fn = "om_k" + std::to_string(ki) + "_s" + std::to_string(st);
+      Emitter em(g, k, L, slots);
+      std::ostringstream body;
+      src << "extern \"C\" __global__ void __launch_bounds__(256)\n" << sp.fn
+          << "(OMPtrs P, const unsigned char *SC, unsigned char *slots, unsigned char *part,\n"
+          << "     unsigned int *done) {\n";
+      for (size_t r = 0; r < sp.reduces.size(); ++r) {
+        const Node &n = k.node(sp.reduces[r]);
+        src << "  " << ctype(n.type) << " acc" << r << " = " << ident(n.type, n.sarg) << ";\n";
+      }
+      src << "  const long long N = (long long)" << L.ms[0] << " * " << L.ms[1] << ";\n"
+          << "  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < N;\n"
+          << "       i += (long long)gridDim.x * blockDim.x) {\n"
+          << "    const int c0 = (int)(i % " << L.ms[0] << "), c1 = (int)(i / " << L.ms[0]
+          << ");\n"
+          << "    (void)c0; (void)c1;\n";
+      for (int s : sp.stores) {
+        const Store &so = k.stores[s];
+        const Node &v = k.node(so.node);
+        const std::string T = ctype(v.type);
+        Emitter e(g, k, L, slots);
+        const std::string val = e.value(so.node, 0, 0);
+        src << "    {\n      " << T << " out = (" << T << ")0;\n"
+            << "      if (" << region_test(reg[k.at.at(so.node)], L) << ") {\n"
+            << e.code << "      out = " << val << ";\n      }\n"
+            << "      ((" << T << " *)P.nxt[" << em.array_index(so.stat) << "])[i] = out;\n"
+            << "    }\n";
+      }
+      for (size_t r = 0; r < sp.reduces.size(); ++r) {
+        const Node &n = k.node(sp.reduces[r]);
+        const int in = n.args[0];
+        Emitter e(g, k, L, slots);
+        const std::string val = e.value(in, 0, 0);
+        const std::string acc = "acc" + std::to_string(r);
+        src << "    {\n      if (" << region_test(reg[k.at.at(in)], L) << ") {\n" << e.code
+            << "      " << acc << " = " << combine(n.sarg, acc, val) << ";\n      }";
+        if (!region_is_all(reg[k.at.at(in)], L))
+          src << " else {\n      " << acc << " = "
+              << combine(n.sarg, acc, std::string("(") + ctype(n.type) + ")0") << ";\n      }";
+        src << "\n    }\n";
+      }
+      src << "  }\n";
+      if (!sp.reduces.empty()) {
+        // per-block fixed tree, partials, then the last block in block order
+        for (size_t r = 0; r < sp.reduces.size(); ++r) {
+          const Node &n = k.node(sp.reduces[r]);
+          const std::string T = ctype(n.type), acc = "acc" + std::to_string(r);
+          const std::string sh = "sh" + std::to_string(r);
+          src << "  {\n    __shared__ " << T << " " << sh << "[256];\n"
+              << "    " << sh << "[threadIdx.x] = " << acc << ";\n    __syncthreads();\n"
+              << "    for (int w = 128; w > 0; w >>= 1) {\n"
+              << "      if ((int)threadIdx.x < w) " << sh << "[threadIdx.x] = "
+              << combine(n.sarg, sh + "[threadIdx.x]", sh + "[threadIdx.x + w]") << ";\n"
+              << "      __syncthreads();\n    }\n"
+              << "    if (threadIdx.x == 0) ((" << T << " *)(part + " << r
+              << " * 8 * gridDim.x))[blockIdx.x] = " << sh << "[0];\n  }\n";
+        }
+        src << "  __shared__ bool last;\n  __threadfence();\n  __syncthreads();\n"
+            << "  if (threadIdx.x == 0) last = atomicAdd(done, 1u) == gridDim.x - 1;\n"
+            << "  __syncthreads();\n"
+            << "  if (!last || threadIdx.x != 0) return;\n  __threadfence();\n";
+        for (size_t r = 0; r < sp.reduces.size(); ++r) {
+          const Node &n = k.node(sp.reduces[r]);
+          const std::string T = ctype(n.type);
+          src << "  {\n    const volatile " << T << " *p = (const volatile " << T
+              << " *)(part + " << r << " * 8 * gridDim.x);\n"
+              << "    " << T << " a = p[0];\n"
+              << "    for (unsigned int b = 1; b < gridDim.x; ++b) a = "
+              << combine(n.sarg, "a", "p[b]") << ";\n"
+              << "    *(" << T << " *)(slots + " << 8 * slots.at(sp.reduces[r]) << ") = a;\n"
+              << "  }\n";
+        }
+        src << "  *done = 0;\n";
+      }
+      src << "}\n\n";
+    }
+    // scalar stores: one thread evaluates every stored value, then writes
+    kp.commit_fn = "om_k" + std::to_string(ki) + "_commit";
+    {
+      src << "extern \"C\" __global__ void " << kp.commit_fn
+          << "(OMPtrs P, unsigned char *SC, unsigned char *slots) {\n"
+          << "  if (threadIdx.x != 0 || blockIdx.x != 0) return;\n"
+          << "  const int c0 = 0, c1 = 0; (void)c0; (void)c1; (void)P;\n";
+      Emitter e(g, k, L, slots);
+      std::vector<std::string> vals;
+      for (int s : kp.scalar_stores) vals.push_back(e.value(k.stores[s].node, 0, 0));
+      src << e.code;
+      for (size_t i = 0; i < kp.scalar_stores.size(); ++i) {
+        const StaticDef &sd = g.statics[k.stores[kp.scalar_stores[i]].stat];
+        if (sd.type == TBool)
+          src << "  *(int *)(SC + " << sd.offset << ") = " << vals[i] << " ? 1 : 0;\n";
+        else
+          src << "  *(" << ctype(sd.type) << " *)(SC + " << sd.offset << ") = " << vals[i]
+              << ";\n";
+      }
+      src << "}\n\n";
+    }
+    plans->push_back(kp);
+  }
+  *nslots = slot;
+  return src.str();
+}
+
+// ---------------------------------------------------------------------------
+// the handle kind
+// ---------------------------------------------------------------------------
+
+struct GraphState {
+  Graph g;
+  Layout L;
+  std::vector<KernelPlan> plans;
+  cudaLibrary_t lib = nullptr;
+  std::vector<std::vector<cudaKernel_t>> stage_k;
+  std::vector<cudaKernel_t> commit_k;
+  unsigned char *slots = nullptr;  // 8 bytes per reduce
+  unsigned char *part = nullptr;   // per reduce of a stage: 8 bytes per block
+  unsigned int *done = nullptr;    // one counter per (kernel, stage)
+  std::vector<std::vector<int>> done_index;
+  int grid = 1;
+  std::string source;
+  bool owned = false;  // freed with the handle once setup has started
+};
+
+static GraphState *gst(Handle *h) { return (GraphState *)h->impl; }
+
+static void graph_free(Handle *h) {
+  GraphState *st = gst(h);
+  if (!st) return;
+  if (st->lib) cudaLibraryUnload(st->lib);
+  cudaFree(st->slots);
+  cudaFree(st->part);
+  cudaFree(st->done);
+  delete st;
+  h->impl = nullptr;
+}
+
+struct OMPtrs {
+  const void *cur[32];
+  void *nxt[32];
+};
+
+static om_status graph_run(Handle *h, int n) {
+  GraphState *st = gst(h);
+  const int ki = h->current_kernel;
+  const KernelPlan &kp = st->plans[ki];
+  for (int rep = 0; rep < n; ++rep) {
+    OMPtrs P;
+    std::memset(&P, 0, sizeof P);
+    for (size_t a = 0; a < h->arrays.size(); ++a) {
+      P.cur[a] = h->arrays[a].d();
+      P.nxt[a] = h->arrays[a].d_next();
+    }
+    unsigned char *SC = (unsigned char *)h->d_scalars;
+    for (size_t s = 0; s < kp.stages.size(); ++s) {
+      unsigned int *done = st->done + st->done_index[ki][s];
+      void *args[] = {&P, &SC, &st->slots, &st->part, &done};
+      OM_CUDA_CHECK(cudaLaunchKernel((const void *)st->stage_k[ki][s], dim3(st->grid), dim3(256),
+                                     args, 0, h->stream));
+      h->launches++;
+    }
+    if (!kp.scalar_stores.empty()) {
+      void *args[] = {&P, &SC, &st->slots};
+      OM_CUDA_CHECK(cudaLaunchKernel((const void *)st->commit_k[ki], dim3(1), dim3(32), args, 0,
+                                     h->stream));
+      h->launches++;
+    }
+    for (int s : kp.stored_arrays) {
+      int a = 0;
+      for (int i = 0; i < s; ++i) a += st->g.statics[i].array ? 1 : 0;
+      h->arrays[a].swap();
+    }
+  }
+  return OM_OK;
+}
+
+// NVRTC: the generated source to a cubin for sm_<major><minor>a
+static om_status nvrtc_cubin(const std::string &source, int major, int minor,
+                             std::vector<char> *cubin) {
+  nvrtcProgram prog;
+  if (nvrtcCreateProgram(&prog, source.c_str(), "omgraph.cu", 0, nullptr, nullptr) !=
+      NVRTC_SUCCESS) {
+    set_error("om_create_graph: nvrtcCreateProgram failed");
+    return OM_ERR_CUDA;
+  }
+  const std::string arch =
+      "--gpu-architecture=sm_" + std::to_string(major) + std::to_string(minor) + "a";
+  const char *opts[] = {arch.c_str(), "--fmad=false", "--std=c++17"};
+  const nvrtcResult r = nvrtcCompileProgram(prog, 3, opts);
+  if (r != NVRTC_SUCCESS) {
+    size_t n = 0;
+    nvrtcGetProgramLogSize(prog, &n);
+    std::string log(n, '\0');
+    nvrtcGetProgramLog(prog, &log[0]);
+    nvrtcDestroyProgram(&prog);
+    set_error("om_create_graph: NVRTC: " + std::string(nvrtcGetErrorString(r)) + "\n" + log);
+    return OM_ERR_CUDA;
+  }
+  size_t bytes = 0;
+  nvrtcGetCUBINSize(prog, &bytes);
+  cubin->resize(bytes);
+  nvrtcGetCUBIN(prog, cubin->data());
+  nvrtcDestroyProgram(&prog);
+  return OM_OK;
+}
+
+static om_status compile(GraphState *st, int device) {
+  int major = 0, minor = 0;
+  OM_CUDA_CHECK(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device));
+  OM_CUDA_CHECK(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, device));
+  std::vector<char> cubin;
+  OM_TRY(nvrtc_cubin(st->source, major, minor, &cubin));
+  OM_CUDA_CHECK(cudaLibraryLoadData(&st->lib, cubin.data(), nullptr, nullptr, 0, nullptr,
+                                    nullptr, 0));
+  st->stage_k.resize(st->plans.size());
+  st->commit_k.resize(st->plans.size());
+  for (size_t k = 0; k < st->plans.size(); ++k) {
+    for (const StagePlan &sp : st->plans[k].stages) {
+      cudaKernel_t f;
+      OM_CUDA_CHECK(cudaLibraryGetKernel(&f, st->lib, sp.fn.c_str()));
+      st->stage_k[k].push_back(f);
+    }
+    OM_CUDA_CHECK(cudaLibraryGetKernel(&st->commit_k[k], st->lib, st->plans[k].commit_fn.c_str()));
+  }
+  return OM_OK;
+}
+
+// Margins (the intersection of every array store's region on open axes),
+// the memory layout, scalar offsets, the plans and the CUDA source: all
+// host-side, no device needed.
+static om_status plan(GraphState *st, int *nslots) {
+  Graph &g = st->g;
+  Layout &L = st->L;
+  L.open = g.open;
+  Region united;
+  for (const KernelDef &k : g.kernels) {
+    const std::vector<Region> reg = regions(k);
+    for (const Store &s : k.stores)
+      if (g.statics[s.stat].array) united = meet(united, reg[k.at.at(s.node)]);
+  }
+  for (int d = 0; d < 2; ++d) {
+    const bool axis_open = g.open && d < g.ndim;
+    const int lo = (!axis_open || united.ax[d].lo_inf) ? 0 : united.ax[d].lo;
+    const int hi = (!axis_open || united.ax[d].hi_inf) ? 0 : -united.ax[d].hi;
+    if (lo < 0 || hi < 0) {
+      set_error("om_create_graph: negative margin (a store reaches beyond the array)");
+      return OM_ERR_ARG;
+    }
+    L.lm[d] = lo;
+    L.size[d] = g.size[d];
+    L.ms[d] = g.size[d] + lo + hi;
+  }
+  int narrays = 0;
+  size_t off = 0;
+  for (StaticDef &s : g.statics) {
+    if (s.array) {
+      if (++narrays > 32) {
+        set_error("om_create_graph: at most 32 array statics");
+        return OM_ERR_UNSUPPORTED;
+      }
+    } else {
+      s.offset = off;
+      off += 8;
+    }
+  }
+  std::map<std::pair<int, int>, int> slot_map;
+  st->plans.clear();
+  st->source = generate(g, L, &st->plans, &slot_map, nslots);
+  return OM_OK;
+}
+
+static om_status graph_setup(Handle *h, void *ctx) {
+  GraphState *st = (GraphState *)ctx;
+  st->owned = true;
+  h->impl = st;
+  h->impl_free = graph_free;
+  Graph &g = st->g;
+  const Layout &L = st->L;
+  int nslots = 0;
+  OM_TRY(plan(st, &nslots));
+  for (int d = 0; d < 2; ++d) {
+    h->lower_margin[d] = L.lm[d];
+    h->upper_margin[d] = L.ms[d] - L.size[d] - L.lm[d];
+  }
+  size_t scalar_end = 8;
+  for (StaticDef &s : g.statics) {
+    if (s.array) {
+      OM_TRY(alloc_array(h, s.name.c_str(), tsize(s.type)));
+    } else {
+      h->scalars.push_back(
+          {s.name, s.type == TDouble ? kDouble : (s.type == TFloat ? kFloat : kInt), s.offset});
+      scalar_end = std::max(scalar_end, s.offset + 8);
+    }
+  }
+  h->scalar_bytes = scalar_end;
+  for (const KernelDef &k : g.kernels) h->kernels.push_back({k.name, graph_run});
+  const long long cells = (long long)L.ms[0] * L.ms[1];
+  st->grid = (int)std::max<long long>(
+      1, std::min<long long>((cells + 255) / 256, 8LL * sm_count(h->device)));
+  int maxred = 1, nstages = 0;
+  st->done_index.resize(st->plans.size());
+  for (size_t k = 0; k < st->plans.size(); ++k)
+    for (const StagePlan &sp : st->plans[k].stages) {
+      maxred = std::max(maxred, (int)sp.reduces.size());
+      st->done_index[k].push_back(nstages++);
+    }
+  if (cudaMalloc(&st->slots, 8 * (size_t)std::max(nslots, 1)) != cudaSuccess ||
+      cudaMalloc(&st->part, 8 * (size_t)maxred * st->grid) != cudaSuccess ||
+      cudaMalloc(&st->done, sizeof(unsigned int) * std::max(nstages, 1)) != cudaSuccess ||
+      cudaMemset(st->done, 0, sizeof(unsigned int) * std::max(nstages, 1)) != cudaSuccess ||
+      cudaMemset(st->slots, 0, 8 * (size_t)std::max(nslots, 1)) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("om_create_graph: allocation failed");
+    return OM_ERR_NOMEM;
+  }
+  return compile(st, h->device);
+}
+
+}  // namespace og
+}  // namespace om
+
+using namespace om;
+
+extern "C" om_status om_create_graph(const char *text, const om_config *cfg, om_handle *out) {
+  if (!text || !out) {
+    set_error("om_create_graph: null argument");
+    return OM_ERR_ARG;
+  }
+  *out = nullptr;
+  og::GraphState *st = new og::GraphState();
+  om_status s = og::parse(text, &st->g);
+  if (s != OM_OK) {
+    delete st;
+    return s;
+  }
+  om_config c;
+  if (cfg) c = *cfg; else om_config_default(&c);
+  c.boundary = st->g.open ? OM_BOUNDARY_OPEN : OM_BOUNDARY_CYCLIC;
+  const int sizes[2] = {st->g.size[0], st->g.size[1]};
+  struct Setup {
+    static om_status run(Handle *h, void *ctx) { return og::graph_setup(h, ctx); }
+  };
+  s = create_handle(OM_KIND_GRAPH, sizes, c, Setup::run, st, out);
+  // once setup has run, the handle owns st (and destroyed it on failure)
+  if (s != OM_OK && !st->owned) delete st;
+  return s;
+}
+
+// Parse, plan, generate and compile a graph for sm_<major><minor>a without a
+// device; *source (valid until the next call on this thread) receives the
+// generated CUDA source.
+extern "C" om_status om_graph_check(const char *text, int major, int minor,
+                                    const char **source) {
+  static thread_local std::string keep;
+  if (!text) {
+    set_error("om_graph_check: null graph");
+    return OM_ERR_ARG;
+  }
+  og::GraphState st;
+  OM_TRY(og::parse(text, &st.g));
+  int nslots = 0;
+  OM_TRY(og::plan(&st, &nslots));
+  keep = st.source;
+  if (source) *source = keep.c_str();
+  std::vector<char> cubin;
+  return og::nvrtc_cubin(st.source, major, minor, &cubin);
+}
+
+extern "C" om_status om_graph_source(om_handle H, const char **source) {
+  Handle *h = handle_of(H);
+  if (!h || h->kind != OM_KIND_GRAPH || !source) {
+    set_error("om_graph_source: needs a graph handle");
+    return OM_ERR_ARG;
+  }
+  *source = og::gst(h)->source.c_str();
+  return OM_OK;
+}

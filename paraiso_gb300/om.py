@@ -21,6 +21,7 @@ LIB_PATH = os.path.join(HERE, "libom_gb300.so")
 OM_OK = 0
 KIND_LIFE = 1
 KIND_HYDRO = 2
+KIND_GRAPH = 3
 CYCLIC = 0
 OPEN = 1
 
@@ -41,7 +42,8 @@ EXPORTS = [
     "om_ensemble_scalar", "om_ensemble_set_scalar", "om_ensemble_totals",
     "om_ensemble_last_launch_count", "om_life_proceed_noalloc", "om_autotune",
     "om_autotune_ensemble", "om_hydro_vjp", "om_hydro_adjoint_run", "om_hydro_time_vjp",
-    "om_hydro_forward", "om_hydro_backward", "om_hydro_tape_free",
+    "om_hydro_forward", "om_hydro_backward", "om_hydro_tape_free", "om_create_graph",
+    "om_graph_source", "om_graph_check",
 ]
 
 
@@ -120,6 +122,9 @@ def load_library(path: str | None = None) -> C.CDLL:
         "om_hydro_forward": (i, [vp, i, i, C.POINTER(vp)]),
         "om_hydro_backward": (i, [vp, vp, C.POINTER(vp), C.POINTER(vp)]),
         "om_hydro_tape_free": (i, [vp]),
+        "om_create_graph": (i, [C.c_char_p, vp, C.POINTER(vp)]),
+        "om_graph_source": (i, [vp, C.POINTER(C.c_char_p)]),
+        "om_graph_check": (i, [C.c_char_p, i, i, C.POINTER(C.c_char_p)]),
         "om_profile_query": (i, [vp, C.c_char_p, C.POINTER(C.c_long), C.POINTER(C.c_double),
                                  C.POINTER(C.c_double)]),
     }
@@ -244,7 +249,7 @@ class OrthotopeMachine:
         p = C.c_void_p()
         t = C.c_int()
         _check(self._L.om_scalar_ptr(self._h, name.encode(), C.byref(p), C.byref(t)))
-        ctype = C.c_int32 if t.value == 0 else C.c_double
+        ctype = {0: C.c_int32, 1: C.c_double, 2: C.c_float}[t.value]
         return C.cast(p, C.POINTER(ctype))
 
     def get_scalar(self, name: str):
@@ -436,6 +441,41 @@ def ensemble_sizes(count: int, seed: int, lo: int = 256, hi: int = 2048, step: i
         h1 = mix(mix(seed) + (2 * k + 1) * 0x9E3779B97F4A7C15)
         out.append((lo + step * (h0 % m), lo + step * (h1 % m)))
     return out
+
+
+class GraphMachine(OrthotopeMachine):
+    """A general Orthotope Machine from a graph (paraiso_gb300.omgraph.OM or
+    its text), compiled into CUDA kernels for this GPU (om_create_graph).
+    Kernels run by name: ``m.run("calculate")``; statics through
+    ``read``/``write``/``array`` and ``get_scalar``/``set_scalar``.  A 1-D
+    machine has arrays of shape (1, n0 + margins)."""
+
+    kind = KIND_GRAPH
+    _NP = {"int": np.int32, "float": np.float32, "double": np.float64, "bool": np.bool_}
+
+    def __init__(self, graph, config: Config | None = None, **kw):
+        L = load_library()
+        self._L = L
+        text = graph.to_text() if hasattr(graph, "to_text") else str(graph)
+        cfg = config if config is not None else default_config(**kw)
+        h = C.c_void_p()
+        _check(L.om_create_graph(text.encode(), C.byref(cfg), C.byref(h)))
+        self._h = h
+        self.config = cfg
+        self._kid = {}
+        self.text = text
+        self.array_dtypes = {}
+        for line in text.splitlines():
+            w = line.split()
+            if w and w[0] == "static" and w[2] == "array":
+                self.array_dtypes[w[1]] = self._NP[w[3]]
+
+    @property
+    def source(self) -> str:
+        """The CUDA source generated for this machine."""
+        p = C.c_char_p()
+        _check(self._L.om_graph_source(self._h, C.byref(p)))
+        return p.value.decode()
 
 
 class HydroTape:

@@ -1,0 +1,105 @@
+"""General OM graphs on the CPU side: the builder's graphs, the numpy oracle
+against known answers of the reference's examples, and the generated CUDA
+compiled for sm_103a with NVRTC (no GPU needed)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle import omgraph_ref as R
+from paraiso_gb300 import omgraph as og
+from paraiso_gb300 import omgraph_examples as ex
+
+
+def run_oracle(om, kernels):
+    m = R.Machine(om.to_text())
+    for k in kernels:
+        m.run(k)
+    return m
+
+
+def test_builder_follows_the_haskell_builder():
+    om = og.OM("T", (4, 4), "cyclic")
+    a = om.static_array("a", og.Double)
+    k = om.kernel("k")
+    x = k.load(a)
+    k.store(a, (1 - x ** 3).pow_t(0.5))
+    text = om.to_text()
+    ops = [l.split()[1] for l in text.splitlines() if l[:1].isdigit()]
+    # x^3 = x * (x*x) (repeated squaring); 1 - ...; ** = exp (log _ * y)
+    assert ops == ["load", "mul", "mul", "imm", "sub", "log", "imm", "mul", "exp"]
+    with pytest.raises(og.OMGraphError):
+        k.store(a, k.load_index(0))          # int into double: needs a cast
+    with pytest.raises(og.OMGraphError):
+        x + k.load_size(0)                   # array + scalar: needs broadcast
+
+
+def test_shift_example_known_answers():
+    # examples/ShiftExample/main.cpp: init, increment, calculate on 8 cells.
+    # Open: margins 1 and 1; calculate writes cells 0..7 (memory 1..8),
+    # 10000*left + 100*center + right with table = index + 1; margins 0.
+    m = run_oracle(ex.shift_example("open"), ["init"])
+    assert (m.lm, m.um) == ([1], [1])
+    assert m.values["table"].ravel().tolist() == list(range(-1, 9))
+    m.run("increment")
+    assert m.values["table"].ravel().tolist() == list(range(0, 10))
+    m.run("calculate")
+    want = [0] + [10000 * (i - 1) + 100 * i + (i + 1) for i in range(1, 9)] + [0]
+    assert m.values["table"].ravel().tolist() == want
+    assert int(m.values["total"]) == sum(want) == 283644
+    # cyclic: no margins, neighbours wrap
+    m = run_oracle(ex.shift_example("cyclic"), ["init", "increment", "calculate"])
+    t = list(range(1, 9))
+    want = [10000 * t[(i - 1) % 8] + 100 * t[i] + t[(i + 1) % 8] for i in range(8)]
+    assert m.values["table"].ravel().tolist() == want
+    assert int(m.values["total"]) == 363636
+
+
+def test_hello_world_known_answer():
+    m = run_oracle(ex.hello_world(), ["create"])
+    assert int(m.values["total"]) == 45 * 190
+    y, x = np.mgrid[0:20, 0:10]
+    assert np.array_equal(m.values["table"], x * y)
+
+
+def test_life_graph_matches_life_oracle(oracle):
+    m = R.Machine(ex.life((40, 24)).to_text())
+    a = oracle.life_bernoulli(40, 24, 5, 0.35)
+    m.values["cell"] = a.copy()
+    for _ in range(12):
+        m.run("proceed")
+    ref, pops = oracle.life_run(a, 12, cyclic=True)
+    assert np.array_equal(m.values["cell"], ref)
+    assert int(m.values["population"]) == int(pops[-1])
+    assert int(m.values["generation"]) == 12
+
+
+def _check(om_lib, text):
+    L = om_lib.load_library()
+    src = C.c_char_p()
+    status = L.om_graph_check(text.encode(), 10, 3, C.byref(src))
+    return status, L.om_last_error().decode(), (src.value or b"").decode()
+
+
+@pytest.mark.parametrize("make", [
+    lambda: ex.hello_world(), lambda: ex.shift_example("open"),
+    lambda: ex.shift_example("cyclic"), lambda: ex.initial_condition((64, 48)),
+    lambda: ex.life(), lambda: ex.life((64, 64), "open")])
+def test_examples_compile_for_sm103a(om_lib, make):
+    status, err, src = _check(om_lib, make().to_text())
+    assert status == 0, err
+    assert "__global__" in src
+
+
+def test_graph_errors_are_reported(om_lib):
+    bad = [
+        "om T 3 4 4 4 cyclic\n",                                   # 3-D
+        "om T 1 8 cyclic\nkernel k\n0 load array int nope\nend\n",  # unknown static
+        "om T 1 8 cyclic\nstatic a array int\nkernel k\n0 frob array int\nend\n",
+        "om T 1 8 cyclic\nstatic a array int\nkernel k\n0 load array int a\n",  # no end
+        "om T 1 8 cyclic\nstatic a array double\nkernel k\n0 loadindex array int 0\n"
+        "store a 0\nend\n",                                        # type mismatch
+    ]
+    for text in bad:
+        status, err, _ = _check(om_lib, text)
+        assert status != 0 and "om_create_graph" in err, text

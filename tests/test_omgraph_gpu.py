@@ -1,0 +1,161 @@
+"""General OM graphs on the GPU (om_create_graph): the reference's examples
+and graphs that exercise every operation, against the numpy oracle of the
+same semantics (bit-exact; transcendental functions within a few ulp)."""
+import numpy as np
+import pytest
+
+from oracle import omgraph_ref as R
+from paraiso_gb300 import omgraph as og
+from paraiso_gb300 import omgraph_examples as ex
+
+pytestmark = pytest.mark.gpu
+
+
+def both(om_lib, om, kernels, init=None):
+    g = om_lib.GraphMachine(om)
+    m = R.Machine(om.to_text())
+    if init:
+        for name, a in init.items():
+            g.write(name, a)
+            m.values[name] = a.copy()
+    for k in kernels:
+        g.run(k)
+        m.run(k)
+    return g, m
+
+
+def assert_same(g, m, names, rtol=0.0):
+    for n in names:
+        realm = m.om["statics"][n][0]
+        got = g.read(n) if realm == "array" else g.get_scalar(n)
+        want = m.values[n]
+        if rtol == 0.0:
+            assert np.array_equal(np.asarray(got), np.asarray(want).astype(np.asarray(got).dtype)), n
+        else:
+            np.testing.assert_allclose(got, want, rtol=rtol, atol=rtol)
+
+
+@pytest.mark.parametrize("boundary", ["open", "cyclic"])
+def test_shift_example(om_lib, boundary):
+    g, m = both(om_lib, ex.shift_example(boundary), [])
+    assert g.om_lower_margin(0) == m.lm[0] and g.om_upper_margin(0) == m.um[0]
+    for k in ("init", "increment", "calculate"):
+        g.run(k)
+        m.run(k)
+        assert_same(g, m, ["table", "total"])
+    g.close()
+
+
+def test_hello_world(om_lib):
+    g, m = both(om_lib, ex.hello_world(), ["create"])
+    assert g.get_scalar("total") == 8550
+    assert_same(g, m, ["table", "total"])
+    g.close()
+
+
+def test_initial_condition(om_lib):
+    g, m = both(om_lib, ex.initial_condition(), ["create"])
+    got, want = g.read("table"), m.values["table"]
+    assert got.shape == (500, 500)
+    np.testing.assert_allclose(got, want, rtol=1e-13, atol=1e-13)
+    g.close()
+
+
+@pytest.mark.parametrize("size", [(256, 192), (37, 29)])
+def test_life_graph_matches_life_oracle(om_lib, oracle, size):
+    a = oracle.life_bernoulli(size[0], size[1], 7, 0.3)
+    g = om_lib.GraphMachine(ex.life(size))
+    g.write("cell", a)
+    g.run("proceed", 30)           # one captured CUDA graph of 30 steps
+    ref, pops = oracle.life_run(a, 30, cyclic=True)
+    assert np.array_equal(g.read("cell"), ref)
+    assert g.get_scalar("population") == int(pops[-1])
+    assert g.get_scalar("generation") == 30
+    for _ in range(3):             # single steps continue from there
+        g.run("proceed")
+    ref, pops = oracle.life_run(ref, 3, cyclic=True)
+    assert np.array_equal(g.read("cell"), ref) and g.get_scalar("generation") == 33
+    g.close()
+
+
+def test_life_graph_open(om_lib, oracle):
+    om = ex.life((64, 48), "open")
+    a = np.zeros((50, 66), np.int32)
+    a[1:-1, 1:-1] = oracle.life_bernoulli(64, 48, 3, 0.4)
+    g, m = both(om_lib, om, ["proceed"] * 5, init={"cell": a})
+    assert (g.om_lower_margin(0), g.om_upper_margin(1)) == (1, 1)
+    assert_same(g, m, ["cell", "population", "generation"])
+    g.close()
+
+
+def semantics_graph(boundary):
+    """Every operation of the format, several types, two reduce stages."""
+    om = og.OM("Sem", (61, 37), boundary)
+    f = om.static_array("f", og.Float)
+    d = om.static_array("d", og.Double)
+    i = om.static_array("i", og.Int)
+    b = om.static_array("b", og.Bool)
+    s_min = om.static_scalar("smin", og.Float)
+    s_max = om.static_scalar("smax", og.Double)
+    s_sum = om.static_scalar("ssum", og.Int)
+    s_flag = om.static_scalar("flag", og.Bool)
+    k = om.kernel("step")
+    fv, dv, iv = k.load(f), k.load(d), k.load(i)
+    x = k.load_index(0)
+    y = k.load_index(1)
+    # integer division and modulo of mixed signs (C truncation); divisors
+    # are never zero
+    den1 = og.select((y - 13).eq(0), 1, y - 13)
+    den2 = og.select((x - 17).eq(0), 1, x - 17)
+    k.store(i, (iv - 7 * x) // den1 + (iv * 3) % den2)
+    # float: shifts both ways, max/min order, abs, signum, inv, cast
+    fs = k.shift(fv, (1, -1)) - k.shift(fv, (-2, 0))
+    ff = og.max_(fs, fv) * 0.5 + og.min_(-fv, fs) + og.abs_(fs) * og.signum(fv)
+    ff = ff + og.cast(og.cast(fv * 10, og.Int), og.Float) + og.recip(og.abs_(fv) + 1)
+    k.store(f, ff)
+    # double: transcendental functions and pow
+    dd = og.sqrt(og.abs_(dv) + 1) + og.exp(-og.abs_(dv)) + og.log(og.abs_(dv) + 2)
+    dd = dd + og.sin(dv) * og.cos(dv) + og.atan2(dv, og.cast(x, og.Double) + 1)
+    dd = dd + og.pow_(og.abs_(dv) + 1, dv * 0.25) + og.tan(dv * 0.1) + og.atan(dv)
+    dd = dd + og.asin(og.sin(dv) * 0.5) + og.acos(og.cos(dv) * 0.5)
+    k.store(d, dd)
+    # bool logic
+    k.store(b, (k.load(b) & (fv > 0)) | ~(dv <= 0.5))
+    # reductions, including regions that exclude cells (open: zeros join)
+    k.store(s_min, k.reduce("min", fs))
+    k.store(s_max, k.reduce("max", dd))
+    k.store(s_sum, k.reduce("sum", og.cast(fs > 0, og.Int)))
+    # second stage: a reduce result broadcast back into an array
+    k2 = om.kernel("center")
+    fv2 = k2.load(f)
+    k2.store(f, fv2 - k2.broadcast(k2.reduce("sum", fv2) / k2.imm(61.0 * 37, og.Float, "scalar")))
+    k2.store(s_flag, k2.reduce("max", og.cast(k2.load(b), og.Int)).eq(k2.imm(1, og.Int, "scalar")))
+    return om
+
+
+@pytest.mark.parametrize("boundary", ["cyclic", "open"])
+def test_semantics_graph(om_lib, boundary):
+    om = semantics_graph(boundary)
+    m0 = R.Machine(om.to_text())
+    rng = np.random.default_rng(11)
+    shape = m0.shape
+    init = {"f": rng.standard_normal(shape).astype(np.float32),
+            "d": rng.standard_normal(shape),
+            "i": rng.integers(-1000, 1000, shape).astype(np.int32),
+            "b": rng.random(shape) < 0.5}
+    g, m = both(om_lib, om, ["step", "step"], init=init)
+    assert_same(g, m, ["i", "b", "smin", "ssum"])
+    assert_same(g, m, ["f"])                      # + - * / max min abs cast: exact
+    assert_same(g, m, ["d", "smax"], rtol=1e-12)  # transcendental: a few ulp
+    g.run("center")
+    m.run("center")
+    np.testing.assert_allclose(g.read("f"), m.values["f"], rtol=1e-6, atol=1e-6)
+    assert g.get_scalar("flag") == int(m.values["flag"])
+    g.close()
+
+
+def test_generated_source_is_available(om_lib):
+    g = om_lib.GraphMachine(ex.hello_world())
+    src = g.source
+    assert "om_k0_s0" in src and "__global__" in src
+    g.close()

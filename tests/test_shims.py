@@ -72,3 +72,47 @@ def test_shim_driver_hydro_open_default(om_lib, oracle, tmp_path):
     assert abs(float(vals["time"]) - t) <= 1e-12 * t
     assert abs(float(vals["mass"]) - rho.sum()) <= 1e-12 * rho.sum()
     assert abs(float(vals["px"]) - (rho * vx).sum()) <= 1e-9 * abs(rho * vx).sum()
+
+
+def emit(tmp_path, om, sub=""):
+    from paraiso_gb300 import omgraph as og
+    d = tmp_path / sub if sub else tmp_path
+    d.mkdir(parents=True, exist_ok=True)
+    (d / f"{om.name}.hpp").write_text(og.emit_header(om))
+
+
+@pytest.mark.skipif(not os.path.isdir(REFERENCE_TREE), reason="reference tree not present")
+@pytest.mark.parametrize("driver,make,sub", [
+    ("examples/ShiftExample/main.cpp", "shift_example", ""),
+    ("examples/HelloWorld/main.cpp", "hello_world", "dist"),
+    ("examples/InitialCondition/main.cpp", "initial_condition", "dist")])
+def test_reference_graph_drivers_compile_unchanged(om_lib, tmp_path, driver, make, sub):
+    # the emitted class stands in for dist/TableMaker.hpp of the generator
+    from paraiso_gb300 import omgraph_examples as ex
+    emit(tmp_path, getattr(ex, make)(), sub)
+    cmd = ["g++", "-std=c++17", "-O1", os.path.join(REFERENCE_TREE, driver), f"-I{INC}",
+           f"-I{tmp_path}", f"-L{LIBDIR}", "-lom_gb300", f"-Wl,-rpath,{LIBDIR}",
+           "-o", str(tmp_path / "drv")]
+    subprocess.run(cmd, check=True)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("boundary", ["open", "cyclic"])
+def test_graph_driver_runs_shift_example(om_lib, tmp_path, boundary):
+    from oracle import omgraph_ref as R
+    from paraiso_gb300 import omgraph_examples as ex
+    om = ex.shift_example(boundary)
+    emit(tmp_path, om)
+    cmd = ["g++", "-std=c++17", "-O1", "-Wall", os.path.join(ROOT, "tests", "cpp",
+           "graph_driver.cpp"), f"-I{INC}", f"-I{tmp_path}", f"-L{LIBDIR}", "-lom_gb300",
+           f"-Wl,-rpath,{LIBDIR}", "-o", str(tmp_path / "gd")]
+    subprocess.run(cmd, check=True)
+    out = subprocess.run([str(tmp_path / "gd")], check=True, capture_output=True,
+                         text=True).stdout.strip().split("\n")
+    m = R.Machine(om.to_text())
+    want = []
+    for k in ("init", "increment", "calculate"):
+        m.run(k)
+        want.append("value: " + " ".join(str(v) for v in m.values["table"].ravel()))
+    want.append(f"total: {int(m.values['total'])}")
+    assert out == want
