@@ -246,6 +246,20 @@ om_status om_ensemble_last_launch_count(om_ensemble e, int *launches);
 om_status om_autotune_ensemble(int count, const int *sizes, const om_config *base,
                                om_config *best, double *best_rate);
 
+/* ---- checkpoints and snapshots (no counterpart: the generated class has
+ * no I/O; its drivers print through the accessors) ------------------------ */
+
+/* Binary checkpoint of every static (arrays, margins included, and
+ * scalars) with a header describing the handle's layout. */
+om_status om_save(om_handle h, const char *path);
+/* Restore a checkpoint into a handle of the same kind, mesh, margins and
+ * statics (OM_ERR_ARG and a reason otherwise). */
+om_status om_load(om_handle h, const char *path);
+/* Hydro: the text snapshot of examples/Hydro/main-kh.cpp:17-31, one line
+ * "x y density velocity0 velocity1 pressure" per interior cell (cell
+ * centres dR (i + 0.5)), a blank line after each row. */
+om_status om_hydro_write_snapshot(om_handle h, const char *path);
+
 /* ---- general OM graphs ---------------------------------------------------
  * The generator's input (Language/Paraiso/OM/Graph.hs:113-123: Load, Store,
  * Shift, Imm, Arith, Reduce, Broadcast, LoadIndex, LoadSize) as text, one

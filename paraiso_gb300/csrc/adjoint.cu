@@ -459,18 +459,14 @@ adj_stage2_tile(Fields<R> Q, Fields<R> U2b, FluxStore<R> F1, Fields<R> U1b, Fiel
 
 // E+F on one TX x TY tile: the face cotangents (left-state part 0..3,
 // right-state part 4..7) of x faces X0 .. X0+TX of each tile row and y faces
-// Y0 .. Y0+TY of each tile column, from the state and stage-1 cotangent box
-// of cells X0-1 .. X0+TX, Y0-1 .. Y0+TY; then per tile cell the
-// previous-state cotangent = base part + its own walls (right state) + the
-// next walls (left state), and the lowest index whose CFL timescale equals
-// the minimum (the arg-min that receives the dt cotangent; ties go to the
-// lowest index).
+// Y0 .. Y0+TY of each tile column, then per tile cell the previous-state
+// cotangent = base part + its own walls (right state) + the next walls
+// (left state), and the lowest index whose CFL timescale equals the minimum
+// (the arg-min that receives the dt cotangent; ties go to the lowest index).
 template <class R, int TX, int TY> struct Stage1Smem {
-  static constexpr int XF = TX + 1, YF = TY + 1, BX = TX + 2, BY = TY + 2;
+  static constexpr int XF = TX + 1, YF = TY + 1;
   R fx[8][TY][XF];
   R fy[8][YF][TX];
-  R p[4][BY][BX];
-  R u[4][BY][BX];
 };
 
 template <class R, int TX, int TY>
@@ -478,23 +474,12 @@ __global__ void __launch_bounds__(256, AdjOcc<R>::stage1)
 adj_stage1_tile(Fields<R> U1b, Fields<R> Pbase, Fields<R> Pb, Geo<R> G,
                 const unsigned long long *minbits, unsigned long long *argmin) {
   using S = Stage1Smem<R, TX, TY>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  S &s = *reinterpret_cast<S *>(smem_raw);
+  __shared__ S s;
   G.dt = (R)G.in->dt;
   const Fields<R> P = G.state();
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int nt0 = (G.n0 + TX - 1) / TX;
   const int X0 = (int)(blockIdx.x % nt0) * TX, Y0 = (int)(blockIdx.x / nt0) * TY;
-  for (int i = tid; i < S::BY * S::BX; i += nthr) {
-    const int by = i / S::BX, bx = i - by * S::BX;
-    const size_t gi = G.at(X0 - 1 + bx, Y0 - 1 + by);
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      s.p[c][by][bx] = P.f[c][gi];
-      s.u[c][by][bx] = U1b.f[c][gi];
-    }
-  }
-  __syncthreads();
   const R h = G.dt / R(2);
   const R d0 = h / G.dR0, d1 = h / G.dR1;
   constexpr int NXF = TY * S::XF, NYF = S::YF * TX;
@@ -502,33 +487,26 @@ adj_stage1_tile(Fields<R> U1b, Fields<R> Pbase, Fields<R> Pb, Geo<R> G,
     PrimBar<R> Lb, Rb;
     ha::zero(Lb);
     ha::zero(Rb);
+    int r, j;
     if (i < NXF) {
-      // x face X0+j of row Y0+r: cells at box (j, r+1) and (j+1, r+1)
-      const int r = i / S::XF, j = i - r * S::XF;
-      const int by = r + 1;
-      const Prim<R> L{s.p[0][by][j], s.p[1][by][j], s.p[2][by][j], s.p[3][by][j]};
-      const Prim<R> Rt{s.p[0][by][j + 1], s.p[1][by][j + 1], s.p[2][by][j + 1],
-                       s.p[3][by][j + 1]};
-      const Flux<R> fb{d0 * (s.u[0][by][j + 1] - s.u[0][by][j]),
-                       d0 * (s.u[1][by][j + 1] - s.u[1][by][j]),
-                       d0 * (s.u[2][by][j + 1] - s.u[2][by][j]),
-                       d0 * (s.u[3][by][j + 1] - s.u[3][by][j])};
-      ha::hllc_rev<0>(G.g, L, Rt, fb, Lb, Rb);
+      r = i / S::XF;
+      j = i - r * S::XF;
+      const size_t ic = G.at(X0 + j, Y0 + r), im = G.at(X0 + j - 1, Y0 + r);
+      const Prim<R> a = U1b.get(ic), c = U1b.get(im);
+      const Flux<R> fb{d0 * (a.rho - c.rho), d0 * (a.v0 - c.v0), d0 * (a.v1 - c.v1),
+                       d0 * (a.p - c.p)};
+      ha::hllc_rev<0>(G.g, P.get(im), P.get(ic), fb, Lb, Rb);
       s.fx[0][r][j] = Lb.rho; s.fx[1][r][j] = Lb.v0; s.fx[2][r][j] = Lb.v1; s.fx[3][r][j] = Lb.p;
       s.fx[4][r][j] = Rb.rho; s.fx[5][r][j] = Rb.v0; s.fx[6][r][j] = Rb.v1; s.fx[7][r][j] = Rb.p;
     } else {
-      // y face Y0+j of column X0+r: cells at box (r+1, j) and (r+1, j+1)
       const int i2 = i - NXF;
-      const int j = i2 / TX, r = i2 - j * TX;
-      const int bx = r + 1;
-      const Prim<R> L{s.p[0][j][bx], s.p[1][j][bx], s.p[2][j][bx], s.p[3][j][bx]};
-      const Prim<R> Rt{s.p[0][j + 1][bx], s.p[1][j + 1][bx], s.p[2][j + 1][bx],
-                       s.p[3][j + 1][bx]};
-      const Flux<R> fb{d1 * (s.u[0][j + 1][bx] - s.u[0][j][bx]),
-                       d1 * (s.u[1][j + 1][bx] - s.u[1][j][bx]),
-                       d1 * (s.u[2][j + 1][bx] - s.u[2][j][bx]),
-                       d1 * (s.u[3][j + 1][bx] - s.u[3][j][bx])};
-      ha::hllc_rev<1>(G.g, L, Rt, fb, Lb, Rb);
+      j = i2 / TX;
+      r = i2 - j * TX;
+      const size_t ic = G.at(X0 + r, Y0 + j), im = G.at(X0 + r, Y0 + j - 1);
+      const Prim<R> a = U1b.get(ic), c = U1b.get(im);
+      const Flux<R> fb{d1 * (a.rho - c.rho), d1 * (a.v0 - c.v0), d1 * (a.v1 - c.v1),
+                       d1 * (a.p - c.p)};
+      ha::hllc_rev<1>(G.g, P.get(im), P.get(ic), fb, Lb, Rb);
       s.fy[0][j][r] = Lb.rho; s.fy[1][j][r] = Lb.v0; s.fy[2][j][r] = Lb.v1; s.fy[3][j][r] = Lb.p;
       s.fy[4][j][r] = Rb.rho; s.fy[5][j][r] = Rb.v0; s.fy[6][j][r] = Rb.v1; s.fy[7][j][r] = Rb.p;
     }
@@ -541,9 +519,9 @@ adj_stage1_tile(Fields<R> U1b, Fields<R> Pbase, Fields<R> Pb, Geo<R> G,
     const int x = X0 + tx, y = Y0 + ty;
     if (x >= G.n0 || y >= G.n1) continue;
     const size_t gi = (size_t)y * G.n0 + x;
-    const R qr = s.p[0][ty + 1][tx + 1], qu = s.p[1][ty + 1][tx + 1],
-            qv = s.p[2][ty + 1][tx + 1], qp = s.p[3][ty + 1][tx + 1];
-    if (hk::ts_bits<R>(hs::timescale(G.g, G.dR0, G.dR1, qr, qu, qv, qp)) == mb && gi < best)
+    const Prim<R> q = P.get(gi);
+    if (hk::ts_bits<R>(hs::timescale(G.g, G.dR0, G.dR1, q.rho, q.v0, q.v1, q.p)) == mb &&
+        gi < best)
       best = gi;
     Prim<R> b = Pbase.get(gi);
     b.rho += s.fx[4][ty][tx] + s.fx[0][ty][tx + 1] + s.fy[4][ty][tx] + s.fy[0][ty + 1][tx];
@@ -644,10 +622,6 @@ template <class R> static cudaError_t allow_tile_smem() {
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)sizeof(FusedSmem<R, TX, TY>));
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(adj::adj_stage1_tile<R, TX, TY>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)sizeof(adj::Stage1Smem<R, TX, TY>));
-  if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(adj::adj_stage2_tile<R, TX, TY>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)sizeof(adj::Stage2Smem<R, TX, TY>));
@@ -746,8 +720,8 @@ static om_status vjp_kernels(Handle *h, AdjointScratch *s, void *const *ub, void
       U, Q, F1, U2b, Pbase, G, s->partials, s->argmin + 1);
   adj::adj_stage2_tile<R, TX, TY><<<nt, 256, sizeof(adj::Stage2Smem<R, TX, TY>), st>>>(
       Q, U2b, F1, U1b, Pbase, G, s->partials + nt);
-  adj::adj_stage1_tile<R, TX, TY><<<nt, 256, sizeof(adj::Stage1Smem<R, TX, TY>), st>>>(
-      U1b, Pbase, Pb, G, s->argmin + 1, s->argmin);
+  adj::adj_stage1_tile<R, TX, TY><<<nt, 256, 0, st>>>(U1b, Pbase, Pb, G, s->argmin + 1,
+                                                      s->argmin);
   adj::adj_dt<R><<<1, 1024, 0, st>>>(Pb, G, s->partials, 2 * nt, (R)cfl, s->argmin);
   OM_CUDA_CHECK(cudaGetLastError());
   return OM_OK;

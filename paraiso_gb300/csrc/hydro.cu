@@ -234,6 +234,10 @@ static void hydro_restore_key(Handle *h, uint64_t key) {
   if (st->ts_valid) ts_mark_current(h);
 }
 
+struct HydroCkState;
+static size_t hydro_save_state(Handle *h, void *out, size_t cap);
+static void hydro_load_state(Handle *h, const void *in, size_t n);
+
 static bool hydro_graph_ok(Handle *h, int kernel_id) {
   (void)kernel_id;
   return hst(h)->variant != 1;  // the plain path round-trips to the host
@@ -306,6 +310,28 @@ struct HydroCkState {
   double ts_dR0, ts_dR1, ts_ext1;
 };
 static_assert(sizeof(HydroCkState) <= 64, "checkpoint bookkeeping size");
+
+// the cached-minimum bookkeeping travels with om_save / om_load, so a
+// restart continues bit-identically (no re-reduction in another build)
+static size_t hydro_save_state(Handle *h, void *out, size_t cap) {
+  const HydroState *st = hst(h);
+  const HydroCkState k{st->ts_valid, st->slot, st->ts_dR0, st->ts_dR1, st->ts_ext1};
+  if (cap < sizeof k) return 0;
+  std::memcpy(out, &k, sizeof k);
+  return sizeof k;
+}
+
+static void hydro_load_state(Handle *h, const void *in, size_t n) {
+  if (n != sizeof(HydroCkState)) return;  // keep the invalidated cache
+  HydroCkState k;
+  std::memcpy(&k, in, sizeof k);
+  HydroState *st = hst(h);
+  st->ts_valid = k.ts_valid;
+  st->slot = k.slot;
+  st->ts_dR0 = k.ts_dR0;
+  st->ts_dR1 = k.ts_dR1;
+  st->ts_ext1 = k.ts_ext1;
+}
 
 om_status hydro_checkpoint_alloc(Handle *h, HydroCheckpoint *c) {
   const size_t bytes = h->memory_size_total() * h->arrays[0].elem_size;
@@ -396,6 +422,8 @@ om_status hydro_setup(Handle *h) {
   h->ops.array_written = hydro_array_written;
   h->ops.reserve = hydro_reserve;
   h->ops.graph_ok = hydro_graph_ok;
+  h->ops.save_state = hydro_save_state;
+  h->ops.load_state = hydro_load_state;
   const int es = st->fp64 ? 8 : 4;
   OM_TRY(alloc_array(h, "density", es));
   OM_TRY(alloc_array(h, "velocity0", es));

@@ -78,6 +78,10 @@ struct KindOps {
   om_status (*reserve)(Handle *, int kernel_id, int n) = nullptr;
   // false when a kernel synchronises with the host mid-run (no graph capture)
   bool (*graph_ok)(Handle *, int kernel_id) = nullptr;
+  // host-side state a checkpoint carries besides the statics (bytes written
+  // into out, at most cap; returns the size), and its restoration
+  size_t (*save_state)(Handle *, void *out, size_t cap) = nullptr;
+  void (*load_state)(Handle *, const void *in, size_t n) = nullptr;
 };
 
 struct Kernel {

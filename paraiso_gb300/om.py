@@ -43,7 +43,7 @@ EXPORTS = [
     "om_ensemble_last_launch_count", "om_life_proceed_noalloc", "om_autotune",
     "om_autotune_ensemble", "om_hydro_vjp", "om_hydro_adjoint_run", "om_hydro_time_vjp",
     "om_hydro_forward", "om_hydro_backward", "om_hydro_tape_free", "om_create_graph",
-    "om_graph_source", "om_graph_check",
+    "om_graph_source", "om_graph_check", "om_save", "om_load", "om_hydro_write_snapshot",
 ]
 
 
@@ -125,6 +125,9 @@ def load_library(path: str | None = None) -> C.CDLL:
         "om_create_graph": (i, [C.c_char_p, vp, C.POINTER(vp)]),
         "om_graph_source": (i, [vp, C.POINTER(C.c_char_p)]),
         "om_graph_check": (i, [C.c_char_p, i, i, C.POINTER(C.c_char_p)]),
+        "om_save": (i, [vp, C.c_char_p]),
+        "om_load": (i, [vp, C.c_char_p]),
+        "om_hydro_write_snapshot": (i, [vp, C.c_char_p]),
         "om_profile_query": (i, [vp, C.c_char_p, C.POINTER(C.c_long), C.POINTER(C.c_double),
                                  C.POINTER(C.c_double)]),
     }
@@ -288,6 +291,14 @@ class OrthotopeMachine:
     def read_to_pointer(self, name: str, ptr: int, nbytes: int) -> None:
         _check(self._L.om_array_read(self._h, name.encode(), C.c_void_p(ptr), nbytes))
 
+    def save(self, path) -> None:
+        """Binary checkpoint of every static (om_save)."""
+        _check(self._L.om_save(self._h, str(path).encode()))
+
+    def load(self, path) -> None:
+        """Restore a checkpoint written by save (om_load)."""
+        _check(self._L.om_load(self._h, str(path).encode()))
+
     def device_pointer(self, name: str) -> int:
         p = C.c_void_p()
         _check(self._L.om_array_device(self._h, name.encode(), C.byref(p)))
@@ -347,6 +358,10 @@ class Hydro(OrthotopeMachine):
 
     def proceed(self, n: int = 1) -> None:
         self.run("proceed", n)
+
+    def write_snapshot(self, path) -> None:
+        """The text snapshot of examples/Hydro/main-kh.cpp (om_hydro_write_snapshot)."""
+        _check(self._L.om_hydro_write_snapshot(self._h, str(path).encode()))
 
     def init_kh(self, seed: int) -> None:
         _check(self._L.om_hydro_init_kh(self._h, C.c_uint64(seed)))

@@ -29,6 +29,8 @@ def assert_same(g, m, names, rtol=0.0):
         realm = m.om["statics"][n][0]
         got = g.read(n) if realm == "array" else g.get_scalar(n)
         want = m.values[n]
+        if realm == "array":          # a 1-D machine reads back as (1, n)
+            want = np.asarray(want).reshape(np.shape(got))
         if rtol == 0.0:
             assert np.array_equal(np.asarray(got), np.asarray(want).astype(np.asarray(got).dtype)), n
         else:
