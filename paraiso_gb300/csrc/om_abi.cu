@@ -6,6 +6,7 @@
 // per OM (Language/Paraiso/Generator/PlanTrans.hs:51-277) together with its
 // host/device container (PlanTrans.hs:724-728).
 #include <cuda_runtime.h>
+#include <cstdlib>
 
 #include <cstdio>
 #include <cstring>
@@ -47,12 +48,36 @@ Scalar *Handle::find_scalar(const char *n) {
   return nullptr;
 }
 
+// Fault injection for tests, on the host: with OM_FAIL_ALLOC_AFTER=n in the
+// environment, array allocations after the first n (counted from when the
+// variable took its current value) report failure without calling the
+// allocator, so every caller's OM_ERR_NOMEM path can be exercised.
+static bool injected_alloc_failure() {
+  static std::mutex mu;
+  static std::string seen;
+  static long count = 0;
+  const char *e = std::getenv("OM_FAIL_ALLOC_AFTER");
+  std::lock_guard<std::mutex> lock(mu);
+  const std::string now = e ? e : "";
+  if (now != seen) {
+    seen = now;
+    count = 0;
+  }
+  if (now.empty()) return false;
+  return count++ >= std::atol(now.c_str());
+}
+
 om_status alloc_array(Handle *h, const char *name, int elem_size) {
   Array a;
   a.name = name;
   a.elem_size = elem_size;
   a.count = h->memory_size_total();
   const size_t bytes = a.count * (size_t)elem_size;
+  if (injected_alloc_failure()) {
+    set_error(std::string("cudaMalloc failed for array ") + name + " (injected by "
+              "OM_FAIL_ALLOC_AFTER)");
+    return OM_ERR_NOMEM;
+  }
   for (int b = 0; b < 2; ++b) {
     if (cudaMalloc(&a.dev[b], bytes) != cudaSuccess) {
       cudaGetLastError();

@@ -410,8 +410,11 @@ class Emitter {
   std::string wrap(const std::string &c, int o, int n) const {
     if (o == 0) return c;
     const std::string x = "(" + c + " + (" + std::to_string(o) + "))";
-    return "((" + x + " % " + std::to_string(n) + " + " + std::to_string(n) + ") % " +
-           std::to_string(n) + ")";
+    const std::string N = std::to_string(n);
+    if (o > -n && o < n)  // one add or subtract brings it back
+      return "(" + x + (o < 0 ? " < 0 ? " + x + " + " + N : " >= " + N + " ? " + x + " - " + N) +
+             " : " + x + ")";
+    return "((" + x + " % " + N + " + " + N + ") % " + N + ")";
   }
 
   std::string addr(int o0, int o1) const {
@@ -592,30 +595,58 @@ static std::string generate(const Graph &g, const Layout &L, std::vector<KernelP
           << "    const int c0 = (int)(i % " << L.ms[0] << "), c1 = (int)(i / " << L.ms[0]
           << ");\n"
           << "    (void)c0; (void)c1;\n";
-      for (int s : sp.stores) {
-        const Store &so = k.stores[s];
-        const Node &v = k.node(so.node);
-        const std::string T = ctype(v.type);
+      // one evaluation block for the whole stage when every store and reduce
+      // of it has the same region (always so on a cyclic mesh): the values
+      // they share are computed once per cell
+      std::vector<std::string> tests;
+      for (int s : sp.stores) tests.push_back(region_test(reg[k.at.at(k.stores[s].node)], L));
+      for (int id : sp.reduces) tests.push_back(region_test(reg[k.at.at(k.node(id).args[0])], L));
+      bool one_region = !tests.empty();
+      for (const std::string &t : tests) one_region = one_region && t == tests[0];
+      bool all_cells = true;
+      for (int id : sp.reduces) all_cells = all_cells && region_is_all(reg[k.at.at(k.node(id).args[0])], L);
+      if (one_region && all_cells && tests[0] == "true") {
         Emitter e(g, k, L, slots);
-        const std::string val = e.value(so.node, 0, 0);
-        src << "    {\n      " << T << " out = (" << T << ")0;\n"
-            << "      if (" << region_test(reg[k.at.at(so.node)], L) << ") {\n"
-            << e.code << "      out = " << val << ";\n      }\n"
-            << "      ((" << T << " *)P.nxt[" << em.array_index(so.stat) << "])[i] = out;\n"
-            << "    }\n";
-      }
-      for (size_t r = 0; r < sp.reduces.size(); ++r) {
-        const Node &n = k.node(sp.reduces[r]);
-        const int in = n.args[0];
-        Emitter e(g, k, L, slots);
-        const std::string val = e.value(in, 0, 0);
-        const std::string acc = "acc" + std::to_string(r);
-        src << "    {\n      if (" << region_test(reg[k.at.at(in)], L) << ") {\n" << e.code
-            << "      " << acc << " = " << combine(n.sarg, acc, val) << ";\n      }";
-        if (!region_is_all(reg[k.at.at(in)], L))
-          src << " else {\n      " << acc << " = "
-              << combine(n.sarg, acc, std::string("(") + ctype(n.type) + ")0") << ";\n      }";
-        src << "\n    }\n";
+        std::vector<std::string> vals;
+        for (int s : sp.stores) vals.push_back(e.value(k.stores[s].node, 0, 0));
+        for (int id : sp.reduces) vals.push_back(e.value(k.node(id).args[0], 0, 0));
+        src << "    {\n" << e.code;
+        size_t v = 0;
+        for (int s : sp.stores)
+          src << "      ((" << ctype(k.node(k.stores[s].node).type) << " *)P.nxt["
+              << em.array_index(k.stores[s].stat) << "])[i] = " << vals[v++] << ";\n";
+        for (size_t r = 0; r < sp.reduces.size(); ++r) {
+          const std::string acc = "acc" + std::to_string(r);
+          src << "      " << acc << " = " << combine(k.node(sp.reduces[r]).sarg, acc, vals[v++])
+              << ";\n";
+        }
+        src << "    }\n";
+      } else {
+        for (int s : sp.stores) {
+          const Store &so = k.stores[s];
+          const Node &v = k.node(so.node);
+          const std::string T = ctype(v.type);
+          Emitter e(g, k, L, slots);
+          const std::string val = e.value(so.node, 0, 0);
+          src << "    {\n      " << T << " out = (" << T << ")0;\n"
+              << "      if (" << region_test(reg[k.at.at(so.node)], L) << ") {\n"
+              << e.code << "      out = " << val << ";\n      }\n"
+              << "      ((" << T << " *)P.nxt[" << em.array_index(so.stat) << "])[i] = out;\n"
+              << "    }\n";
+        }
+        for (size_t r = 0; r < sp.reduces.size(); ++r) {
+          const Node &n = k.node(sp.reduces[r]);
+          const int in = n.args[0];
+          Emitter e(g, k, L, slots);
+          const std::string val = e.value(in, 0, 0);
+          const std::string acc = "acc" + std::to_string(r);
+          src << "    {\n      if (" << region_test(reg[k.at.at(in)], L) << ") {\n" << e.code
+              << "      " << acc << " = " << combine(n.sarg, acc, val) << ";\n      }";
+          if (!region_is_all(reg[k.at.at(in)], L))
+            src << " else {\n      " << acc << " = "
+                << combine(n.sarg, acc, std::string("(") + ctype(n.type) + ")0") << ";\n      }";
+          src << "\n    }\n";
+        }
       }
       src << "  }\n";
       if (!sp.reduces.empty()) {
