@@ -544,7 +544,8 @@ def adjoint_workload(args, dist: Dist) -> dict:
     # forward step and adjoint step, device time on the handle's stream
     h.proceed(max(args.warmup, 1))
     fwd_ms = h.time_run("proceed", 20) / 20
-    vjp_ms = h.time_vjp(10)
+    vjp_ms = h.time_vjp(10)      # reverse sweep of one step from its tape
+    tape_ms = h.time_tape(10)    # the taped forward step of the recompute
     # the full gradient: forward with sqrt(T) checkpoints, recompute, backward
     h.set_state(st0)
     h.set_scalar("time", 0.0)
@@ -598,6 +599,14 @@ def adjoint_workload(args, dist: Dist) -> dict:
                                "(amplitude 0.1), gradient w.r.t. initial rho, vx, vy, p",
                    "n0": n, "n1": n},
         "forward_step_ms": round(fwd_ms, 4), "adjoint_step_ms": round(vjp_ms, 4),
+        "taped_step_ms": round(tape_ms, 4),
+        "adjoint_step_note": "reverse sweep of one step from the tape its forward step wrote "
+                             "when the backward pass recomputed the segment; per gradient step "
+                             "the work is forward + taped recompute + reverse",
+        "per_step_cost_over_forward": {
+            "reverse": round(vjp_ms / fwd_ms, 3),
+            "taped_recompute": round(tape_ms / fwd_ms, 3),
+            "gradient_wall": round(grad_s * 1e3 / T / fwd_ms, 3)},
         "gradient_run_s": round(grad_s, 3), "loss": loss,
         "forward_gcell_s": round(cells / (fwd_ms * 1e-3) / 1e9, 3),
         "fd": {"directions": args.fd_dirs, "forward": "FP64 fused (bit-exact with the oracle)",

@@ -180,8 +180,15 @@ om_status om_hydro_tape_free(om_hydro_tape tape);
  * The handle ends at the final state; *loss receives the loss. */
 om_status om_hydro_adjoint_run(om_handle h, int steps, const void *target,
                                int checkpoint_every, double *loss, void *const *grad);
-/* Device time of one adjoint step at the current state (ms, mean of reps). */
+/* Device time (ms, mean of reps) of one adjoint step at the current state:
+ * the reverse sweep from the step's tape.  The tape (stage-1 state and both
+ * stages' flux differences) is written by the forward step itself when the
+ * backward pass recomputes a segment from its checkpoint; its cost is
+ * om_hydro_time_tape's. */
 om_status om_hydro_time_vjp(om_handle h, int reps, float *ms);
+/* Device time (ms, mean of reps) of one taped forward step at the current
+ * state; the handle does not move. */
+om_status om_hydro_time_tape(om_handle h, int reps, float *ms);
 
 /* ---- measurement ------------------------------------------------------- */
 

@@ -6,19 +6,22 @@
 // cotangent of the state before it, through both stages, both axes, the
 // MUSCL-minmod reconstruction, the HLLC fluxes, the clamps and the dt of the
 // step (dt = cfl * min timescale: its cotangent is routed to the arg-min
-// cell).  Three launches over TX x TY tiles whose face work lives in shared
-// memory, so every cotangent is written by exactly one thread, and one
-// single-block launch:
-//   A+B  forward recompute of the tile (as the fused forward step); stage-1
-//        state and walls stored; stage-2 update reverse per cell -> U2b,
-//        base part, dt partial; minimum CFL timescale
+// cell).  It reads the step's tape, written by the forward step itself when
+// it is recomputed from a checkpoint (hydro_fused_tape_kernel: the stage-1
+// state and both stages' flux differences), and runs as three launches over
+// TX x TY tiles whose face work lives in shared memory, so every cotangent
+// is written by exactly one thread, and one single-block launch:
+//   B    stage-2 update reverse per cell -> conserved cotangent U2b, base
+//        part of the previous-state cotangent, dt partial; minimum CFL
+//        timescale of the state
 //   C+D  stage-2 walls reverse (HLLC, MUSCL, per stencil slot in shared
 //        memory), gather into the stage-1 cotangent, stage-1 update reverse
 //   E+F  stage-1 walls reverse and gather into the previous-state cotangent;
 //        arg-min of the timescale
 //   G    dt cotangent (partials summed in a fixed order) to the arg-min cell
 // Multi-step gradients use sqrt(T) checkpointing: the forward keeps every
-// s-th state, the backward recomputes each segment and walks it backwards.
+// s-th state; the backward recomputes each segment with the taped step and
+// walks it backwards.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -58,6 +61,7 @@ constexpr int kCheapWrap = 40;
 struct StepIn {
   double dt;
   void *state[4];
+  void *tape[20];   // the step's HydroTapeOut: q[4], d1[8], d2[8]
 };
 
 template <class R> struct Geo {
@@ -68,6 +72,18 @@ template <class R> struct Geo {
   __device__ __forceinline__ Fields<R> state() const {
     return Fields<R>{{(R *)in->state[0], (R *)in->state[1], (R *)in->state[2],
                       (R *)in->state[3]}};
+  }
+  // the tape: stage-1 state, stage-1 and stage-2 flux differences
+  __device__ __forceinline__ Fields<R> q() const {
+    return Fields<R>{{(R *)in->tape[0], (R *)in->tape[1], (R *)in->tape[2], (R *)in->tape[3]}};
+  }
+  __device__ __forceinline__ void d1(size_t i, R D[8]) const {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) D[k] = ((const R *)in->tape[4 + k])[i];
+  }
+  __device__ __forceinline__ void d2(size_t i, R D[8]) const {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) D[k] = ((const R *)in->tape[12 + k])[i];
   }
   // periodic index of a cell at most 4 cells (or one tile plus 3 cells)
   // outside the mesh
@@ -82,17 +98,6 @@ template <class R> struct Geo {
       y %= n1; if (y < 0) y += n1;
     }
     return (size_t)y * n0 + x;
-  }
-};
-
-// one stored flux per face and axis: 4 arrays per axis
-template <class R> struct FluxStore {
-  R *f[8];  // axis 0: fd, fm0, fm1, fe; axis 1: fd, fm0, fm1, fe
-  __device__ __forceinline__ Flux<R> get(int ax, size_t i) const {
-    return Flux<R>{f[4 * ax][i], f[4 * ax + 1][i], f[4 * ax + 2][i], f[4 * ax + 3][i]};
-  }
-  __device__ __forceinline__ void set(int ax, size_t i, const Flux<R> &v) const {
-    f[4 * ax][i] = v.fd; f[4 * ax + 1][i] = v.fm0; f[4 * ax + 2][i] = v.fm1; f[4 * ax + 3][i] = v.fe;
   }
 };
 
@@ -121,20 +126,14 @@ __device__ __forceinline__ unsigned long long warp_min(unsigned long long v) {
   return v;
 }
 
-// A+B on one TX x TY tile: the forward recompute of the step in the layout
-// of the fused forward kernel (state box with a 3-cell halo, stage-1 walls,
-// stage-1 cells with a 2-cell halo, stage-2 walls of the tile), storing the
-// stage-1 state Q and the stage-1 walls F1 of the tile cells; then per tile
-// cell the stage-2 update reverse (conserved cotangent U2b, base part of the
-// previous-state cotangent, the dt partial) and the CFL timescale minimum of
-// the state.
+// B on one TX x TY tile: per cell the stage-2 update reverse from the
+// taped flux differences (conserved cotangent U2b, base part of the
+// previous-state cotangent, the dt partial) and the CFL timescale minimum
+// of the state.
 template <class R, int TX, int TY>
 __global__ void __launch_bounds__(256)
-adj_forward_tile(Fields<R> Ub, Fields<R> Q, FluxStore<R> F1, Fields<R> U2b, Fields<R> Pbase,
-                 Geo<R> G, double *partial, unsigned long long *minbits) {
-  using S = FusedSmem<R, TX, TY>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  S &s = *reinterpret_cast<S *>(smem_raw);
+adj_update2_rev(Fields<R> Ub, Fields<R> U2b, Fields<R> Pbase, Geo<R> G, double *partial,
+                unsigned long long *minbits) {
   __shared__ double sh[8];
   G.dt = (R)G.in->dt;
   const Fields<R> P = G.state();
@@ -142,107 +141,6 @@ adj_forward_tile(Fields<R> Ub, Fields<R> Q, FluxStore<R> F1, Fields<R> U2b, Fiel
   const int nt0 = (G.n0 + TX - 1) / TX;
   const int X0 = (int)(blockIdx.x % nt0) * TX, Y0 = (int)(blockIdx.x / nt0) * TY;
   const R g = G.g;
-  // state box (origin X0-3, Y0-3) with sound speeds
-  for (int i = tid; i < S::PY * S::PX; i += nthr) {
-    const int py = i / S::PX, px = i - py * S::PX;
-    const size_t gi = G.at(X0 + px - 3, Y0 + py - 3);
-    const R r = P.f[0][gi], u = P.f[1][gi], v = P.f[2][gi], q = P.f[3][gi];
-    s.P[0][py][px] = r;
-    s.P[1][py][px] = u;
-    s.P[2][py][px] = v;
-    s.P[3][py][px] = q;
-    s.C[py][px] = hs::sound(g, r, q);
-  }
-  __syncthreads();
-  // stage-1 walls: x wall fx of box row fy+1 is the left wall of box cell
-  // (fx+1, fy+1); y wall (fx, fy) is the lower wall of box cell (fx+1, fy+1)
-  {
-    constexpr int NX = S::FXY * S::FXX, NY = S::FYY * S::FYX;
-    for (int i = tid; i < NX + NY; i += nthr) {
-      if (i < NX) {
-        const int fy = i / S::FXX, fx = i - fy * S::FXX;
-        const int py = fy + 1;
-        const Prim<R> L{s.P[0][py][fx], s.P[1][py][fx], s.P[2][py][fx], s.P[3][py][fx]};
-        const Prim<R> Rt{s.P[0][py][fx + 1], s.P[1][py][fx + 1], s.P[2][py][fx + 1],
-                         s.P[3][py][fx + 1]};
-        s.fx[i] = hs::hllc<0>(g, L, s.C[py][fx], Rt, s.C[py][fx + 1]);
-      } else {
-        const int j = i - NX;
-        const int fy = j / S::FYX, fx = j - fy * S::FYX;
-        const int px = fx + 1;
-        const Prim<R> L{s.P[0][fy][px], s.P[1][fy][px], s.P[2][fy][px], s.P[3][fy][px]};
-        const Prim<R> Rt{s.P[0][fy + 1][px], s.P[1][fy + 1][px], s.P[2][fy + 1][px],
-                         s.P[3][fy + 1][px]};
-        s.fy[j] = hs::hllc<1>(g, L, s.C[fy][px], Rt, s.C[fy + 1][px]);
-      }
-    }
-  }
-  __syncthreads();
-  // stage-1 cells (Q box cell (qx, qy) is state box cell (qx+1, qy+1))
-  {
-    const R h = G.dt / R(2);
-    const R dtdx0 = h / G.dR0, dtdx1 = h / G.dR1;
-    for (int i = tid; i < S::QY * S::QX; i += nthr) {
-      const int qy = i / S::QX, qx = i - qy * S::QX;
-      const int py = qy + 1, px = qx + 1;
-      const Prim<R> b{s.P[0][py][px], s.P[1][py][px], s.P[2][py][px], s.P[3][py][px]};
-      const Prim<R> q = hs::update(g, b, dtdx0, dtdx1, s.fx[qy * S::FXX + qx],
-                                   s.fx[qy * S::FXX + qx + 1], s.fy[qy * S::FYX + qx],
-                                   s.fy[(qy + 1) * S::FYX + qx]);
-      s.Q[0][qy][qx] = q.rho;
-      s.Q[1][qy][qx] = q.v0;
-      s.Q[2][qy][qx] = q.v1;
-      s.Q[3][qy][qx] = q.p;
-    }
-  }
-  __syncthreads();
-  // the tile's stage-1 state and its cells' own (left / lower) stage-1 walls
-  for (int i = tid; i < TX * TY; i += nthr) {
-    const int ty = i / TX, tx = i - ty * TX;
-    const int x = X0 + tx, y = Y0 + ty;
-    if (x >= G.n0 || y >= G.n1) continue;
-    const size_t gi = (size_t)y * G.n0 + x;
-#pragma unroll
-    for (int c = 0; c < 4; ++c) Q.f[c][gi] = s.Q[c][ty + 2][tx + 2];
-    F1.set(0, gi, s.fx[(ty + 2) * S::FXX + tx + 2]);
-    F1.set(1, gi, s.fy[(ty + 2) * S::FYX + tx + 2]);
-  }
-  __syncthreads();
-  // stage-2 walls of the tile (MUSCL on the stage-1 state)
-  {
-    constexpr int NX = TY * (TX + 1), NY = (TY + 1) * TX;
-    for (int i = tid; i < NX + NY; i += nthr) {
-      hs::Prim<R> L, Rt;
-      if (i < NX) {
-        const int sy = i / (TX + 1), sx = i - sy * (TX + 1);
-        const int qy = sy + 2;
-#pragma unroll
-        for (int f = 0; f < 4; ++f) {
-          R l, r;
-          hs::muscl(s.Q[f][qy][sx], s.Q[f][qy][sx + 1], s.Q[f][qy][sx + 2], s.Q[f][qy][sx + 3],
-                    l, r);
-          (&L.rho)[f] = l;
-          (&Rt.rho)[f] = r;
-        }
-        s.fx[i] = hs::hllc<0>(g, L, hs::sound(g, L.rho, L.p), Rt, hs::sound(g, Rt.rho, Rt.p));
-      } else {
-        const int j = i - NX;
-        const int sy = j / TX, sx = j - sy * TX;
-        const int qx = sx + 2;
-#pragma unroll
-        for (int f = 0; f < 4; ++f) {
-          R l, r;
-          hs::muscl(s.Q[f][sy][qx], s.Q[f][sy + 1][qx], s.Q[f][sy + 2][qx], s.Q[f][sy + 3][qx],
-                    l, r);
-          (&L.rho)[f] = l;
-          (&Rt.rho)[f] = r;
-        }
-        s.fy[j] = hs::hllc<1>(g, L, hs::sound(g, L.rho, L.p), Rt, hs::sound(g, Rt.rho, Rt.p));
-      }
-    }
-  }
-  __syncthreads();
-  // stage-2 update reverse per tile cell
   const R d0 = G.dt / G.dR0, d1 = G.dt / G.dR1;
   const R rdR0 = R(1) / G.dR0, rdR1 = R(1) / G.dR1;
   double dtb = 0;
@@ -252,12 +150,11 @@ adj_forward_tile(Fields<R> Ub, Fields<R> Q, FluxStore<R> F1, Fields<R> U2b, Fiel
     const int x = X0 + tx, y = Y0 + ty;
     if (x >= G.n0 || y >= G.n1) continue;
     const size_t gi = (size_t)y * G.n0 + x;
-    const Flux<R> l0 = s.fx[ty * (TX + 1) + tx], r0 = s.fx[ty * (TX + 1) + tx + 1];
-    const Flux<R> l1 = s.fy[ty * TX + tx], r1 = s.fy[(ty + 1) * TX + tx];
-    const Prim<R> b{s.P[0][ty + 3][tx + 3], s.P[1][ty + 3][tx + 3], s.P[2][ty + 3][tx + 3],
-                    s.P[3][ty + 3][tx + 3]};
+    R D[8];
+    G.d2(gi, D);
+    const Prim<R> b = P.get(gi);
     R u[4];
-    ha::update_cons(g, b, d0, d1, l0, r0, l1, r1, u);
+    ha::update_cons_d(g, b, d0, d1, D, u);
     const Prim<R> qb_ = Ub.get(gi);
     const PrimBar<R> qb{qb_.rho, qb_.v0, qb_.v1, qb_.p};
     R U[4];
@@ -267,10 +164,8 @@ adj_forward_tile(Fields<R> Ub, Fields<R> Q, FluxStore<R> F1, Fields<R> U2b, Fiel
     ha::zero(bb);
     ha::cons_of_prim_rev(g, b, U, bb);
     Pbase.set(gi, Prim<R>{bb.rho, bb.v0, bb.v1, bb.p});
-    const R t0 = U[0] * (l0.fd - r0.fd) + U[1] * (l0.fm0 - r0.fm0) + U[2] * (l0.fm1 - r0.fm1) +
-                 U[3] * (l0.fe - r0.fe);
-    const R t1 = U[0] * (l1.fd - r1.fd) + U[1] * (l1.fm0 - r1.fm0) + U[2] * (l1.fm1 - r1.fm1) +
-                 U[3] * (l1.fe - r1.fe);
+    const R t0 = U[0] * D[0] + U[1] * D[1] + U[2] * D[2] + U[3] * D[3];
+    const R t1 = U[0] * D[4] + U[1] * D[5] + U[2] * D[6] + U[3] * D[7];
     dtb += (double)(t0 * rdR0 + t1 * rdR1);
     const unsigned long long tb =
         hk::ts_bits<R>(hs::timescale(g, G.dR0, G.dR1, b.rho, b.v0, b.v1, b.p));
@@ -341,14 +236,13 @@ __device__ __forceinline__ void face2_rev(R g, const Prim<R> st[4], const Flux<R
 // stage-1 update reverse.
 template <class R, int TX, int TY>
 __global__ void __launch_bounds__(256, AdjOcc<R>::stage2)
-adj_stage2_tile(Fields<R> Q, Fields<R> U2b, FluxStore<R> F1, Fields<R> U1b, Fields<R> Pbase,
-                Geo<R> G, double *partial) {
+adj_stage2_tile(Fields<R> U2b, Fields<R> U1b, Fields<R> Pbase, Geo<R> G, double *partial) {
   using S = Stage2Smem<R, TX, TY>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   S &s = *reinterpret_cast<S *>(smem_raw);
   __shared__ double sh[8];
   G.dt = (R)G.in->dt;
-  const Fields<R> P = G.state();
+  const Fields<R> P = G.state(), Q = G.q();
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int nt0 = (G.n0 + TX - 1) / TX;
   const int X0 = (int)(blockIdx.x % nt0) * TX, Y0 = (int)(blockIdx.x / nt0) * TY;
@@ -432,11 +326,11 @@ adj_stage2_tile(Fields<R> Q, Fields<R> U2b, FluxStore<R> F1, Fields<R> U1b, Fiel
       qb[c] = s.qx[c][ty][tx] + acc;
     }
     const size_t gi = (size_t)y * G.n0 + x;
-    const Flux<R> l0 = F1.get(0, gi), r0 = F1.get(0, G.at(x + 1, y));
-    const Flux<R> l1 = F1.get(1, gi), r1 = F1.get(1, G.at(x, y + 1));
+    R D[8];
+    G.d1(gi, D);
     const Prim<R> b = P.get(gi);
     R u[4];
-    ha::update_cons(G.g, b, e0, e1, l0, r0, l1, r1, u);
+    ha::update_cons_d(G.g, b, e0, e1, D, u);
     const PrimBar<R> qbar{qb[0], qb[1], qb[2], qb[3]};
     R U[4];
     ha::cons_from_prim_rev(G.g, u[0], u[1], u[2], u[3], qbar, U);
@@ -446,10 +340,8 @@ adj_stage2_tile(Fields<R> Q, Fields<R> U2b, FluxStore<R> F1, Fields<R> U1b, Fiel
     bb.rho = pb0.rho; bb.v0 = pb0.v0; bb.v1 = pb0.v1; bb.p = pb0.p;
     ha::cons_of_prim_rev(G.g, b, U, bb);
     Pbase.set(gi, Prim<R>{bb.rho, bb.v0, bb.v1, bb.p});
-    const R t0 = U[0] * (l0.fd - r0.fd) + U[1] * (l0.fm0 - r0.fm0) + U[2] * (l0.fm1 - r0.fm1) +
-                 U[3] * (l0.fe - r0.fe);
-    const R t1 = U[0] * (l1.fd - r1.fd) + U[1] * (l1.fm0 - r1.fm0) + U[2] * (l1.fm1 - r1.fm1) +
-                 U[3] * (l1.fe - r1.fe);
+    const R t0 = U[0] * D[0] + U[1] * D[1] + U[2] * D[2] + U[3] * D[3];
+    const R t1 = U[0] * D[4] + U[1] * D[5] + U[2] * D[6] + U[3] * D[7];
     // dtdx = (dt / 2) / dR
     dtb += (double)(R(0.5) * (t0 * rdR0 + t1 * rdR1));
   }
@@ -585,10 +477,45 @@ adj_loss(const R *rho, const R *target, R *rhob, size_t n, double *partial) {
 // host side
 // ---------------------------------------------------------------------------
 
+// The tape of one step: HydroTapeOut's 20 arrays (q[4], d1[8], d2[8]).
+struct StepTape {
+  void *p[20] = {};
+  HydroTapeOut out() const {
+    HydroTapeOut t;
+    for (int k = 0; k < 4; ++k) t.q[k] = p[k];
+    for (int k = 0; k < 8; ++k) {
+      t.d1[k] = p[4 + k];
+      t.d2[k] = p[12 + k];
+    }
+    return t;
+  }
+};
+
+static void tape_free(StepTape *t) {
+  for (void *&q : t->p) {
+    if (q) cudaFree(q);
+    q = nullptr;
+  }
+}
+
+static bool tape_alloc(size_t bytes, StepTape *t) {
+  for (void *&q : t->p)
+    if (cudaMalloc(&q, bytes) != cudaSuccess) {
+      q = nullptr;
+      cudaGetLastError();
+      tape_free(t);
+      return false;
+    }
+  return true;
+}
+
 struct AdjointScratch {
   int fp64 = -1;
   size_t cells = 0;
-  void *q[4], *u2b[4], *u1b[4], *pbase[4], *ub[4], *pb[4], *f1[8];
+  void *u2b[4], *u1b[4], *pbase[4], *ub[4], *pb[4], *next[4];
+  StepTape tape1;                 // the tape of a single step
+  HydroScalars *sc = nullptr;     // scalar block a single taped step updates
+  double *dt_scratch = nullptr;
   adj::StepIn *d_in = nullptr;    // the step being reversed (device)
   adj::StepIn *h_in1 = nullptr;   // pinned slot for single steps
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // by cotangent buffer parity
@@ -597,7 +524,7 @@ struct AdjointScratch {
   double *partials = nullptr;
   unsigned long long *argmin = nullptr;
   int nparts = 0;   // blocks of the grid-stride kernels
-  int ntiles = 0;   // tiles of the fused reverse kernels
+  int ntiles = 0;   // tiles of the reverse kernels
   std::vector<void *> all;
 };
 
@@ -608,6 +535,9 @@ static void free_scratch(AdjointScratch *s) {
   cudaFree(s->d_in);
   cudaFreeHost(s->h_in1);
   for (void *p : s->all) cudaFree(p);
+  tape_free(&s->tape1);
+  cudaFree(s->sc);
+  cudaFree(s->dt_scratch);
   cudaFree(s->partials);
   cudaFree(s->argmin);
   delete s;
@@ -618,10 +548,6 @@ static std::vector<std::pair<Handle *, AdjointScratch *>> g_scratch;
 
 template <class R> static cudaError_t allow_tile_smem() {
   constexpr int TX = adj::AdjTile<R>::TX, TY = adj::AdjTile<R>::TY;
-  cudaError_t e = cudaFuncSetAttribute(adj::adj_forward_tile<R, TX, TY>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)sizeof(FusedSmem<R, TX, TY>));
-  if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(adj::adj_stage2_tile<R, TX, TY>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)sizeof(adj::Stage2Smem<R, TX, TY>));
@@ -641,10 +567,9 @@ static om_status get_scratch(Handle *h, int fp64, AdjointScratch **out) {
   s->fp64 = fp64;
   s->cells = h->memory_size_total();
   const size_t bytes = s->cells * (fp64 ? 8 : 4);
-  void **groups[7] = {s->q, s->u2b, s->u1b, s->pbase, s->ub, s->pb, s->f1};
-  const int sizes[7] = {4, 4, 4, 4, 4, 4, 8};
-  for (int gi = 0; gi < 7; ++gi)
-    for (int k = 0; k < sizes[gi]; ++k) {
+  void **groups[6] = {s->u2b, s->u1b, s->pbase, s->ub, s->pb, s->next};
+  for (int gi = 0; gi < 6; ++gi)
+    for (int k = 0; k < 4; ++k) {
       void *p = nullptr;
       if (cudaMalloc(&p, bytes) != cudaSuccess) {
         cudaGetLastError();
@@ -660,7 +585,9 @@ static om_status get_scratch(Handle *h, int fp64, AdjointScratch **out) {
   const int ty = fp64 ? adj::AdjTile<double>::TY : adj::AdjTile<float>::TY;
   s->ntiles = ((h->size[0] + tx - 1) / tx) * ((h->size[1] + ty - 1) / ty);
   const cudaError_t ea = fp64 ? allow_tile_smem<double>() : allow_tile_smem<float>();
-  if (ea != cudaSuccess ||
+  if (ea != cudaSuccess || !tape_alloc(bytes, &s->tape1) ||
+      cudaMalloc(&s->sc, sizeof(HydroScalars)) != cudaSuccess ||
+      cudaMalloc(&s->dt_scratch, sizeof(double)) != cudaSuccess ||
       cudaMalloc(&s->partials, sizeof(double) * std::max(s->nparts, 2 * s->ntiles)) !=
           cudaSuccess ||
       cudaMalloc(&s->d_in, sizeof(adj::StepIn)) != cudaSuccess ||
@@ -689,18 +616,12 @@ template <class R> static adj::Fields<R> F4(void *const *p) {
   return adj::Fields<R>{{(R *)p[0], (R *)p[1], (R *)p[2], (R *)p[3]}};
 }
 
-template <class R> static adj::FluxStore<R> FS(void *const *p) {
-  adj::FluxStore<R> f;
-  for (int k = 0; k < 8; ++k) f.f[k] = (R *)p[k];
-  return f;
-}
-
 // kernels of one adjoint step (the three tile kernels and the dt kernel)
 constexpr int kVjpLaunches = 4;
 
-// The kernels of one adjoint step, reading the step's dt and state from
-// s->d_in: ub (4 device arrays, cotangent of the state after the step) ->
-// pb_out (4 device arrays, cotangent of the state before it).
+// The kernels of one adjoint step, reading the step's dt, state and tape
+// from s->d_in: ub (4 device arrays, cotangent of the state after the step)
+// -> pb_out (4 device arrays, cotangent of the state before it).
 template <class R>
 static om_status vjp_kernels(Handle *h, AdjointScratch *s, void *const *ub, void *const *pb_out,
                              double cfl) {
@@ -711,15 +632,14 @@ static om_status vjp_kernels(Handle *h, AdjointScratch *s, void *const *ub, void
                 s->d_in,    cheap};
   const int nt = s->ntiles;
   constexpr int TX = adj::AdjTile<R>::TX, TY = adj::AdjTile<R>::TY;
-  const auto Q = F4<R>(s->q), U = F4<R>(ub), U2b = F4<R>(s->u2b), U1b = F4<R>(s->u1b),
-             Pbase = F4<R>(s->pbase), Pb = F4<R>(pb_out);
-  const auto F1 = FS<R>(s->f1);
+  const auto U = F4<R>(ub), U2b = F4<R>(s->u2b), U1b = F4<R>(s->u1b), Pbase = F4<R>(s->pbase),
+             Pb = F4<R>(pb_out);
   // argmin[0]: arg-min cell, argmin[1]: minimum timescale bits
   OM_CUDA_CHECK(cudaMemsetAsync(s->argmin, 0xFF, 2 * sizeof(unsigned long long), st));
-  adj::adj_forward_tile<R, TX, TY><<<nt, 256, sizeof(FusedSmem<R, TX, TY>), st>>>(
-      U, Q, F1, U2b, Pbase, G, s->partials, s->argmin + 1);
+  adj::adj_update2_rev<R, TX, TY><<<nt, 256, 0, st>>>(U, U2b, Pbase, G, s->partials,
+                                                      s->argmin + 1);
   adj::adj_stage2_tile<R, TX, TY><<<nt, 256, sizeof(adj::Stage2Smem<R, TX, TY>), st>>>(
-      Q, U2b, F1, U1b, Pbase, G, s->partials + nt);
+      U2b, U1b, Pbase, G, s->partials + nt);
   adj::adj_stage1_tile<R, TX, TY><<<nt, 256, 0, st>>>(U1b, Pbase, Pb, G, s->argmin + 1,
                                                       s->argmin);
   adj::adj_dt<R><<<1, 1024, 0, st>>>(Pb, G, s->partials, 2 * nt, (R)cfl, s->argmin);
@@ -727,10 +647,21 @@ static om_status vjp_kernels(Handle *h, AdjointScratch *s, void *const *ub, void
   return OM_OK;
 }
 
+// The taped step of the handle's current state into s->tape1 (the handle
+// does not move) and the record of that step in *in.
+static om_status tape_current(Handle *h, AdjointScratch *s, adj::StepIn *in) {
+  unsigned long long bits;
+  OM_TRY(hydro_current_dt(h, &in->dt, &bits));
+  for (int k = 0; k < 4; ++k) in->state[k] = h->arrays[k].d();
+  OM_TRY(hydro_tape_step(h, s->next, s->sc, s->dt_scratch, s->tape1.out()));
+  for (int k = 0; k < 20; ++k) in->tape[k] = s->tape1.p[k];
+  return OM_OK;
+}
+
 // One adjoint step.  `slot` (pinned host memory, left untouched until the
-// stream has passed this step) holds the step's dt and state; it is copied
-// to s->d_in, then the kernel sequence runs from a CUDA graph captured once
-// per pair of cotangent buffers (and per cfl, dR0, dR1).
+// stream has passed this step) holds the step's dt, state and tape; it is
+// copied to s->d_in, then the kernel sequence runs from a CUDA graph
+// captured once per pair of cotangent buffers (and per cfl, dR0, dR1).
 template <class R>
 static om_status vjp_step(Handle *h, AdjointScratch *s, const adj::StepIn *slot,
                           void *const *ub, void *const *pb_out, double cfl) {
@@ -784,10 +715,14 @@ struct om_hydro_tape_s {
   int steps = 0, seg = 0, nck = 0;
   std::vector<HydroCheckpoint> ck;     // state before segment j, and the final state
   std::vector<HydroCheckpoint> segst;  // states of one recomputed segment
+  std::vector<StepTape> tapes;         // tapes of one recomputed segment (empty:
+                                       // each step is taped again before its reverse)
+  std::vector<HydroTapeOut> outs;      // their records, alive while steps launch
   adj::StepIn *h_in = nullptr;         // pinned: one record per step
   ~om_hydro_tape_s() {
     for (auto &c : ck) hydro_checkpoint_free(&c);
     for (auto &c : segst) hydro_checkpoint_free(&c);
+    for (auto &t : tapes) tape_free(&t);
     if (h_in) cudaFreeHost(h_in);
   }
 };
@@ -805,9 +740,7 @@ extern "C" om_status om_hydro_vjp(om_handle H, void *const *cot_next, void *cons
   for (int i = 0; i < 4; ++i) OM_TRY(bring_device(h, h->arrays[i]));
   // the pinned slot may still feed a step in flight
   OM_CUDA_CHECK(cudaStreamSynchronize(h->stream));
-  unsigned long long bits;
-  OM_TRY(hydro_current_dt(h, &s->h_in1->dt, &bits));
-  for (int k = 0; k < 4; ++k) s->h_in1->state[k] = h->arrays[k].d();
+  OM_TRY(tape_current(h, s, s->h_in1));
   const double cfl = ((HydroScalars *)h->h_scalars)->cfl;
   OM_CUDA_CHECK(cudaMemcpyAsync(s->d_in, s->h_in1, sizeof(adj::StepIn), cudaMemcpyHostToDevice,
                                 h->stream));
@@ -855,6 +788,26 @@ extern "C" om_status om_hydro_forward(om_handle H, int steps, int checkpoint_eve
     if ((status = hydro_checkpoint_alloc(h, &c)) != OM_OK) return fail(status);
   for (auto &c : t->segst)
     if ((status = hydro_checkpoint_alloc(h, &c)) != OM_OK) return fail(status);
+  {
+    // one tape per step of a segment when they fit in half the free memory;
+    // otherwise each step is taped again right before its reverse
+    const size_t bytes = h->memory_size_total() * h->arrays[0].elem_size;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+      cudaGetLastError();
+      free_b = 0;
+    }
+    if ((double)bytes * 20.0 * t->seg <= 0.5 * (double)free_b && !injected_alloc_failure()) {
+      t->tapes.resize(t->seg);
+      for (auto &tp : t->tapes)
+        if (!tape_alloc(bytes, &tp)) {
+          for (auto &q : t->tapes) tape_free(&q);
+          t->tapes.clear();
+          break;
+        }
+      for (auto &tp : t->tapes) t->outs.push_back(tp.out());
+    }
+  }
   if (cudaMallocHost(&t->h_in, sizeof(adj::StepIn) * (size_t)steps) != cudaSuccess) {
     cudaGetLastError();
     t->h_in = nullptr;
@@ -890,7 +843,9 @@ static om_status backward_core(om_handle H, om_hydro_tape t, AdjointScratch *s, 
   const double cfl = ((HydroScalars *)h->h_scalars)->cfl;
   for (int j = t->nck - 1; j >= 0; --j) {
     const int len = std::min(t->seg, t->steps - j * t->seg);
-    // recompute the segment from its checkpoint, keeping every state
+    const bool taped = (int)t->tapes.size() >= len;
+    // recompute the segment from its checkpoint with the taped step,
+    // keeping every state
     OM_TRY(hydro_restore(h, &t->ck[j]));
     for (int m = 0; m < len; ++m) {
       adj::StepIn &in = t->h_in[j * t->seg + m];
@@ -898,10 +853,25 @@ static om_status backward_core(om_handle H, om_hydro_tape t, AdjointScratch *s, 
       OM_TRY(hydro_save(h, &t->segst[m]));
       OM_TRY(hydro_current_dt(h, &in.dt, &bits));
       for (int k = 0; k < 4; ++k) in.state[k] = t->segst[m].f[k];
-      OM_TRY(om_run(H, kid));
+      if (taped) {
+        for (int k = 0; k < 20; ++k) in.tape[k] = t->tapes[m].p[k];
+        hydro_set_tape(h, &t->outs[m]);
+        const om_status r = om_run(H, kid);
+        hydro_set_tape(h, nullptr);
+        OM_TRY(r);
+      } else {
+        OM_TRY(om_run(H, kid));
+      }
     }
     for (int m = len - 1; m >= 0; --m) {
-      OM_TRY(run_vjp_step(h, s, &t->h_in[j * t->seg + m], ub, pb, cfl));
+      adj::StepIn &in = t->h_in[j * t->seg + m];
+      if (!taped) {
+        // tape this step again from its saved state (one tape buffer)
+        OM_TRY(hydro_restore(h, &t->segst[m]));
+        OM_TRY(hydro_tape_step(h, s->next, s->sc, s->dt_scratch, s->tape1.out()));
+        for (int k = 0; k < 20; ++k) in.tape[k] = s->tape1.p[k];
+      }
+      OM_TRY(run_vjp_step(h, s, &in, ub, pb, cfl));
       for (int k = 0; k < 4; ++k) std::swap(ub[k], pb[k]);
     }
   }
@@ -1011,9 +981,10 @@ extern "C" om_status om_hydro_adjoint_run(om_handle H, int steps, const void *ta
   return done(OM_OK);
 }
 
-// device time (ms) of one adjoint step at the handle's current state, for
-// measurement (cotangent input: zero arrays; the kernels' work does not
-// depend on the values)
+// Device time (ms) of one adjoint step at the handle's current state, for
+// measurement: the reverse sweep from the step's tape (made once, outside
+// the timed region) with zero cotangents (the kernels' work does not depend
+// on their values).
 extern "C" om_status om_hydro_time_vjp(om_handle H, int reps, float *ms) {
   Handle *h = handle_of(H);
   if (!h || h->kind != OM_KIND_HYDRO || reps < 1 || !ms) {
@@ -1026,9 +997,7 @@ extern "C" om_status om_hydro_time_vjp(om_handle H, int reps, float *ms) {
   OM_TRY(get_scratch(h, fp64, &s));
   for (int i = 0; i < 4; ++i) OM_TRY(bring_device(h, h->arrays[i]));
   OM_CUDA_CHECK(cudaStreamSynchronize(h->stream));
-  unsigned long long bits;
-  OM_TRY(hydro_current_dt(h, &s->h_in1->dt, &bits));
-  for (int k = 0; k < 4; ++k) s->h_in1->state[k] = h->arrays[k].d();
+  OM_TRY(tape_current(h, s, s->h_in1));
   const size_t bytes = h->memory_size_total() * (fp64 ? 8 : 4);
   for (int k = 0; k < 4; ++k) OM_CUDA_CHECK(cudaMemsetAsync(s->ub[k], 0, bytes, h->stream));
   const double cfl = ((HydroScalars *)h->h_scalars)->cfl;
@@ -1047,6 +1016,42 @@ extern "C" om_status om_hydro_time_vjp(om_handle H, int reps, float *ms) {
                       cudaEventSynchronize(e1) != cudaSuccess ||
                       cudaEventElapsedTime(ms, e0, e1) != cudaSuccess)) {
     set_error("om_hydro_time_vjp: timing failed");
+    st = OM_ERR_CUDA;
+  }
+  if (st == OM_OK) *ms /= reps;
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  return st;
+}
+
+// Device time (ms) of one taped forward step at the handle's current state
+// (the step the backward pass recomputes each segment with), mean of reps;
+// the handle does not move.
+extern "C" om_status om_hydro_time_tape(om_handle H, int reps, float *ms) {
+  Handle *h = handle_of(H);
+  if (!h || h->kind != OM_KIND_HYDRO || reps < 1 || !ms) {
+    set_error("om_hydro_time_tape: bad arguments");
+    return OM_ERR_ARG;
+  }
+  OM_CUDA_CHECK(cudaSetDevice(h->device));
+  const int fp64 = h->cfg.precision == 64;
+  AdjointScratch *s;
+  OM_TRY(get_scratch(h, fp64, &s));
+  const HydroTapeOut out = s->tape1.out();
+  OM_TRY(hydro_tape_step(h, s->next, s->sc, s->dt_scratch, out));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  om_status st = OM_OK;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess ||
+      cudaEventRecord(e0, h->stream) != cudaSuccess) {
+    set_error("om_hydro_time_tape: event setup failed");
+    st = OM_ERR_CUDA;
+  }
+  for (int r = 0; st == OM_OK && r < reps; ++r)
+    st = hydro_tape_step(h, s->next, s->sc, s->dt_scratch, out);
+  if (st == OM_OK && (cudaEventRecord(e1, h->stream) != cudaSuccess ||
+                      cudaEventSynchronize(e1) != cudaSuccess ||
+                      cudaEventElapsedTime(ms, e0, e1) != cudaSuccess)) {
+    set_error("om_hydro_time_tape: timing failed");
     st = OM_ERR_CUDA;
   }
   if (st == OM_OK) *ms /= reps;

@@ -350,6 +350,23 @@ __device__ __forceinline__ void update_cons(R g, const Prim<R> &b, R dtdx0, R dt
   out[3] = e1 + dtdx0 * (l0.fe - r0.fe);
 }
 
+// update_cons from the taped flux differences D (D[4 * axis + k], left
+// wall - right wall), in the same operation order
+template <class R>
+__device__ __forceinline__ void update_cons_d(R g, const Prim<R> &b, R dtdx0, R dtdx1,
+                                              const R D[8], R out[4]) {
+  const R m0 = b.rho * b.v0, m1 = b.rho * b.v1;
+  const R e = hs::kinetic(b.v0, b.v1, m0, m1) + (R(1) / (g - R(1))) * b.p;
+  const R d1 = b.rho + dtdx1 * D[4];
+  const R a0 = m0 + dtdx1 * D[5];
+  const R a1 = m1 + dtdx1 * D[6];
+  const R e1 = e + dtdx1 * D[7];
+  out[0] = d1 + dtdx0 * D[0];
+  out[1] = a0 + dtdx0 * D[1];
+  out[2] = a1 + dtdx0 * D[2];
+  out[3] = e1 + dtdx0 * D[3];
+}
+
 // timescale reverse at one cell: tb -> (rho, v0, v1, p)
 template <class R>
 __device__ __forceinline__ void timescale_rev(R g, R dR0, R dR1, const Prim<R> &x, R tb,

@@ -32,6 +32,26 @@ static cudaError_t launch_fused(const HydroStepArgs &a0, cudaStream_t s, int *gr
   return cudaGetLastError();
 }
 
+template <class R>
+static cudaError_t launch_tape(const HydroStepArgs &a0, const HydroTapeOut &t, cudaStream_t s) {
+  constexpr int TX = 32, TY = 16, NT = 256;
+  HydroStepArgs a = a0;
+  a.nt0 = (a.n0 + TX - 1) / TX;
+  const int nt1 = (a.n1 + TY - 1) / TY;
+  const size_t smem = sizeof(FusedSmem<R, TX, TY>);
+  cudaError_t e = cudaFuncSetAttribute(hydro_fused_tape_kernel<R, TX, TY, NT>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  hydro_fused_tape_kernel<R, TX, TY, NT><<<a.nt0 * nt1, NT, smem, s>>>(a, t);
+  return cudaGetLastError();
+}
+
+// taped step of the FP64 and exact FP32 builds
+cudaError_t hydro_fused_tape_exact(int fp64, const HydroStepArgs &a, const HydroTapeOut &t,
+                                   cudaStream_t s) {
+  return fp64 ? launch_tape<double>(a, t, s) : launch_tape<float>(a, t, s);
+}
+
 // a.lm > 0: open grid (margins, jet boundary condition)
 cudaError_t hydro_fused_f64(const HydroStepArgs &a, int tile, cudaStream_t s, int *grid_out) {
   (void)tile;  // one shape in FP64: 32x16 (104 KB of shared memory)

@@ -70,6 +70,24 @@ int hydro_ensemble_occupancy(int fp64, int tile, bool exact) {
   }
 }
 
+cudaError_t hydro_fused_tape_exact(int fp64, const HydroStepArgs &a, const HydroTapeOut &t,
+                                   cudaStream_t s);
+
+cudaError_t hydro_fused_tape(int fp64, bool exact, const HydroStepArgs &a0, const HydroTapeOut &t,
+                             cudaStream_t s) {
+  if (fp64 || exact) return hydro_fused_tape_exact(fp64, a0, t, s);
+  constexpr int TX = 32, TY = 16, NT = 256;
+  HydroStepArgs a = a0;
+  a.nt0 = (a.n0 + TX - 1) / TX;
+  const int nt1 = (a.n1 + TY - 1) / TY;
+  const size_t smem = sizeof(FusedSmem<float, TX, TY>);
+  cudaError_t e = cudaFuncSetAttribute(hydro_fused_tape_kernel<float, TX, TY, NT>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  hydro_fused_tape_kernel<float, TX, TY, NT><<<a.nt0 * nt1, NT, smem, s>>>(a, t);
+  return cudaGetLastError();
+}
+
 cudaError_t hydro_fused_f32(const HydroStepArgs &a, int tile, bool exact, cudaStream_t s,
                             int *grid_out) {
   if (exact) return hydro_fused_f32_exact(a, s, grid_out);

@@ -37,6 +37,17 @@ struct HydroStepArgs {
   const unsigned long long *margin_min;
 };
 
+// What a taped step keeps for the reverse sweep (periodic grids; arrays of
+// n0 x n1 values of the OM's Real type): the stage-1 state q, and per stage
+// the flux differences (left wall - right wall) of each axis that the
+// conservative update adds, d[4 * axis + k] for k = density, momentum 0,
+// momentum 1, energy.
+struct HydroTapeOut {
+  void *q[4];
+  void *d1[8];
+  void *d2[8];
+};
+
 namespace hk {
 
 // A CFL minimum is kept as the bit pattern of a positive value of the OM's
@@ -105,6 +116,21 @@ __device__ __forceinline__ hs::Prim<R> jet_state(R g, R dR0, R dR1, R ext1, int 
   return q;
 }
 
+// the flux differences of one cell's update, as hs::update forms them
+template <class R>
+__device__ __forceinline__ void tape_diffs(void *const *d, size_t gi, const hs::Flux<R> &l0,
+                                           const hs::Flux<R> &r0, const hs::Flux<R> &l1,
+                                           const hs::Flux<R> &r1) {
+  ((R *)d[0])[gi] = l0.fd - r0.fd;
+  ((R *)d[1])[gi] = l0.fm0 - r0.fm0;
+  ((R *)d[2])[gi] = l0.fm1 - r0.fm1;
+  ((R *)d[3])[gi] = l0.fe - r0.fe;
+  ((R *)d[4])[gi] = l1.fd - r1.fd;
+  ((R *)d[5])[gi] = l1.fm0 - r1.fm0;
+  ((R *)d[6])[gi] = l1.fm1 - r1.fm1;
+  ((R *)d[7])[gi] = l1.fe - r1.fe;
+}
+
 // dt of this step in the OM's Real type: dtG = cfl * reduce Min dts
 template <class R> __device__ __forceinline__ R step_dt(const HydroStepArgs &a) {
   const R tsmin = ts_from_bits<R>(a.sc->tsmin[a.read_slot]);
@@ -156,9 +182,12 @@ template <class R, int TX, int TY> struct FusedSmem {
 // OPEN: the grid has margins of width a.lm; box cells outside the interior
 // take the jet state of the boundary condition instead of a periodic image,
 // and the margin cells' timescale minimum joins the CFL minimum.
-template <class R, int TX, int TY, int NT, bool OPEN = false>
+// TAPE (periodic grids): the tile's stage-1 states and both stages' flux
+// differences are also written to `tape`.
+template <class R, int TX, int TY, int NT, bool OPEN = false, bool TAPE = false>
 __device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
-                                           FusedSmem<R, TX, TY> &s, unsigned long long *red) {
+                                           FusedSmem<R, TX, TY> &s, unsigned long long *red,
+                                           const HydroTapeOut *tape = nullptr) {
   using S = FusedSmem<R, TX, TY>;
   const int tid = threadIdx.x;
   const int t0 = tile % a.nt0, t1 = tile / a.nt0;
@@ -238,6 +267,18 @@ __device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
       s.Q[1][qy][qx] = q.v0;
       s.Q[2][qy][qx] = q.v1;
       s.Q[3][qy][qx] = q.p;
+      if (TAPE) {
+        const int ty = qy - 2, tx = qx - 2;
+        if (ty >= 0 && ty < TY && tx >= 0 && tx < TX && Y0 + ty < n1 && X0 + tx < n0) {
+          const size_t gi = (size_t)(Y0 + ty) * n0 + (X0 + tx);
+          ((R *)tape->q[0])[gi] = q.rho;
+          ((R *)tape->q[1])[gi] = q.v0;
+          ((R *)tape->q[2])[gi] = q.v1;
+          ((R *)tape->q[3])[gi] = q.p;
+          hk::tape_diffs<R>(tape->d1, gi, s.fx[qy * S::FXX + qx], s.fx[qy * S::FXX + qx + 1],
+                            s.fy[qy * S::FYX + qx], s.fy[(qy + 1) * S::FYX + qx]);
+        }
+      }
     }
   }
   __syncthreads();
@@ -292,6 +333,9 @@ __device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
           hs::update(g, b, dtdx0, dtdx1, s.fx[oy * (TX + 1) + ox], s.fx[oy * (TX + 1) + ox + 1],
                      s.fy[oy * TX + ox], s.fy[(oy + 1) * TX + ox]);
       const size_t gi = OPEN ? (size_t)(gy + a.lm) * a.ms0 + (gx + a.lm) : (size_t)gy * n0 + gx;
+      if (TAPE)
+        hk::tape_diffs<R>(tape->d2, gi, s.fx[oy * (TX + 1) + ox], s.fx[oy * (TX + 1) + ox + 1],
+                          s.fy[oy * TX + ox], s.fy[(oy + 1) * TX + ox]);
       orho[gi] = q.rho;
       ovx[gi] = q.v0;
       ovy[gi] = q.v1;
@@ -337,6 +381,16 @@ hydro_fused_kernel(HydroStepArgs a) {
   __shared__ unsigned long long red[32];
   fused_tile<R, TX, TY, NT, OPEN>(a, blockIdx.x,
                                   *reinterpret_cast<FusedSmem<R, TX, TY> *>(smem_raw), red);
+}
+
+// the fused step that also writes the tape of the reverse sweep (periodic)
+template <class R, int TX, int TY, int NT>
+__global__ void __launch_bounds__(NT)
+hydro_fused_tape_kernel(HydroStepArgs a, const __grid_constant__ HydroTapeOut t) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ unsigned long long red[32];
+  fused_tile<R, TX, TY, NT, false, true>(
+      a, blockIdx.x, *reinterpret_cast<FusedSmem<R, TX, TY> *>(smem_raw), red, &t);
 }
 
 // CFL timescale minimum of the margin cells of an open grid (the jet state

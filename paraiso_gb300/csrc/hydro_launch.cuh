@@ -18,6 +18,10 @@ void hydro_tile_dims(int tile, int *tx, int *ty);
 cudaError_t hydro_fused_f32(const HydroStepArgs &a, int tile, bool exact, cudaStream_t s,
                             int *grid_out);
 cudaError_t hydro_fused_f64(const HydroStepArgs &a, int tile, cudaStream_t s, int *grid_out);
+// one fused step of a periodic grid that also writes the tape of the
+// reverse sweep (32x16 tiles; the build of the handle's variant)
+cudaError_t hydro_fused_tape(int fp64, bool exact, const HydroStepArgs &a, const HydroTapeOut &t,
+                             cudaStream_t s);
 
 // ensemble step over every instance (persistent grid of `grid` blocks, 0 =
 // resident blocks x SMs); args/prefix in device memory
@@ -78,5 +82,12 @@ om_status hydro_save(Handle *h, HydroCheckpoint *c);
 om_status hydro_restore(Handle *h, const HydroCheckpoint *c);
 // dt of the next step and the CFL minimum bits of the current state
 om_status hydro_current_dt(Handle *h, double *dt, unsigned long long *bits);
+// the next single fused step of h also writes `tape` (nullptr: none); the
+// record must stay valid until that step has been launched
+void hydro_set_tape(Handle *h, const HydroTapeOut *tape);
+// one taped step from h's current state into out[4]; h is left unchanged
+// (the step's scalar updates go to sc_scratch and dt_scratch)
+om_status hydro_tape_step(Handle *h, void *const *out, HydroScalars *sc_scratch,
+                          double *dt_scratch, const HydroTapeOut &tape);
 
 }  // namespace om

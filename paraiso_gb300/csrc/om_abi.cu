@@ -52,7 +52,7 @@ Scalar *Handle::find_scalar(const char *n) {
 // environment, array allocations after the first n (counted from when the
 // variable took its current value) report failure without calling the
 // allocator, so every caller's OM_ERR_NOMEM path can be exercised.
-static bool injected_alloc_failure() {
+bool injected_alloc_failure() {
   static std::mutex mu;
   static std::string seen;
   static long count = 0;

@@ -148,6 +148,9 @@ om_status create_handle(int kind, const int sizes[2], const om_config &cfg,
 om_status alloc_array(Handle *h, const char *name, int elem_size);
 // Device copy up to date (uploads the host mirror if the host is newer).
 om_status bring_device(Handle *h, Array &a);
+// OM_FAIL_ALLOC_AFTER=N (environment): every allocation request after the
+// first N reports failure (tests of the out-of-memory paths)
+bool injected_alloc_failure();
 // Host copy up to date (downloads if the device is newer).
 om_status bring_host(Handle *h, Array &a);
 // Upload the host scalar block before a kernel; download it after.

@@ -42,7 +42,7 @@ EXPORTS = [
     "om_ensemble_scalar", "om_ensemble_set_scalar", "om_ensemble_totals",
     "om_ensemble_last_launch_count", "om_life_proceed_noalloc", "om_autotune",
     "om_autotune_ensemble", "om_hydro_vjp", "om_hydro_adjoint_run", "om_hydro_time_vjp",
-    "om_hydro_forward", "om_hydro_backward", "om_hydro_tape_free", "om_create_graph",
+    "om_hydro_time_tape", "om_hydro_forward", "om_hydro_backward", "om_hydro_tape_free", "om_create_graph",
     "om_graph_source", "om_graph_check", "om_save", "om_load", "om_hydro_write_snapshot",
 ]
 
@@ -119,6 +119,7 @@ def load_library(path: str | None = None) -> C.CDLL:
         "om_hydro_vjp": (i, [vp, C.POINTER(vp), C.POINTER(vp)]),
         "om_hydro_adjoint_run": (i, [vp, i, vp, i, C.POINTER(C.c_double), C.POINTER(vp)]),
         "om_hydro_time_vjp": (i, [vp, i, C.POINTER(C.c_float)]),
+        "om_hydro_time_tape": (i, [vp, i, C.POINTER(C.c_float)]),
         "om_hydro_forward": (i, [vp, i, i, C.POINTER(vp)]),
         "om_hydro_backward": (i, [vp, vp, C.POINTER(vp), C.POINTER(vp)]),
         "om_hydro_tape_free": (i, [vp]),
@@ -432,8 +433,15 @@ class Hydro(OrthotopeMachine):
         return tuple(grads)
 
     def time_vjp(self, reps: int = 5) -> float:
+        """Device ms of one adjoint step (the reverse sweep from its tape)."""
         ms = C.c_float()
         _check(self._L.om_hydro_time_vjp(self._h, int(reps), C.byref(ms)))
+        return ms.value
+
+    def time_tape(self, reps: int = 5) -> float:
+        """Device ms of one taped forward step (the backward pass's recompute)."""
+        ms = C.c_float()
+        _check(self._L.om_hydro_time_tape(self._h, int(reps), C.byref(ms)))
         return ms.value
 
     def set_state(self, st) -> None:

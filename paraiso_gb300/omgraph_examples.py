@@ -88,3 +88,247 @@ def life(size=(80, 48), boundary="cyclic") -> og.OM:
     k.store(generation, gen + 1)
     k.store(cell, new)
     return om
+
+
+# ---------------------------------------------------------------------------
+# examples/Hydro (Hydro.hs, HydroMain.hs)
+# ---------------------------------------------------------------------------
+
+class _HydroRecord:
+    """A bound Hydro record (Hydro.hs:52-130): every field as a node, made
+    in bindHydro's order from a primitive or a conserved triple."""
+
+    def __init__(self, f):
+        self.__dict__.update(f)
+
+
+def _contract(k, terms, typ):
+    acc = k.imm(0, typ)                  # foldl (+) zero
+    for t in terms:
+        acc = acc + t
+    return acc
+
+
+def _bind_hydro(k, g, typ, dens, velo=None, pres=None, mome=None, enrg=None):
+    """bindHydro of a PrimitiveVar (dens, velo, pres) or a ConservedVar
+    (dens, mome, enrg): the Hydrable defaults, each field bound once."""
+    G = lambda: k.imm(g, typ)                           # each kGamma is an imm
+    if velo is not None:                                # PrimitiveVar
+        density, velocity, pressure = dens, list(velo), pres
+        momentum = [density * velocity[i] for i in range(2)]
+        kinetic = k.imm(0.5, typ) * _contract(k, [velocity[i] * momentum[i]
+                                                  for i in range(2)], typ)
+        energy = kinetic + 1 / (G() - 1) * pressure
+    else:                                               # ConservedVar
+        density, momentum, energy = dens, list(mome), enrg
+        velocity = [momentum[i] / density for i in range(2)]
+        kinetic = k.imm(0.5, typ) * _contract(k, [velocity[i] * momentum[i]
+                                                  for i in range(2)], typ)
+        internal = energy - kinetic
+        pressure = (G() - 1) * internal
+    # bindHydro's order: density, velocity, pressure, momentum, energy, ...
+    enthalpy = energy + pressure
+    density_flux = momentum
+    momentum_flux = [[momentum[i] * velocity[j] + pressure * k.imm(1 if i == j else 0, typ)
+                      for j in range(2)] for i in range(2)]
+    energy_flux = [enthalpy * velocity[i] for i in range(2)]
+    sound = og.sqrt(G() * pressure / density)
+    return _HydroRecord(dict(density=density, velocity=velocity, pressure=pressure,
+                             momentum=momentum, energy=energy, enthalpy=enthalpy,
+                             density_flux=density_flux, momentum_flux=momentum_flux,
+                             energy_flux=energy_flux, sound=sound))
+
+
+_FIELDS = ("density", "velocity", "pressure", "momentum", "energy", "enthalpy",
+           "density_flux", "momentum_flux", "energy_flux", "sound")
+
+
+def _map_record(rec, f):
+    out = {}
+    for name in _FIELDS:
+        v = getattr(rec, name)
+        if name == "momentum_flux":
+            out[name] = [[f(x) for x in row] for row in v]
+        elif isinstance(v, list):
+            out[name] = [f(x) for x in v]
+        else:
+            out[name] = f(v)
+    return _HydroRecord(out)
+
+
+def _zip_records(recs, f):
+    out = {}
+    for name in _FIELDS:
+        vs = [getattr(r, name) for r in recs]
+        if name == "momentum_flux":
+            out[name] = [[f(*[v[i][j] for v in vs]) for j in range(2)] for i in range(2)]
+        elif isinstance(vs[0], list):
+            out[name] = [f(*[v[i] for v in vs]) for i in range(2)]
+        else:
+            out[name] = f(*vs)
+    return _HydroRecord(out)
+
+
+def hydro(size=(1024, 1024), gamma=5.0 / 3.0, boundary="open", typ=og.Double) -> og.OM:
+    """examples/Hydro: HydroMain.hs:44-302 with Hydro.hs:37-130 (the
+    statics, buildInit, boundaryCondition, buildProceed, proceedSingle,
+    addFlux, interpolate, hllc), for gamma and Real of choice."""
+    om = og.OM("Hydro", size, boundary)
+    T = typ
+    om.static_scalar("generation", og.Int)
+    time_s = om.static_scalar("time", T)
+    cfl_s = om.static_scalar("cfl", T)
+    dR_s = [om.static_scalar(f"dR{i}", T) for i in range(2)]
+    ext_s = [om.static_scalar(f"extent{i}", T) for i in range(2)]
+    dens_s = om.static_array("density", T)
+    velo_s = [om.static_array(f"velocity{i}", T) for i in range(2)]
+    pres_s = om.static_array("pressure", T)
+
+    def coords(k):
+        dRG = [k.load(s) for s in dR_s]
+        extG = [k.load(s) for s in ext_s]
+        dR = [k.broadcast(v) for v in dRG]
+        extent = [k.broadcast(v) for v in extG]
+        icoord = [og.cast(k.load_index(i), T) for i in range(2)]
+        return dR, extent, icoord, [dR[i] * icoord[i] for i in range(2)]
+
+    def region_of(k, coord, extent):
+        return ((coord[1] > k.imm(0.47, T) * extent[1]) & (coord[1] < k.imm(0.53, T) * extent[1])
+                & (coord[0] < 0))
+
+    # buildInit (HydroMain.hs:79-102)
+    k = om.kernel("init")
+    dR, extent, icoord, coord = coords(k)
+    region = region_of(k, coord, extent)
+    vplus, vminus = (6, 0), (0, 0)
+    velo = [og.select(region, k.imm(vplus[i], T), k.imm(vminus[i], T)) for i in range(2)]
+    factor = 1 + k.imm(1e-3, T) * og.sin(k.imm(6, T) * k.imm(og.PI, T) * coord[0])
+    k.store(dens_s, factor * k.imm(gamma, T) * k.imm(gamma, T) *
+            og.select(region, k.imm(1, T), k.imm(10, T)))
+    for i in range(2):
+        k.store(velo_s[i], velo[i])
+    k.store(pres_s, factor * 0.6)
+
+    # buildProceed (HydroMain.hs:134-164)
+    k = om.kernel("proceed")
+    dens = k.load(dens_s)
+    velo = [k.load(s) for s in velo_s]
+    pres = k.load(pres_s)
+    timeG = k.load(time_s)
+    cflG = k.load(cfl_s)
+    dRG = [k.load(s) for s in dR_s]
+    dR = [k.broadcast(v) for v in dRG]
+    cell0 = _bind_hydro(k, gamma, T, dens, velo, pres)
+
+    # boundaryCondition (HydroMain.hs:105-131)
+    dRG2 = [k.load(s) for s in dR_s]
+    extG = [k.load(s) for s in ext_s]
+    dRb = [k.broadcast(v) for v in dRG2]
+    extent = [k.broadcast(v) for v in extG]
+    icoord = [og.cast(k.load_index(i), T) for i in range(2)]
+    isize = [k.broadcast(og.cast(k.load_size(i), T)) for i in range(2)]
+    coord = [dRb[i] * icoord[i] for i in range(2)]
+    region = region_of(k, coord, extent)
+    jet = _bind_hydro(k, gamma, T,
+                      k.imm(gamma, T) * k.imm(gamma, T) *
+                      og.select(region, k.imm(1, T), k.imm(10, T)),
+                      [og.select(region, k.imm(vplus[i], T), k.imm(vminus[i], T))
+                       for i in range(2)],
+                      k.imm(0.6, T))
+    out_of = ((icoord[0] < 0) | (icoord[1] < 0)) | ((icoord[0] >= isize[0]) |
+                                                    (icoord[1] >= isize[1]))
+    cell = _zip_records([jet, cell0], lambda a, b: og.select(out_of, a, b))
+
+    # CFL (HydroMain.hs:150-154)
+    ts = [dR[i] / (cell.sound + og.abs_(cell.velocity[i])) for i in range(2)]
+    dts = og.min_(ts[0], ts[1])
+    dtG = cflG * k.reduce("min", dts)
+    dt = k.broadcast(dtG)
+
+    def interpolate(order, i, rec):
+        def sh(n):
+            v = [0, 0]
+            v[i] = n
+            return lambda x: k.shift(x, tuple(v))
+        a0, a1, a2, a3 = (_map_record(rec, sh(n)) for n in (2, 1, 0, -1))
+
+        def single(x0, x1, x2, x3):
+            if order == 1:
+                return (x1, x2)
+            d01, d12, d23 = x1 - x0, x2 - x1, x3 - x2
+
+            def absmaller(a, b):
+                return og.select((a * b) <= 0, k.imm(0, T),
+                                 og.select(og.abs_(a) < og.abs_(b), a, b))
+            d1 = absmaller(d01, d12)
+            d2 = absmaller(d12, d23)
+            return (x1 + d1 / 2, x2 - d2 / 2)
+        lr = _zip_records([a0, a1, a2, a3], single)
+        left = _map_record(lr, lambda p: p[0])
+        right = _map_record(lr, lambda p: p[1])
+
+        def bp(x):
+            return _bind_hydro(k, gamma, T, x.density, list(x.velocity), x.pressure)
+        return bp(left), bp(right)
+
+    def hllc(i, left, right):
+        G = lambda: k.imm(gamma, T)
+        dens_mid = (left.density + right.density) / 2
+        sound_mid = (left.sound + right.sound) / 2
+        speed_l, speed_r = left.velocity[i], right.velocity[i]
+        pres_star = og.max_(k.imm(0, T), (left.pressure + right.pressure) / 2 -
+                            dens_mid * sound_mid * (speed_r - speed_l))
+
+        def q(sp, p):
+            return og.select(p <= sp, k.imm(1, T),
+                             og.sqrt(1 + (G() + 1) / (2 * G()) * (sp / p - 1)))
+        shock_l = left.velocity[i] - left.sound * q(pres_star, left.pressure)
+        shock_r = right.velocity[i] + right.sound * q(pres_star, right.pressure)
+        shock_star = ((right.pressure - left.pressure
+                       + left.density * speed_l * (shock_l - speed_l)
+                       - right.density * speed_r * (shock_r - speed_r))
+                      / (left.density * (shock_l - speed_l) -
+                         right.density * (shock_r - speed_r)))
+
+        def star(star_shock, shock, x):
+            speed = x.velocity[i]
+            d = x.density * (shock - speed) / (shock - star_shock)
+            mome = [d * (star_shock if i == j else x.velocity[j]) for j in range(2)]
+            e = d * (x.energy / x.density + (star_shock - speed) *
+                     (star_shock + x.pressure / x.density / (shock - speed)))
+            return _bind_hydro(k, gamma, T, d, mome=mome, enrg=e)
+        lesta = star(shock_star, shock_l, left)
+        rista = star(shock_star, shock_r, right)
+
+        def selector(a, b, c, d):
+            return og.select(0 < shock_l, a,
+                             og.select(0 < shock_star, b, og.select(0 < shock_r, c, d)))
+        return _zip_records([left, lesta, rista, right], selector)
+
+    def add_flux(dt_, dR_, wall, ex, rec):
+        dtdx = dt_ / dR_[ex]
+        left_w = wall[ex]
+        back = [0, 0]
+        back[ex] = -1
+        right_w = _map_record(wall[ex], lambda x: k.shift(x, tuple(back)))
+        dens1 = rec.density + dtdx * (left_w.density_flux[ex] - right_w.density_flux[ex])
+        mome1 = [rec.momentum[j] + dtdx * (left_w.momentum_flux[j][ex] -
+                                           right_w.momentum_flux[j][ex]) for j in range(2)]
+        enrg1 = rec.energy + dtdx * (left_w.energy_flux[ex] - right_w.energy_flux[ex])
+        return _bind_hydro(k, gamma, T, dens1, mome=mome1, enrg=enrg1)
+
+    def proceed_single(order, dt_, dR_, cell_f, cell_s):
+        wall = [hllc(i, *interpolate(order, i, cell_f)) for i in range(2)]
+        # foldl1 (.) over the axes: axis 1 is added first, then axis 0
+        cell_n = add_flux(dt_, dR_, wall, 0, add_flux(dt_, dR_, wall, 1, cell_s))
+        return _bind_hydro(k, gamma, T, og.max_(k.imm(1e-2, T), cell_n.density),
+                           list(cell_n.velocity), og.max_(k.imm(1e-2, T), cell_n.pressure))
+
+    cell2 = proceed_single(1, dt / 2, dR, cell, cell)
+    cell3 = proceed_single(2, dt, dR, cell2, cell)
+    k.store(time_s, timeG + dtG)
+    k.store(dens_s, cell3.density)
+    for i in range(2):
+        k.store(velo_s[i], cell3.velocity[i])
+    k.store(pres_s, cell3.pressure)
+    return om

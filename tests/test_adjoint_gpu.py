@@ -166,3 +166,42 @@ def test_backward_rejects_foreign_tape(om_lib, oracle):
             b.backward(tape, [np.zeros(st[0].shape)] * 4)
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_segment_tapes_match_retaping(om_lib, oracle, monkeypatch, precision):
+    # The backward pass recomputes each segment with the taped step, keeping
+    # one tape per step; when those tapes cannot be allocated it recomputes
+    # with the plain step and tapes each step again before its reverse.  The
+    # taped step writes the same states as the plain one, so both paths give
+    # the same gradient bit for bit.
+    size = (64, 48)
+    steps = 9
+    st = noisy_kh(oracle, size, 21)
+    if precision == 32:
+        st = tuple(a.astype(np.float32) for a in st)
+    rng = np.random.default_rng(5)
+    cot = tuple(rng.standard_normal(a.shape).astype(st[0].dtype) for a in st)
+    grads = []
+    for retape in (False, True):
+        h = make(om_lib, size, precision)
+        h.set_state(st)
+        if retape:
+            monkeypatch.setenv("OM_FAIL_ALLOC_AFTER", "0")
+        tape = h.forward(steps, checkpoint_every=4)
+        monkeypatch.delenv("OM_FAIL_ALLOC_AFTER", raising=False)
+        with tape:
+            grads.append(tape.backward(cot))
+        h.close()
+    for a, b in zip(*grads):
+        assert np.array_equal(a, b)
+
+
+def test_adjoint_step_timers(om_lib, oracle):
+    st = tuple(a.astype(np.float32) for a in noisy_kh(oracle, (128, 96), 4))
+    h = make(om_lib, (128, 96), 32)
+    h.set_state(st)
+    assert h.time_tape(2) > 0 and h.time_vjp(2) > 0
+    for a, b in zip(h.state(), st):            # neither timer moves the handle
+        assert np.array_equal(a, b)
+    h.close()

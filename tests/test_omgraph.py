@@ -74,6 +74,57 @@ def test_life_graph_matches_life_oracle(oracle):
     assert int(m.values["generation"]) == 12
 
 
+HYDRO_FIELDS = ("density", "velocity0", "velocity1", "pressure")
+
+
+def hydro_graph_machine(state, n0, n1, gamma, boundary, typ, cfl):
+    """The numpy oracle on examples/Hydro's OM written in the builder, with
+    the scalars the Hydro drivers set (dR = extent / n, unit extent)."""
+    m = R.Machine(ex.hydro((n0, n1), gamma, boundary, typ).to_text())
+    f = np.float32 if typ == og.Float else np.float64
+    for name, v in (("cfl", f(cfl)), ("dR0", f(1) / f(n0)), ("dR1", f(1) / f(n1)),
+                    ("extent0", f(1)), ("extent1", f(1)), ("time", f(0))):
+        m.values[name] = f(v)
+    for name, a in zip(HYDRO_FIELDS, state):
+        m.values[name] = a.copy()
+    return m
+
+
+@pytest.mark.parametrize("boundary", ["cyclic", "open"])
+def test_hydro_graph_matches_hydro_oracle(oracle, boundary):
+    # the builder's transcription of HydroMain.hs, run by the numpy graph
+    # oracle, against the C restatement of the generated Hydro code (FP64)
+    n0, n1, g = 40, 24, 1.4
+    cyc = boundary == "cyclic"
+    st = (oracle.hydro_init_kh(n0, n1, 5) if cyc else
+          oracle.hydro_init_jet(n0, n1, cyclic=False, gamma=g, dtype=np.float64))
+    m = hydro_graph_machine(st, n0, n1, g, boundary, og.Double, 0.5)
+    assert m.lm == [0, 0] if cyc else m.lm == [3, 3] and m.um == [3, 3]
+    for _ in range(4):
+        m.run("proceed")
+    ref, t, _ = oracle.hydro_run(st, 4, cyclic=cyc, gamma=g, cfl=0.5)
+    for name, a in zip(HYDRO_FIELDS, ref):
+        assert np.array_equal(np.asarray(m.values[name]).reshape(a.shape), a), name
+    assert float(m.values["time"]) == t
+
+
+def test_hydro_graph_matches_reference_golden(oracle):
+    # 1024^2 float, open, gamma 5/3, the generated init, 2 steps: every
+    # memory array bit-identical to the reference's generated float code
+    import hashlib
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                             "hydro_ref_jet.npz"))
+    st = oracle.hydro_init_jet(1024, 1024, cyclic=False, gamma=5 / 3, dtype=np.float32)
+    m = hydro_graph_machine(st, 1024, 1024, 5 / 3, "open", og.Float, float(g["cfl"]))
+    m.run("proceed")
+    m.run("proceed")
+    got = [hashlib.sha256(np.ascontiguousarray(m.values[n]).tobytes()).hexdigest()
+           for n in HYDRO_FIELDS]
+    assert got == [str(s) for s in g["sha256"]]
+    assert np.float32(m.values["time"]) == np.float32(g["times"][-1])
+
+
 def _check(om_lib, text):
     L = om_lib.load_library()
     src = C.c_char_p()

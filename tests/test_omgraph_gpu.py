@@ -161,3 +161,51 @@ def test_generated_source_is_available(om_lib):
     src = g.source
     assert "om_k0_s0" in src and "__global__" in src
     g.close()
+
+
+HYDRO_FIELDS = ("density", "velocity0", "velocity1", "pressure")
+
+
+def hydro_graph(om_lib, state, n0, n1, gamma, boundary, typ, cfl):
+    """examples/Hydro's OM, written in the builder, on the executor, with the
+    scalars the Hydro drivers set (dR = extent / n, unit extent)."""
+    g = om_lib.GraphMachine(ex.hydro((n0, n1), gamma, boundary, typ))
+    f = np.float32 if typ == og.Float else np.float64
+    for name, v in (("cfl", f(cfl)), ("dR0", f(1) / f(n0)), ("dR1", f(1) / f(n1)),
+                    ("extent0", f(1)), ("extent1", f(1)), ("time", f(0))):
+        g.set_scalar(name, float(v))
+    for name, a in zip(HYDRO_FIELDS, state):
+        g.write(name, a)
+    return g
+
+
+def test_hydro_graph_cyclic_fp64_matches_oracle(om_lib, oracle):
+    n0, n1 = 96, 64
+    st = oracle.hydro_init_kh(n0, n1, 3)
+    g = hydro_graph(om_lib, st, n0, n1, 1.4, "cyclic", og.Double, 0.4)
+    g.run("proceed")
+    g.run("proceed", 5)              # five more steps in one captured graph
+    ref, t, _ = oracle.hydro_run(st, 6, cyclic=True, gamma=1.4, cfl=0.4)
+    for name, a in zip(HYDRO_FIELDS, ref):
+        assert np.array_equal(g.read(name), a), name
+    assert g.get_scalar("time") == t
+    g.close()
+
+
+def test_hydro_graph_open_matches_reference_golden(om_lib, oracle):
+    # 1024^2 float, open (3-cell margins found by the executor), gamma 5/3,
+    # 2 steps: bit-identical to the reference's generated float code
+    import hashlib
+    import os
+    gold = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                                "hydro_ref_jet.npz"))
+    st = oracle.hydro_init_jet(1024, 1024, cyclic=False, gamma=5 / 3, dtype=np.float32)
+    g = hydro_graph(om_lib, st, 1024, 1024, 5 / 3, "open", og.Float, float(gold["cfl"]))
+    assert (g.om_lower_margin(0), g.om_upper_margin(1)) == (3, 3)
+    g.run("proceed")
+    g.run("proceed")
+    got = [hashlib.sha256(np.ascontiguousarray(g.read(n)).tobytes()).hexdigest()
+           for n in HYDRO_FIELDS]
+    assert got == [str(s) for s in gold["sha256"]]
+    assert np.float32(g.get_scalar("time")) == np.float32(gold["times"][-1])
+    g.close()
