@@ -9,8 +9,9 @@
 // cell).  It reads the step's tape, written by the forward step itself when
 // it is recomputed from a checkpoint (hydro_fused_tape_kernel: the stage-1
 // state and both stages' flux differences), and runs as three launches over
-// TX x TY tiles whose face work lives in shared memory, so every cotangent
-// is written by exactly one thread, and one single-block launch:
+// TX x TY tiles (the face work of C+D and E+F lives in shared memory, so
+// every cotangent is written by exactly one thread) and one single-block
+// launch:
 //   B    stage-2 update reverse per cell -> conserved cotangent U2b, base
 //        part of the previous-state cotangent, dt partial; minimum CFL
 //        timescale of the state
@@ -56,19 +57,34 @@ template <class R> struct Fields {
 constexpr int kCheapWrap = 40;
 
 // What changes from one adjoint step to the next, read by the kernels from
-// device memory so that one captured graph serves every step: the step's dt
-// and the four arrays of the state before the step.
+// device memory so that one captured graph serves every step: where the
+// step's CFL minimum is (its dt = cfl * minimum, formed in the OM's Real
+// type as the forward step forms it), the four arrays of the state before
+// the step and the step's tape.
 struct StepIn {
-  double dt;
+  const unsigned long long *tsbits;  // CFL minimum of the state (hk::ts_bits)
+  double cfl;
   void *state[4];
   void *tape[20];   // the step's HydroTapeOut: q[4], d1[8], d2[8]
+};
+
+// eight taped arrays of flux differences, D[4 * axis + k] at a cell
+template <class R> struct Diffs {
+  const R *f[8];
+  __device__ __forceinline__ void get(size_t i, R D[8]) const {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) D[k] = f[k][i];
+  }
 };
 
 template <class R> struct Geo {
   int n0, n1;
   R g, dR0, dR1, dt;
-  const StepIn *in;   // this step's dt and state (device memory)
+  const StepIn *in;   // this step's record (device memory)
   int cheap;          // n0, n1 >= kCheapWrap: one add or subtract wraps an index
+  __device__ __forceinline__ R step_dt() const {
+    return (R)in->cfl * hk::ts_from_bits<R>(*in->tsbits);
+  }
   __device__ __forceinline__ Fields<R> state() const {
     return Fields<R>{{(R *)in->state[0], (R *)in->state[1], (R *)in->state[2],
                       (R *)in->state[3]}};
@@ -77,13 +93,16 @@ template <class R> struct Geo {
   __device__ __forceinline__ Fields<R> q() const {
     return Fields<R>{{(R *)in->tape[0], (R *)in->tape[1], (R *)in->tape[2], (R *)in->tape[3]}};
   }
-  __device__ __forceinline__ void d1(size_t i, R D[8]) const {
+  // the arrays of the stage-1 (d1) and stage-2 (d2) flux differences; read
+  // once per kernel (the record is in global memory, so accesses through it
+  // after a store would be reloaded)
+  __device__ __forceinline__ Diffs<R> d1() const { return diffs(4); }
+  __device__ __forceinline__ Diffs<R> d2() const { return diffs(12); }
+  __device__ __forceinline__ Diffs<R> diffs(int first) const {
+    Diffs<R> d;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) D[k] = ((const R *)in->tape[4 + k])[i];
-  }
-  __device__ __forceinline__ void d2(size_t i, R D[8]) const {
-#pragma unroll
-    for (int k = 0; k < 8; ++k) D[k] = ((const R *)in->tape[12 + k])[i];
+    for (int k = 0; k < 8; ++k) d.f[k] = (const R *)in->tape[first + k];
+    return d;
   }
   // periodic index of a cell at most 4 cells (or one tile plus 3 cells)
   // outside the mesh
@@ -135,12 +154,12 @@ __global__ void __launch_bounds__(256)
 adj_update2_rev(Fields<R> Ub, Fields<R> U2b, Fields<R> Pbase, Geo<R> G, double *partial,
                 unsigned long long *minbits) {
   __shared__ double sh[8];
-  G.dt = (R)G.in->dt;
+  G.dt = G.step_dt();
   const Fields<R> P = G.state();
+  const Diffs<R> D2 = G.d2();
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int nt0 = (G.n0 + TX - 1) / TX;
   const int X0 = (int)(blockIdx.x % nt0) * TX, Y0 = (int)(blockIdx.x / nt0) * TY;
-  const R g = G.g;
   const R d0 = G.dt / G.dR0, d1 = G.dt / G.dR1;
   const R rdR0 = R(1) / G.dR0, rdR1 = R(1) / G.dR1;
   double dtb = 0;
@@ -151,24 +170,24 @@ adj_update2_rev(Fields<R> Ub, Fields<R> U2b, Fields<R> Pbase, Geo<R> G, double *
     if (x >= G.n0 || y >= G.n1) continue;
     const size_t gi = (size_t)y * G.n0 + x;
     R D[8];
-    G.d2(gi, D);
+    D2.get(gi, D);
     const Prim<R> b = P.get(gi);
     R u[4];
-    ha::update_cons_d(g, b, d0, d1, D, u);
+    ha::update_cons_d(G.g, b, d0, d1, D, u);
     const Prim<R> qb_ = Ub.get(gi);
     const PrimBar<R> qb{qb_.rho, qb_.v0, qb_.v1, qb_.p};
     R U[4];
-    ha::cons_from_prim_rev(g, u[0], u[1], u[2], u[3], qb, U);
+    ha::cons_from_prim_rev(G.g, u[0], u[1], u[2], u[3], qb, U);
     U2b.set(gi, Prim<R>{U[0], U[1], U[2], U[3]});
     PrimBar<R> bb;
     ha::zero(bb);
-    ha::cons_of_prim_rev(g, b, U, bb);
+    ha::cons_of_prim_rev(G.g, b, U, bb);
     Pbase.set(gi, Prim<R>{bb.rho, bb.v0, bb.v1, bb.p});
     const R t0 = U[0] * D[0] + U[1] * D[1] + U[2] * D[2] + U[3] * D[3];
     const R t1 = U[0] * D[4] + U[1] * D[5] + U[2] * D[6] + U[3] * D[7];
     dtb += (double)(t0 * rdR0 + t1 * rdR1);
     const unsigned long long tb =
-        hk::ts_bits<R>(hs::timescale(g, G.dR0, G.dR1, b.rho, b.v0, b.v1, b.p));
+        hk::ts_bits<R>(hs::timescale(G.g, G.dR0, G.dR1, b.rho, b.v0, b.v1, b.p));
     best = tb < best ? tb : best;
   }
   best = warp_min(best);
@@ -241,8 +260,9 @@ adj_stage2_tile(Fields<R> U2b, Fields<R> U1b, Fields<R> Pbase, Geo<R> G, double 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   S &s = *reinterpret_cast<S *>(smem_raw);
   __shared__ double sh[8];
-  G.dt = (R)G.in->dt;
+  G.dt = G.step_dt();
   const Fields<R> P = G.state(), Q = G.q();
+  const Diffs<R> D1 = G.d1();
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int nt0 = (G.n0 + TX - 1) / TX;
   const int X0 = (int)(blockIdx.x % nt0) * TX, Y0 = (int)(blockIdx.x / nt0) * TY;
@@ -261,7 +281,7 @@ adj_stage2_tile(Fields<R> U2b, Fields<R> U1b, Fields<R> Pbase, Geo<R> G, double 
   __syncthreads();
   const R d0 = G.dt / G.dR0, d1 = G.dt / G.dR1;
   // x faces: face X0-1+j of row Y0+r has stencil box columns j..j+3 of box
-  // row r+3 and cells (right, left) at U2b box columns j+1, j of row r+2
+  // row r+3 and cells (right, left) at stage-2 cotangent box columns j+1, j of row r+2
   for (int i = tid; i < TY * S::XF; i += nthr) {
     const int r = i / S::XF, j = i - r * S::XF;
     Prim<R> st[4];
@@ -291,7 +311,7 @@ adj_stage2_tile(Fields<R> U2b, Fields<R> U1b, Fields<R> Pbase, Geo<R> G, double 
   }
   __syncthreads();
   // y faces: face Y0-1+j of column X0+r has stencil box rows j..j+3 of box
-  // column r+3 and cells at U2b box rows j+1, j of column r+2
+  // column r+3 and cells at stage-2 cotangent box rows j+1, j of column r+2
   for (int i = tid; i < S::YF * TX; i += nthr) {
     const int j = i / TX, r = i - j * TX;
     Prim<R> st[4];
@@ -327,7 +347,7 @@ adj_stage2_tile(Fields<R> U2b, Fields<R> U1b, Fields<R> Pbase, Geo<R> G, double 
     }
     const size_t gi = (size_t)y * G.n0 + x;
     R D[8];
-    G.d1(gi, D);
+    D1.get(gi, D);
     const Prim<R> b = P.get(gi);
     R u[4];
     ha::update_cons_d(G.g, b, e0, e1, D, u);
@@ -367,7 +387,7 @@ adj_stage1_tile(Fields<R> U1b, Fields<R> Pbase, Fields<R> Pb, Geo<R> G,
                 const unsigned long long *minbits, unsigned long long *argmin) {
   using S = Stage1Smem<R, TX, TY>;
   __shared__ S s;
-  G.dt = (R)G.in->dt;
+  G.dt = G.step_dt();
   const Fields<R> P = G.state();
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int nt0 = (G.n0 + TX - 1) / TX;
@@ -491,21 +511,20 @@ struct StepTape {
   }
 };
 
+// the 20 arrays of a tape share one allocation (p[0] is its base)
 static void tape_free(StepTape *t) {
-  for (void *&q : t->p) {
-    if (q) cudaFree(q);
-    q = nullptr;
-  }
+  if (t->p[0]) cudaFree(t->p[0]);
+  for (void *&q : t->p) q = nullptr;
 }
 
 static bool tape_alloc(size_t bytes, StepTape *t) {
-  for (void *&q : t->p)
-    if (cudaMalloc(&q, bytes) != cudaSuccess) {
-      q = nullptr;
-      cudaGetLastError();
-      tape_free(t);
-      return false;
-    }
+  const size_t pitch = (bytes + 255) / 256 * 256;
+  char *base = nullptr;
+  if (cudaMalloc(&base, pitch * 20) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  for (int k = 0; k < 20; ++k) t->p[k] = base + pitch * k;
   return true;
 }
 
@@ -647,13 +666,57 @@ static om_status vjp_kernels(Handle *h, AdjointScratch *s, void *const *ub, void
   return OM_OK;
 }
 
+// One taped forward step between explicit buffers, in[4] -> out[4], with the
+// adjoint's own scalar block s->sc: dt from s->sc->tsmin[read_slot], the CFL
+// minimum of out into s->sc->tsmin[1 - read_slot].
+static om_status launch_tape(Handle *h, AdjointScratch *s, void *const *in, void *const *out,
+                             int read_slot, const HydroTapeOut &t) {
+  HydroStepArgs a;
+  a.rho = in[0]; a.v0 = in[1]; a.v1 = in[2]; a.p = in[3];
+  a.nrho = out[0]; a.nv0 = out[1]; a.nv1 = out[2]; a.np = out[3];
+  a.n0 = h->size[0]; a.n1 = h->size[1];
+  a.nt0 = 0;
+  a.gamma = h->cfg.gamma;
+  a.sc = s->sc;
+  a.read_slot = read_slot;
+  a.dt_hist = s->dt_scratch;
+  a.lm = 0;
+  a.ms0 = h->size[0];
+  a.margin_min = nullptr;
+  OM_CUDA_CHECK(cudaMemsetAsync(&s->sc->tsmin[1 - read_slot], 0xFF, sizeof(unsigned long long),
+                                h->stream));
+  const cudaError_t e = hydro_fused_tape(s->fp64, h->cfg.variant == 2, a, t, h->stream);
+  if (e != cudaSuccess) {
+    set_error(std::string("Hydro taped step: ") + cudaGetErrorString(e));
+    return OM_ERR_CUDA;
+  }
+  h->launches++;
+  return OM_OK;
+}
+
+// s->sc becomes a copy of the handle's scalar block with the CFL minimum of
+// the handle's current state in tsmin[0].
+static om_status load_scalars(Handle *h, AdjointScratch *s) {
+  unsigned long long *ts = nullptr;
+  OM_TRY(hydro_tsmin_device(h, &ts));
+  OM_CUDA_CHECK(cudaMemcpyAsync(s->sc, h->d_scalars, sizeof(HydroScalars),
+                                cudaMemcpyDeviceToDevice, h->stream));
+  OM_CUDA_CHECK(cudaMemcpyAsync(&s->sc->tsmin[0], ts, sizeof(unsigned long long),
+                                cudaMemcpyDeviceToDevice, h->stream));
+  return OM_OK;
+}
+
 // The taped step of the handle's current state into s->tape1 (the handle
 // does not move) and the record of that step in *in.
 static om_status tape_current(Handle *h, AdjointScratch *s, adj::StepIn *in) {
-  unsigned long long bits;
-  OM_TRY(hydro_current_dt(h, &in->dt, &bits));
-  for (int k = 0; k < 4; ++k) in->state[k] = h->arrays[k].d();
-  OM_TRY(hydro_tape_step(h, s->next, s->sc, s->dt_scratch, s->tape1.out()));
+  for (int k = 0; k < 4; ++k) OM_TRY(bring_device(h, h->arrays[k]));
+  OM_TRY(load_scalars(h, s));
+  void *cur[4];
+  for (int k = 0; k < 4; ++k) cur[k] = h->arrays[k].d();
+  OM_TRY(launch_tape(h, s, cur, s->next, 0, s->tape1.out()));
+  in->tsbits = &s->sc->tsmin[0];
+  in->cfl = ((HydroScalars *)h->h_scalars)->cfl;
+  for (int k = 0; k < 4; ++k) in->state[k] = cur[k];
   for (int k = 0; k < 20; ++k) in->tape[k] = s->tape1.p[k];
   return OM_OK;
 }
@@ -714,16 +777,17 @@ struct om_hydro_tape_s {
   Handle *h = nullptr;
   int steps = 0, seg = 0, nck = 0;
   std::vector<HydroCheckpoint> ck;     // state before segment j, and the final state
-  std::vector<HydroCheckpoint> segst;  // states of one recomputed segment
+  std::vector<HydroCheckpoint> segst;  // states of one recomputed segment (1 .. seg-1)
   std::vector<StepTape> tapes;         // tapes of one recomputed segment (empty:
                                        // each step is taped again before its reverse)
-  std::vector<HydroTapeOut> outs;      // their records, alive while steps launch
   adj::StepIn *h_in = nullptr;         // pinned: one record per step
+  unsigned long long *d_ts = nullptr;  // CFL minimum of each step's state
   ~om_hydro_tape_s() {
     for (auto &c : ck) hydro_checkpoint_free(&c);
     for (auto &c : segst) hydro_checkpoint_free(&c);
     for (auto &t : tapes) tape_free(&t);
     if (h_in) cudaFreeHost(h_in);
+    cudaFree(d_ts);
   }
 };
 
@@ -786,8 +850,8 @@ extern "C" om_status om_hydro_forward(om_handle H, int steps, int checkpoint_eve
   };
   for (auto &c : t->ck)
     if ((status = hydro_checkpoint_alloc(h, &c)) != OM_OK) return fail(status);
-  for (auto &c : t->segst)
-    if ((status = hydro_checkpoint_alloc(h, &c)) != OM_OK) return fail(status);
+  for (int m = 1; m < t->seg; ++m)  // a segment's first state is its checkpoint
+    if ((status = hydro_checkpoint_alloc(h, &t->segst[m])) != OM_OK) return fail(status);
   {
     // one tape per step of a segment when they fit in half the free memory;
     // otherwise each step is taped again right before its reverse
@@ -805,12 +869,11 @@ extern "C" om_status om_hydro_forward(om_handle H, int steps, int checkpoint_eve
           t->tapes.clear();
           break;
         }
-      for (auto &tp : t->tapes) t->outs.push_back(tp.out());
     }
   }
-  if (cudaMallocHost(&t->h_in, sizeof(adj::StepIn) * (size_t)steps) != cudaSuccess) {
+  if (cudaMallocHost(&t->h_in, sizeof(adj::StepIn) * (size_t)steps) != cudaSuccess ||
+      cudaMalloc(&t->d_ts, sizeof(unsigned long long) * (size_t)steps) != cudaSuccess) {
     cudaGetLastError();
-    t->h_in = nullptr;
     set_error("om_hydro_forward: allocation failed");
     return fail(OM_ERR_NOMEM);
   }
@@ -828,13 +891,14 @@ extern "C" om_status om_hydro_forward(om_handle H, int steps, int checkpoint_eve
 
 // Backward over the tape from the final-state cotangent already in s->ub.
 // On return result[4] holds the arrays (s->ub or s->pb) with the cotangent
-// of the tape's start state; the handle is at the final state.  Every copy
-// and kernel runs on the handle's stream, so a segment buffer is refilled
-// only after the steps that read it.
-static om_status backward_core(om_handle H, om_hydro_tape t, AdjointScratch *s, void **result) {
+// of the tape's start state; the handle is at the final state.  Each
+// segment is recomputed from its checkpoint with the taped step, state to
+// state on the device (no host round trip), keeping every step's CFL
+// minimum, then walked backwards.  Every copy and kernel runs on the
+// handle's stream, so a buffer is refilled only after the steps that read
+// it.
+static om_status backward_core(om_hydro_tape t, AdjointScratch *s, void **result) {
   Handle *h = t->h;
-  int kid = -1;
-  OM_TRY(om_kernel_id(H, "proceed", &kid));
   void *ub[4], *pb[4];
   for (int k = 0; k < 4; ++k) {
     ub[k] = s->ub[k];
@@ -844,32 +908,29 @@ static om_status backward_core(om_handle H, om_hydro_tape t, AdjointScratch *s, 
   for (int j = t->nck - 1; j >= 0; --j) {
     const int len = std::min(t->seg, t->steps - j * t->seg);
     const bool taped = (int)t->tapes.size() >= len;
-    // recompute the segment from its checkpoint with the taped step,
-    // keeping every state
     OM_TRY(hydro_restore(h, &t->ck[j]));
+    OM_TRY(load_scalars(h, s));
     for (int m = 0; m < len; ++m) {
-      adj::StepIn &in = t->h_in[j * t->seg + m];
-      unsigned long long bits;
-      OM_TRY(hydro_save(h, &t->segst[m]));
-      OM_TRY(hydro_current_dt(h, &in.dt, &bits));
-      for (int k = 0; k < 4; ++k) in.state[k] = t->segst[m].f[k];
-      if (taped) {
-        for (int k = 0; k < 20; ++k) in.tape[k] = t->tapes[m].p[k];
-        hydro_set_tape(h, &t->outs[m]);
-        const om_status r = om_run(H, kid);
-        hydro_set_tape(h, nullptr);
-        OM_TRY(r);
-      } else {
-        OM_TRY(om_run(H, kid));
-      }
+      const int k = j * t->seg + m;
+      adj::StepIn &in = t->h_in[k];
+      void *const *cur = m == 0 ? t->ck[j].f : t->segst[m].f;
+      void *const *nxt = m + 1 < len ? t->segst[m + 1].f : s->next;
+      OM_CUDA_CHECK(cudaMemcpyAsync(&t->d_ts[k], &s->sc->tsmin[m & 1], sizeof(unsigned long long),
+                                    cudaMemcpyDeviceToDevice, h->stream));
+      in.tsbits = &t->d_ts[k];
+      in.cfl = cfl;
+      for (int q = 0; q < 4; ++q) in.state[q] = cur[q];
+      const StepTape &tp = taped ? t->tapes[m] : s->tape1;
+      for (int q = 0; q < 20; ++q) in.tape[q] = tp.p[q];
+      OM_TRY(launch_tape(h, s, cur, nxt, m & 1, tp.out()));
     }
     for (int m = len - 1; m >= 0; --m) {
       adj::StepIn &in = t->h_in[j * t->seg + m];
       if (!taped) {
-        // tape this step again from its saved state (one tape buffer)
-        OM_TRY(hydro_restore(h, &t->segst[m]));
-        OM_TRY(hydro_tape_step(h, s->next, s->sc, s->dt_scratch, s->tape1.out()));
-        for (int k = 0; k < 20; ++k) in.tape[k] = s->tape1.p[k];
+        // one tape buffer: tape this step again from its kept state
+        OM_CUDA_CHECK(cudaMemcpyAsync(&s->sc->tsmin[0], in.tsbits, sizeof(unsigned long long),
+                                      cudaMemcpyDeviceToDevice, h->stream));
+        OM_TRY(launch_tape(h, s, in.state, s->next, 0, s->tape1.out()));
       }
       OM_TRY(run_vjp_step(h, s, &in, ub, pb, cfl));
       for (int k = 0; k < 4; ++k) std::swap(ub[k], pb[k]);
@@ -895,7 +956,7 @@ extern "C" om_status om_hydro_backward(om_handle H, om_hydro_tape t, const void 
   for (int k = 0; k < 4; ++k)
     OM_CUDA_CHECK(cudaMemcpyAsync(s->ub[k], cot_final[k], bytes, cudaMemcpyDefault, h->stream));
   void *res[4];
-  om_status status = backward_core(H, t, s, res);
+  om_status status = backward_core(t, s, res);
   if (status != OM_OK) {
     hydro_restore(h, &t->ck[t->nck]);
     return status;
@@ -965,7 +1026,7 @@ extern "C" om_status om_hydro_adjoint_run(om_handle H, int steps, const void *ta
     if (loss) *loss = l / (double)cells;
   }
   void *res[4];
-  if ((status = backward_core(H, t, sc, res)) != OM_OK) {
+  if ((status = backward_core(t, sc, res)) != OM_OK) {
     hydro_restore(h, &t->ck[t->nck]);
     return done(status);
   }
@@ -1037,8 +1098,9 @@ extern "C" om_status om_hydro_time_tape(om_handle H, int reps, float *ms) {
   const int fp64 = h->cfg.precision == 64;
   AdjointScratch *s;
   OM_TRY(get_scratch(h, fp64, &s));
+  adj::StepIn rec;
+  OM_TRY(tape_current(h, s, &rec));  // warms up, and loads s->sc
   const HydroTapeOut out = s->tape1.out();
-  OM_TRY(hydro_tape_step(h, s->next, s->sc, s->dt_scratch, out));
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   om_status st = OM_OK;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess ||
@@ -1047,7 +1109,7 @@ extern "C" om_status om_hydro_time_tape(om_handle H, int reps, float *ms) {
     st = OM_ERR_CUDA;
   }
   for (int r = 0; st == OM_OK && r < reps; ++r)
-    st = hydro_tape_step(h, s->next, s->sc, s->dt_scratch, out);
+    st = launch_tape(h, s, rec.state, s->next, 0, out);
   if (st == OM_OK && (cudaEventRecord(e1, h->stream) != cudaSuccess ||
                       cudaEventSynchronize(e1) != cudaSuccess ||
                       cudaEventElapsedTime(ms, e0, e1) != cudaSuccess)) {

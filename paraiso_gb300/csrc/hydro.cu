@@ -43,7 +43,6 @@ struct HydroState {
   unsigned long long *d_min = nullptr, *h_min = nullptr;  // plain path reduce result
   double *d_partials = nullptr, *d_totals = nullptr, *h_totals = nullptr;
   int totals_blocks = 1024;
-  const HydroTapeOut *tape = nullptr;  // set: the next single step writes this tape
 };
 
 static HydroState *hst(Handle *h) { return (HydroState *)h->impl; }
@@ -149,11 +148,8 @@ static om_status proceed_fused(Handle *h, int n) {
     a.ms0 = (int)h->memory_size(0);
     a.margin_min = st->d_margin;
     cudaEvent_t ev = prof_begin(h);
-    cudaError_t e =
-        (st->tape && n == 1 && st->lm == 0)
-            ? hydro_fused_tape(st->fp64, st->variant == 2, a, *st->tape, h->stream)
-        : st->fp64 ? hydro_fused_f64(a, st->tile, h->stream, nullptr)
-                   : hydro_fused_f32(a, st->tile, st->variant == 2, h->stream, nullptr);
+    cudaError_t e = st->fp64 ? hydro_fused_f64(a, st->tile, h->stream, nullptr)
+                             : hydro_fused_f32(a, st->tile, st->variant == 2, h->stream, nullptr);
     if (e != cudaSuccess) {
       set_error(std::string("Hydro fused step: ") + cudaGetErrorString(e));
       return OM_ERR_CUDA;
@@ -282,46 +278,12 @@ static void hydro_free(Handle *h) {
   h->impl = nullptr;
 }
 
-// the next single fused step also writes `tape` (nullptr: no tape)
-void hydro_set_tape(Handle *h, const HydroTapeOut *tape) { hst(h)->tape = tape; }
-
-// One taped step from the handle's current state into out[4], leaving the
-// handle as it is: the kernel reads the current CFL minimum and updates a
-// copy of the scalar block (sc_scratch) and dt_scratch instead of the
-// handle's.
-om_status hydro_tape_step(Handle *h, void *const *out, HydroScalars *sc_scratch,
-                          double *dt_scratch, const HydroTapeOut &tape) {
-  HydroState *st = hst(h);
-  if (st->lm > 0 || st->variant == 1) {
-    set_error("Hydro tape: periodic grids on the fused path only");
-    return OM_ERR_UNSUPPORTED;
-  }
+// the device address of the CFL minimum of the current state (computed
+// first if the cached one does not belong to it)
+om_status hydro_tsmin_device(Handle *h, unsigned long long **ptr) {
   OM_TRY(upload_scalars(h));
-  for (int i = 0; i < 4; ++i) OM_TRY(bring_device(h, h->arrays[i]));
   OM_TRY(ensure_tsmin(h));
-  OM_CUDA_CHECK(cudaMemcpyAsync(sc_scratch, hsc_dev(h), sizeof(HydroScalars),
-                                cudaMemcpyDeviceToDevice, h->stream));
-  OM_CUDA_CHECK(cudaMemsetAsync(&sc_scratch->tsmin[1 - st->slot], 0xFF,
-                                sizeof(unsigned long long), h->stream));
-  HydroStepArgs a;
-  a.rho = h->arrays[0].d(); a.v0 = h->arrays[1].d();
-  a.v1 = h->arrays[2].d(); a.p = h->arrays[3].d();
-  a.nrho = out[0]; a.nv0 = out[1]; a.nv1 = out[2]; a.np = out[3];
-  a.n0 = h->size[0]; a.n1 = h->size[1];
-  a.nt0 = 0;
-  a.gamma = h->cfg.gamma;
-  a.sc = sc_scratch;
-  a.read_slot = st->slot;
-  a.dt_hist = dt_scratch;
-  a.lm = 0;
-  a.ms0 = (int)h->memory_size(0);
-  a.margin_min = nullptr;
-  const cudaError_t e = hydro_fused_tape(st->fp64, st->variant == 2, a, tape, h->stream);
-  if (e != cudaSuccess) {
-    set_error(std::string("Hydro taped step: ") + cudaGetErrorString(e));
-    return OM_ERR_CUDA;
-  }
-  h->launches++;
+  *ptr = &hsc_dev(h)->tsmin[hst(h)->slot];
   return OM_OK;
 }
 
@@ -380,22 +342,23 @@ static void hydro_load_state(Handle *h, const void *in, size_t n) {
   st->ts_ext1 = k.ts_ext1;
 }
 
+// the four arrays of a checkpoint share one allocation (f[0] is its base)
 om_status hydro_checkpoint_alloc(Handle *h, HydroCheckpoint *c) {
   const size_t bytes = h->memory_size_total() * h->arrays[0].elem_size;
-  for (int i = 0; i < 4; ++i)
-    if (cudaMalloc(&c->f[i], bytes) != cudaSuccess) {
-      cudaGetLastError();
-      set_error("Hydro checkpoint allocation failed");
-      return OM_ERR_NOMEM;
-    }
+  const size_t pitch = (bytes + 255) / 256 * 256;
+  char *base = nullptr;
+  if (cudaMalloc(&base, pitch * 4) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("Hydro checkpoint allocation failed");
+    return OM_ERR_NOMEM;
+  }
+  for (int i = 0; i < 4; ++i) c->f[i] = base + pitch * i;
   return OM_OK;
 }
 
 void hydro_checkpoint_free(HydroCheckpoint *c) {
-  for (int i = 0; i < 4; ++i) {
-    if (c->f[i]) cudaFree(c->f[i]);
-    c->f[i] = nullptr;
-  }
+  if (c->f[0]) cudaFree(c->f[0]);
+  for (int i = 0; i < 4; ++i) c->f[i] = nullptr;
 }
 
 om_status hydro_save(Handle *h, HydroCheckpoint *c) {
@@ -414,6 +377,9 @@ om_status hydro_save(Handle *h, HydroCheckpoint *c) {
 
 om_status hydro_restore(Handle *h, const HydroCheckpoint *c) {
   const size_t bytes = h->memory_size_total() * h->arrays[0].elem_size;
+  // the host scalar block is pinned: a copy from it that is still queued
+  // reads it when it runs, so it is rewritten only once the stream is idle
+  OM_CUDA_CHECK(cudaStreamSynchronize(h->stream));
   for (int i = 0; i < 4; ++i) {
     OM_CUDA_CHECK(cudaMemcpyAsync(h->arrays[i].d(), c->f[i], bytes, cudaMemcpyDeviceToDevice,
                                   h->stream));

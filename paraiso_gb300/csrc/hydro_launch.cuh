@@ -82,12 +82,8 @@ om_status hydro_save(Handle *h, HydroCheckpoint *c);
 om_status hydro_restore(Handle *h, const HydroCheckpoint *c);
 // dt of the next step and the CFL minimum bits of the current state
 om_status hydro_current_dt(Handle *h, double *dt, unsigned long long *bits);
-// the next single fused step of h also writes `tape` (nullptr: none); the
-// record must stay valid until that step has been launched
-void hydro_set_tape(Handle *h, const HydroTapeOut *tape);
-// one taped step from h's current state into out[4]; h is left unchanged
-// (the step's scalar updates go to sc_scratch and dt_scratch)
-om_status hydro_tape_step(Handle *h, void *const *out, HydroScalars *sc_scratch,
-                          double *dt_scratch, const HydroTapeOut &tape);
+// the device address of the CFL minimum of h's current state (computed first
+// when the cached one does not belong to it)
+om_status hydro_tsmin_device(Handle *h, unsigned long long **ptr);
 
 }  // namespace om

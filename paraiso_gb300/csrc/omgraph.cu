@@ -345,6 +345,11 @@ static std::string lit(Type t, const std::string &s) {
   return t == TFloat ? std::string("((float)") + buf + ")" : std::string("(") + buf + ")";
 }
 
+// A stage whose per-cell code has at most kMaxVectorStatements statements
+// evaluates kCellsPerThread cells per thread.
+constexpr int kCellsPerThread = 4;
+constexpr int kMaxVectorStatements = 400;
+
 // Emits the statements computing (node, offset) values of one kernel, each
 // once, into a block of code.
 class Emitter {
@@ -417,16 +422,33 @@ class Emitter {
     return "((" + x + " % " + N + " + " + N + ") % " + N + ")";
   }
 
-  std::string addr(int o0, int o1) const {
-    std::string x, y;
-    if (L_.open) {
-      x = "(c0 + (" + std::to_string(o0) + "))";
-      y = "(c1 + (" + std::to_string(o1) + "))";
-    } else {
-      x = wrap("c0", o0, L_.ms[0]);
-      y = wrap("c1", o1, L_.ms[1]);
-    }
-    return "(long long)" + y + " * " + std::to_string(L_.ms[0]) + " + " + x;
+  // the column c0 + o (wrapped on a cyclic mesh) and the memory offset of
+  // row c1 + o, each declared once per cell and shared by every load
+  std::string col(int o) {
+    if (o == 0) return "c0";
+    auto it = cols_.find(o);
+    if (it != cols_.end()) return it->second;
+    const std::string name = "x" + off_name(o);
+    const std::string e =
+        L_.open ? "(c0 + (" + std::to_string(o) + "))" : wrap("c0", o, L_.ms[0]);
+    code += "      const int " + name + " = " + e + ";\n";
+    return cols_[o] = name;
+  }
+
+  std::string row(int o) {
+    auto it = rows_.find(o);
+    if (it != rows_.end()) return it->second;
+    const std::string name = "y" + off_name(o);
+    const std::string r =
+        L_.open ? "(c1 + (" + std::to_string(o) + "))" : wrap("c1", o, L_.ms[1]);
+    code += "      const long long " + name + " = (long long)" + r + " * " +
+            std::to_string(L_.ms[0]) + ";\n";
+    return rows_[o] = name;
+  }
+
+  std::string addr(int o0, int o1) {
+    const std::string y = row(o1);
+    return y + " + " + col(o0);
   }
 
   std::string scalar_read(const StaticDef &s) const {
@@ -472,6 +494,7 @@ class Emitter {
   const Layout &L_;
   const std::map<int, int> &slots_;
   std::map<std::tuple<int, int, int>, std::string> memo_;
+  std::map<int, std::string> cols_, rows_;
 };
 
 static std::string region_test(const Region &r, const Layout &L) {
@@ -589,12 +612,6 @@ static std::string generate(const Graph &g, const Layout &L, std::vector<KernelP
         const Node &n = k.node(sp.reduces[r]);
         src << "  " << ctype(n.type) << " acc" << r << " = " << ident(n.type, n.sarg) << ";\n";
       }
-      src << "  const long long N = (long long)" << L.ms[0] << " * " << L.ms[1] << ";\n"
-          << "  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < N;\n"
-          << "       i += (long long)gridDim.x * blockDim.x) {\n"
-          << "    const int c0 = (int)(i % " << L.ms[0] << "), c1 = (int)(i / " << L.ms[0]
-          << ");\n"
-          << "    (void)c0; (void)c1;\n";
       // one evaluation block for the whole stage when every store and reduce
       // of it has the same region (always so on a cyclic mesh): the values
       // they share are computed once per cell
@@ -605,20 +622,51 @@ static std::string generate(const Graph &g, const Layout &L, std::vector<KernelP
       for (const std::string &t : tests) one_region = one_region && t == tests[0];
       bool all_cells = true;
       for (int id : sp.reduces) all_cells = all_cells && region_is_all(reg[k.at.at(k.node(id).args[0])], L);
-      if (one_region && all_cells && tests[0] == "true") {
+      const bool shared = one_region && all_cells && tests[0] == "true";
+      // cells per thread: a thread evaluates V neighbouring cells of a row as
+      // offsets 0 .. V-1 of its first one, so loads they share are made once
+      // and V cells' loads are in flight together (small stages on rows that
+      // are whole multiples of 256 V cells)
+      int V = 1;
+      if (shared && L.ms[0] % (256 * kCellsPerThread) == 0) {
+        Emitter trial(g, k, L, slots);
+        for (int s : sp.stores) trial.value(k.stores[s].node, 0, 0);
+        for (int id : sp.reduces) trial.value(k.node(id).args[0], 0, 0);
+        if (std::count(trial.code.begin(), trial.code.end(), '\n') <= kMaxVectorStatements)
+          V = kCellsPerThread;
+      }
+      // work items: chunks of 256 V cells of a memory row, rows in order; a
+      // block takes items blockIdx.x, blockIdx.x + gridDim.x, ...
+      const int chunk = 256 * V;
+      src << "  constexpr int CX = " << (L.ms[0] + chunk - 1) / chunk << ";\n"
+          << "  const long long NW = (long long)" << L.ms[1] << " * CX;\n"
+          << "  for (long long w = blockIdx.x; w < NW; w += gridDim.x) {\n"
+          << "    const int c1 = (int)(w / CX);\n"
+          << "    const int c0 = (int)(w - (long long)c1 * CX) * " << chunk << " + (int)threadIdx.x";
+      if (V > 1) src << " * " << V;
+      src << ";\n";
+      if (V == 1) src << "    if (c0 >= " << L.ms[0] << ") continue;\n";
+      src << "    const long long i = (long long)c1 * " << L.ms[0] << " + c0;\n"
+          << "    (void)c0; (void)c1;\n";
+      if (shared) {
         Emitter e(g, k, L, slots);
         std::vector<std::string> vals;
-        for (int s : sp.stores) vals.push_back(e.value(k.stores[s].node, 0, 0));
-        for (int id : sp.reduces) vals.push_back(e.value(k.node(id).args[0], 0, 0));
+        for (int c = 0; c < V; ++c) {
+          for (int s : sp.stores) vals.push_back(e.value(k.stores[s].node, c, 0));
+          for (int id : sp.reduces) vals.push_back(e.value(k.node(id).args[0], c, 0));
+        }
         src << "    {\n" << e.code;
         size_t v = 0;
-        for (int s : sp.stores)
-          src << "      ((" << ctype(k.node(k.stores[s].node).type) << " *)P.nxt["
-              << em.array_index(k.stores[s].stat) << "])[i] = " << vals[v++] << ";\n";
-        for (size_t r = 0; r < sp.reduces.size(); ++r) {
-          const std::string acc = "acc" + std::to_string(r);
-          src << "      " << acc << " = " << combine(k.node(sp.reduces[r]).sarg, acc, vals[v++])
-              << ";\n";
+        for (int c = 0; c < V; ++c) {
+          const std::string at = c == 0 ? "i" : "i + " + std::to_string(c);
+          for (int s : sp.stores)
+            src << "      ((" << ctype(k.node(k.stores[s].node).type) << " *)P.nxt["
+                << em.array_index(k.stores[s].stat) << "])[" << at << "] = " << vals[v++] << ";\n";
+          for (size_t r = 0; r < sp.reduces.size(); ++r) {
+            const std::string acc = "acc" + std::to_string(r);
+            src << "      " << acc << " = " << combine(k.node(sp.reduces[r]).sarg, acc, vals[v++])
+                << ";\n";
+          }
         }
         src << "    }\n";
       } else {

@@ -90,9 +90,9 @@ def test_life_graph_open(om_lib, oracle):
     g.close()
 
 
-def semantics_graph(boundary):
+def semantics_graph(boundary, size=(61, 37)):
     """Every operation of the format, several types, two reduce stages."""
-    om = og.OM("Sem", (61, 37), boundary)
+    om = og.OM("Sem", size, boundary)
     f = om.static_array("f", og.Float)
     d = om.static_array("d", og.Double)
     i = om.static_array("i", og.Int)
@@ -130,7 +130,8 @@ def semantics_graph(boundary):
     # second stage: a reduce result broadcast back into an array
     k2 = om.kernel("center")
     fv2 = k2.load(f)
-    k2.store(f, fv2 - k2.broadcast(k2.reduce("sum", fv2) / k2.imm(61.0 * 37, og.Float, "scalar")))
+    k2.store(f, fv2 - k2.broadcast(k2.reduce("sum", fv2) /
+                                   k2.imm(float(size[0] * size[1]), og.Float, "scalar")))
     k2.store(s_flag, k2.reduce("max", og.cast(k2.load(b), og.Int)).eq(k2.imm(1, og.Int, "scalar")))
     return om
 
@@ -208,4 +209,36 @@ def test_hydro_graph_open_matches_reference_golden(om_lib, oracle):
            for n in HYDRO_FIELDS]
     assert got == [str(s) for s in gold["sha256"]]
     assert np.float32(g.get_scalar("time")) == np.float32(gold["times"][-1])
+    g.close()
+
+
+def test_life_graph_four_cells_per_thread(om_lib, oracle):
+    # rows of 2048 cells: each thread of the stage evaluates four neighbouring
+    # cells (the generated source says so); results equal the Life oracle
+    a = oracle.life_bernoulli(2048, 40, 9, 0.3)
+    g = om_lib.GraphMachine(ex.life((2048, 40)))
+    assert "threadIdx.x * 4" in g.source
+    g.write("cell", a)
+    g.run("proceed", 12)
+    ref, pops = oracle.life_run(a, 12, cyclic=True)
+    assert np.array_equal(g.read("cell"), ref)
+    assert g.get_scalar("population") == int(pops[-1])
+    g.close()
+
+
+@pytest.mark.parametrize("boundary", ["cyclic", "open"])
+def test_semantics_graph_long_rows(om_lib, boundary):
+    # the operation mix on rows of 1024 cells (several cells per thread where
+    # the stage allows it)
+    om = semantics_graph(boundary, (1024, 9))
+    m0 = R.Machine(om.to_text())
+    rng = np.random.default_rng(12)
+    shape = m0.shape
+    init = {"f": rng.standard_normal(shape).astype(np.float32),
+            "d": rng.standard_normal(shape),
+            "i": rng.integers(-1000, 1000, shape).astype(np.int32),
+            "b": rng.random(shape) < 0.5}
+    g, m = both(om_lib, om, ["step"], init=init)
+    assert_same(g, m, ["i", "b", "smin", "ssum", "f"])
+    assert_same(g, m, ["d", "smax"], rtol=1e-12)
     g.close()
