@@ -8,15 +8,13 @@
 // step (dt = cfl * min timescale: its cotangent is routed to the arg-min
 // cell).  It reads the step's tape, written by the forward step itself when
 // it is recomputed from a checkpoint (hydro_fused_tape_kernel: the stage-1
-// state and both stages' flux differences), and runs as three launches over
-// TX x TY tiles (the face work of C+D and E+F lives in shared memory, so
-// every cotangent is written by exactly one thread) and one single-block
-// launch:
-//   B    stage-2 update reverse per cell -> conserved cotangent U2b, base
-//        part of the previous-state cotangent, dt partial; minimum CFL
-//        timescale of the state
-//   C+D  stage-2 walls reverse (HLLC, MUSCL, per stencil slot in shared
-//        memory), gather into the stage-1 cotangent, stage-1 update reverse
+// state and both stages' flux differences), and runs as two launches over
+// TX x TY tiles whose face work lives in shared memory, so every cotangent
+// is written by exactly one thread, and one single-block launch:
+//   B-D  stage-2 update reverse on the tile and a 2-cell halo, stage-2 walls
+//        reverse (HLLC, MUSCL, per stencil slot in shared memory), gather
+//        into the stage-1 cotangent, stage-1 update reverse; base part of the
+//        previous-state cotangent, dt partial and minimum CFL timescale
 //   E+F  stage-1 walls reverse and gather into the previous-state cotangent;
 //        arg-min of the timescale
 //   G    dt cotangent (partials summed in a fixed order) to the arg-min cell
@@ -65,7 +63,20 @@ struct StepIn {
   const unsigned long long *tsbits;  // CFL minimum of the state (hk::ts_bits)
   double cfl;
   void *state[4];
-  void *tape[20];   // the step's HydroTapeOut: q[4], d1[8], d2[8]
+  void *tape[24];   // the step's HydroTapeOut: q[4], d1[8], d2[8], u2[4]
+  // the reverse step run just before this one (the step after it in time)
+  // left its dt cotangent pending: it is added to this step's incoming
+  // cotangent at that step's arg-min cell, whose state is prev_state
+  int has_prev;
+  void *prev_state[4];
+};
+
+// Where the pending dt cotangent of the previous reverse step is: its block
+// partials (summed in a fixed order) and its arg-min cell.
+struct PendingDt {
+  const double *partials;
+  int nparts;
+  const unsigned long long *argmin;
 };
 
 // eight taped arrays of flux differences, D[4 * axis + k] at a cell
@@ -89,9 +100,14 @@ template <class R> struct Geo {
     return Fields<R>{{(R *)in->state[0], (R *)in->state[1], (R *)in->state[2],
                       (R *)in->state[3]}};
   }
-  // the tape: stage-1 state, stage-1 and stage-2 flux differences
+  // the tape: stage-1 state, stage-1 and stage-2 flux differences, the
+  // stage-2 conserved state before the primitive recovery
   __device__ __forceinline__ Fields<R> q() const {
     return Fields<R>{{(R *)in->tape[0], (R *)in->tape[1], (R *)in->tape[2], (R *)in->tape[3]}};
+  }
+  __device__ __forceinline__ Fields<R> u2() const {
+    return Fields<R>{
+        {(R *)in->tape[20], (R *)in->tape[21], (R *)in->tape[22], (R *)in->tape[23]}};
   }
   // the arrays of the stage-1 (d1) and stage-2 (d2) flux differences; read
   // once per kernel (the record is in global memory, so accesses through it
@@ -120,6 +136,10 @@ template <class R> struct Geo {
   }
 };
 
+// fixed-order sum of n doubles by a whole block: a strided sum per thread,
+// then block_sum; every block that calls it gets the same bits
+__device__ __forceinline__ double block_sum_of(const double *x, int n, double *sh);
+
 __device__ __forceinline__ double block_sum(double v, double *sh) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -132,7 +152,13 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
   return t;
 }
 
-// Tile shapes of the fused kernels (A+B, C+D and E+F below)
+__device__ __forceinline__ double block_sum_of(const double *x, int n, double *sh) {
+  double acc = 0;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) acc += x[k];
+  return block_sum(acc, sh);
+}
+
+// Tile shapes of the tile kernels
 template <class R> struct AdjTile;
 template <> struct AdjTile<float> { static constexpr int TX = 32, TY = 16; };
 template <> struct AdjTile<double> { static constexpr int TX = 32, TY = 8; };
@@ -143,57 +169,6 @@ __device__ __forceinline__ unsigned long long warp_min(unsigned long long v) {
     v = w < v ? w : v;
   }
   return v;
-}
-
-// B on one TX x TY tile: per cell the stage-2 update reverse from the
-// taped flux differences (conserved cotangent U2b, base part of the
-// previous-state cotangent, the dt partial) and the CFL timescale minimum
-// of the state.
-template <class R, int TX, int TY>
-__global__ void __launch_bounds__(256)
-adj_update2_rev(Fields<R> Ub, Fields<R> U2b, Fields<R> Pbase, Geo<R> G, double *partial,
-                unsigned long long *minbits) {
-  __shared__ double sh[8];
-  G.dt = G.step_dt();
-  const Fields<R> P = G.state();
-  const Diffs<R> D2 = G.d2();
-  const int tid = threadIdx.x, nthr = blockDim.x;
-  const int nt0 = (G.n0 + TX - 1) / TX;
-  const int X0 = (int)(blockIdx.x % nt0) * TX, Y0 = (int)(blockIdx.x / nt0) * TY;
-  const R d0 = G.dt / G.dR0, d1 = G.dt / G.dR1;
-  const R rdR0 = R(1) / G.dR0, rdR1 = R(1) / G.dR1;
-  double dtb = 0;
-  unsigned long long best = ~0ull;
-  for (int i = tid; i < TX * TY; i += nthr) {
-    const int ty = i / TX, tx = i - ty * TX;
-    const int x = X0 + tx, y = Y0 + ty;
-    if (x >= G.n0 || y >= G.n1) continue;
-    const size_t gi = (size_t)y * G.n0 + x;
-    R D[8];
-    D2.get(gi, D);
-    const Prim<R> b = P.get(gi);
-    R u[4];
-    ha::update_cons_d(G.g, b, d0, d1, D, u);
-    const Prim<R> qb_ = Ub.get(gi);
-    const PrimBar<R> qb{qb_.rho, qb_.v0, qb_.v1, qb_.p};
-    R U[4];
-    ha::cons_from_prim_rev(G.g, u[0], u[1], u[2], u[3], qb, U);
-    U2b.set(gi, Prim<R>{U[0], U[1], U[2], U[3]});
-    PrimBar<R> bb;
-    ha::zero(bb);
-    ha::cons_of_prim_rev(G.g, b, U, bb);
-    Pbase.set(gi, Prim<R>{bb.rho, bb.v0, bb.v1, bb.p});
-    const R t0 = U[0] * D[0] + U[1] * D[1] + U[2] * D[2] + U[3] * D[3];
-    const R t1 = U[0] * D[4] + U[1] * D[5] + U[2] * D[6] + U[3] * D[7];
-    dtb += (double)(t0 * rdR0 + t1 * rdR1);
-    const unsigned long long tb =
-        hk::ts_bits<R>(hs::timescale(G.g, G.dR0, G.dR1, b.rho, b.v0, b.v1, b.p));
-    best = tb < best ? tb : best;
-  }
-  best = warp_min(best);
-  if ((tid & 31) == 0) atomicMin(minbits, best);
-  const double sum = block_sum(dtb, sh);
-  if (tid == 0) partial[blockIdx.x] = sum;
 }
 
 // C+D on one TX x TY tile.  Stage-1 state box with a 3-cell halo (origin
@@ -214,7 +189,7 @@ template <class R, int TX, int TY> struct Stage2Smem {
 };
 
 template <class R> struct AdjOcc;  // CTAs per SM the tile kernels are built for
-template <> struct AdjOcc<float> { static constexpr int stage2 = 3, stage1 = 3; };
+template <> struct AdjOcc<float> { static constexpr int stage2 = 3, stage1 = 4; };
 template <> struct AdjOcc<double> { static constexpr int stage2 = 2, stage1 = 2; };
 
 // MUSCL reverse of the four fields of one face into its 16 slot values
@@ -255,14 +230,17 @@ __device__ __forceinline__ void face2_rev(R g, const Prim<R> st[4], const Flux<R
 // stage-1 update reverse.
 template <class R, int TX, int TY>
 __global__ void __launch_bounds__(256, AdjOcc<R>::stage2)
-adj_stage2_tile(Fields<R> U2b, Fields<R> U1b, Fields<R> Pbase, Geo<R> G, double *partial) {
+adj_stage2_tile(Fields<R> Ub, Fields<R> U1b, Fields<R> Pbase, Geo<R> G, double *partial,
+                unsigned long long *minbits, PendingDt pending) {
   using S = Stage2Smem<R, TX, TY>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   S &s = *reinterpret_cast<S *>(smem_raw);
   __shared__ double sh[8];
+  __shared__ unsigned long long pend_j;
+  __shared__ R pend[4];
   G.dt = G.step_dt();
-  const Fields<R> P = G.state(), Q = G.q();
-  const Diffs<R> D1 = G.d1();
+  const Fields<R> P = G.state(), Q = G.q(), U2 = G.u2();
+  const Diffs<R> D1 = G.d1(), D2 = G.d2();
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int nt0 = (G.n0 + TX - 1) / TX;
   const int X0 = (int)(blockIdx.x % nt0) * TX, Y0 = (int)(blockIdx.x / nt0) * TY;
@@ -272,14 +250,55 @@ adj_stage2_tile(Fields<R> U2b, Fields<R> U1b, Fields<R> Pbase, Geo<R> G, double 
 #pragma unroll
     for (int c = 0; c < 4; ++c) s.q[c][by][bx] = Q.f[c][gi];
   }
+  const R d0 = G.dt / G.dR0, d1 = G.dt / G.dR1;
+  // the previous reverse step's dt cotangent, when its arg-min cell lies in
+  // this tile's stage-2 box (blocks that find it compute the same value)
+  if (tid == 0) {
+    pend_j = ~0ull;
+    if (G.in->has_prev) {
+      const unsigned long long j = *pending.argmin;
+      if (j != ~0ull) {
+        const int jx = (int)(j % (unsigned long long)G.n0), jy = (int)(j / (unsigned long long)G.n0);
+        const int dx = ((jx - (X0 - 2)) % G.n0 + G.n0) % G.n0;
+        const int dy = ((jy - (Y0 - 2)) % G.n1 + G.n1) % G.n1;
+        if (dx < S::UX && dy < S::UY) pend_j = j;
+      }
+    }
+  }
+  __syncthreads();
+  if (pend_j != ~0ull) {
+    const double dtb = block_sum_of(pending.partials, pending.nparts, sh);
+    if (tid == 0) {
+      const Fields<R> X{{(R *)G.in->prev_state[0], (R *)G.in->prev_state[1],
+                         (R *)G.in->prev_state[2], (R *)G.in->prev_state[3]}};
+      PrimBar<R> xb;
+      ha::zero(xb);
+      // dt = (Real)cfl * min: the minimum's cotangent is dt's times (Real)cfl
+      const R cfl = (R)G.in->cfl;
+      ha::timescale_rev(G.g, G.dR0, G.dR1, X.get(pend_j), (R)(dtb * (double)cfl), xb);
+      pend[0] = xb.rho; pend[1] = xb.v0; pend[2] = xb.v1; pend[3] = xb.p;
+    }
+    __syncthreads();
+  }
+  // B: the stage-2 update reverse on the tile and a 2-cell halo, the
+  // conserved cotangent of each cell's stage-2 update from the next-state
+  // cotangent and the taped conserved state
   for (int i = tid; i < S::UY * S::UX; i += nthr) {
     const int by = i / S::UX, bx = i - by * S::UX;
     const size_t gi = G.at(X0 - 2 + bx, Y0 - 2 + by);
+    const Prim<R> u_ = U2.get(gi);
+    const R u[4] = {u_.rho, u_.v0, u_.v1, u_.p};
+    const Prim<R> qb_ = Ub.get(gi);
+    PrimBar<R> qb{qb_.rho, qb_.v0, qb_.v1, qb_.p};
+    if (gi == pend_j) {
+      qb.rho += pend[0]; qb.v0 += pend[1]; qb.v1 += pend[2]; qb.p += pend[3];
+    }
+    R U[4];
+    ha::cons_from_prim_rev(G.g, u[0], u[1], u[2], u[3], qb, U);
 #pragma unroll
-    for (int c = 0; c < 4; ++c) s.u[c][by][bx] = U2b.f[c][gi];
+    for (int c = 0; c < 4; ++c) s.u[c][by][bx] = U[c];
   }
   __syncthreads();
-  const R d0 = G.dt / G.dR0, d1 = G.dt / G.dR1;
   // x faces: face X0-1+j of row Y0+r has stencil box columns j..j+3 of box
   // row r+3 and cells (right, left) at stage-2 cotangent box columns j+1, j of row r+2
   for (int i = tid; i < TY * S::XF; i += nthr) {
@@ -333,6 +352,7 @@ adj_stage2_tile(Fields<R> U2b, Fields<R> U1b, Fields<R> Pbase, Geo<R> G, double 
   const R e0 = h / G.dR0, e1 = h / G.dR1;
   const R rdR0 = R(1) / G.dR0, rdR1 = R(1) / G.dR1;
   double dtb = 0;
+  unsigned long long best = ~0ull;
   for (int i = tid; i < TX * TY; i += nthr) {
     const int ty = i / TX, tx = i - ty * TX;
     const int x = X0 + tx, y = Y0 + ty;
@@ -355,16 +375,29 @@ adj_stage2_tile(Fields<R> U2b, Fields<R> U1b, Fields<R> Pbase, Geo<R> G, double 
     R U[4];
     ha::cons_from_prim_rev(G.g, u[0], u[1], u[2], u[3], qbar, U);
     U1b.set(gi, Prim<R>{U[0], U[1], U[2], U[3]});
+    // base parts of both stages' updates (the stage-2 conserved cotangent
+    // of this cell is the centre of the box)
+    const R U2[4] = {s.u[0][ty + 2][tx + 2], s.u[1][ty + 2][tx + 2], s.u[2][ty + 2][tx + 2],
+                     s.u[3][ty + 2][tx + 2]};
     PrimBar<R> bb;
-    const Prim<R> pb0 = Pbase.get(gi);
-    bb.rho = pb0.rho; bb.v0 = pb0.v0; bb.v1 = pb0.v1; bb.p = pb0.p;
+    ha::zero(bb);
+    ha::cons_of_prim_rev(G.g, b, U2, bb);
     ha::cons_of_prim_rev(G.g, b, U, bb);
     Pbase.set(gi, Prim<R>{bb.rho, bb.v0, bb.v1, bb.p});
     const R t0 = U[0] * D[0] + U[1] * D[1] + U[2] * D[2] + U[3] * D[3];
     const R t1 = U[0] * D[4] + U[1] * D[5] + U[2] * D[6] + U[3] * D[7];
     // dtdx = (dt / 2) / dR
     dtb += (double)(R(0.5) * (t0 * rdR0 + t1 * rdR1));
+    D2.get(gi, D);
+    const R s0 = U2[0] * D[0] + U2[1] * D[1] + U2[2] * D[2] + U2[3] * D[3];
+    const R s1 = U2[0] * D[4] + U2[1] * D[5] + U2[2] * D[6] + U2[3] * D[7];
+    dtb += (double)(s0 * rdR0 + s1 * rdR1);
+    const unsigned long long tb =
+        hk::ts_bits<R>(hs::timescale(G.g, G.dR0, G.dR1, b.rho, b.v0, b.v1, b.p));
+    best = tb < best ? tb : best;
   }
+  best = warp_min(best);
+  if ((tid & 31) == 0) atomicMin(minbits, best);
   const double sum = block_sum(dtb, sh);
   if (tid == 0) partial[blockIdx.x] = sum;
 }
@@ -446,33 +479,36 @@ adj_stage1_tile(Fields<R> U1b, Fields<R> Pbase, Fields<R> Pb, Geo<R> G,
   if ((tid & 31) == 0 && best != ~0ull) atomicMin(argmin, best);
 }
 
-// G: dt cotangent to the arg-min cell.  One block of 1024 threads sums the
-// block partials in a fixed order (strided per thread, then a fixed tree),
-// so the result does not depend on scheduling.
+// G: dt cotangent of the last reverse step of a run to its arg-min cell
+// (the others are applied by the next step's C+D kernel).  One block of 256
+// threads sums the block partials in the fixed order of block_sum_of, as
+// those kernels do; the arg-min cell's state and cotangent are fetched by
+// the last warp while the others sum.
 template <class R>
-__global__ void __launch_bounds__(1024)
+__global__ void __launch_bounds__(256)
 adj_dt(Fields<R> Pb, Geo<R> G, const double *partials, int nparts, R cfl,
        const unsigned long long *argmin) {
-  __shared__ double sh[1024];
-  double acc = 0;
-  for (int k = threadIdx.x; k < nparts; k += blockDim.x) acc += partials[k];
-  sh[threadIdx.x] = acc;
-  __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
-    __syncthreads();
+  __shared__ double sh[8];
+  __shared__ R cell[8];
+  __shared__ unsigned long long jsh;
+  if (threadIdx.x == blockDim.x - 32) {
+    const unsigned long long j = *argmin;
+    jsh = j;
+    if (j != ~0ull) {
+      const Prim<R> x = G.state().get(j), b = Pb.get(j);
+      cell[0] = x.rho; cell[1] = x.v0; cell[2] = x.v1; cell[3] = x.p;
+      cell[4] = b.rho; cell[5] = b.v0; cell[6] = b.v1; cell[7] = b.p;
+    }
   }
+  const double dtb = block_sum_of(partials, nparts, sh);
   if (threadIdx.x != 0) return;
-  const double dtb = sh[0];
-  const unsigned long long j = *argmin;
+  const unsigned long long j = jsh;
   if (j == ~0ull) return;
   const R tb = (R)(dtb * (double)cfl);
   PrimBar<R> xb;
   ha::zero(xb);
-  ha::timescale_rev(G.g, G.dR0, G.dR1, G.state().get(j), tb, xb);
-  Prim<R> b = Pb.get(j);
-  b.rho += xb.rho; b.v0 += xb.v0; b.v1 += xb.v1; b.p += xb.p;
-  Pb.set(j, b);
+  ha::timescale_rev(G.g, G.dR0, G.dR1, Prim<R>{cell[0], cell[1], cell[2], cell[3]}, tb, xb);
+  Pb.set(j, Prim<R>{cell[4] + xb.rho, cell[5] + xb.v0, cell[6] + xb.v1, cell[7] + xb.p});
 }
 
 // loss = mean((rho - target)^2) and its cotangent 2 (rho - target) / N
@@ -497,9 +533,10 @@ adj_loss(const R *rho, const R *target, R *rhob, size_t n, double *partial) {
 // host side
 // ---------------------------------------------------------------------------
 
-// The tape of one step: HydroTapeOut's 20 arrays (q[4], d1[8], d2[8]).
+// The tape of one step: HydroTapeOut's 24 arrays (q[4], d1[8], d2[8], u2[4]).
+constexpr int kTapeArrays = 24;
 struct StepTape {
-  void *p[20] = {};
+  void *p[kTapeArrays] = {};
   HydroTapeOut out() const {
     HydroTapeOut t;
     for (int k = 0; k < 4; ++k) t.q[k] = p[k];
@@ -507,11 +544,12 @@ struct StepTape {
       t.d1[k] = p[4 + k];
       t.d2[k] = p[12 + k];
     }
+    for (int k = 0; k < 4; ++k) t.u2[k] = p[20 + k];
     return t;
   }
 };
 
-// the 20 arrays of a tape share one allocation (p[0] is its base)
+// the arrays of a tape share one allocation (p[0] is its base)
 static void tape_free(StepTape *t) {
   if (t->p[0]) cudaFree(t->p[0]);
   for (void *&q : t->p) q = nullptr;
@@ -520,18 +558,18 @@ static void tape_free(StepTape *t) {
 static bool tape_alloc(size_t bytes, StepTape *t) {
   const size_t pitch = (bytes + 255) / 256 * 256;
   char *base = nullptr;
-  if (cudaMalloc(&base, pitch * 20) != cudaSuccess) {
+  if (cudaMalloc(&base, pitch * kTapeArrays) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  for (int k = 0; k < 20; ++k) t->p[k] = base + pitch * k;
+  for (int k = 0; k < kTapeArrays; ++k) t->p[k] = base + pitch * k;
   return true;
 }
 
 struct AdjointScratch {
   int fp64 = -1;
   size_t cells = 0;
-  void *u2b[4], *u1b[4], *pbase[4], *ub[4], *pb[4], *next[4];
+  void *u1b[4], *pbase[4], *ub[4], *pb[4], *next[4];
   StepTape tape1;                 // the tape of a single step
   HydroScalars *sc = nullptr;     // scalar block a single taped step updates
   double *dt_scratch = nullptr;
@@ -540,10 +578,12 @@ struct AdjointScratch {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // by cotangent buffer parity
   void *graph_io[2][8] = {};        // ub[4], pb[4] each graph was captured with
   double graph_scalars[2][3] = {};  // cfl, dR0, dR1 each graph was captured with
+  // by step parity (the cotangent buffer a step reads): block partials of
+  // the dt cotangent (ntiles each) and {arg-min cell, minimum bits}
   double *partials = nullptr;
   unsigned long long *argmin = nullptr;
   int nparts = 0;   // blocks of the grid-stride kernels
-  int ntiles = 0;   // tiles of the reverse kernels
+  int ntiles = 0;   // tiles of the reverse kernels (one dt partial each)
   std::vector<void *> all;
 };
 
@@ -586,8 +626,8 @@ static om_status get_scratch(Handle *h, int fp64, AdjointScratch **out) {
   s->fp64 = fp64;
   s->cells = h->memory_size_total();
   const size_t bytes = s->cells * (fp64 ? 8 : 4);
-  void **groups[6] = {s->u2b, s->u1b, s->pbase, s->ub, s->pb, s->next};
-  for (int gi = 0; gi < 6; ++gi)
+  void **groups[5] = {s->u1b, s->pbase, s->ub, s->pb, s->next};
+  for (int gi = 0; gi < 5; ++gi)
     for (int k = 0; k < 4; ++k) {
       void *p = nullptr;
       if (cudaMalloc(&p, bytes) != cudaSuccess) {
@@ -611,7 +651,8 @@ static om_status get_scratch(Handle *h, int fp64, AdjointScratch **out) {
           cudaSuccess ||
       cudaMalloc(&s->d_in, sizeof(adj::StepIn)) != cudaSuccess ||
       cudaMallocHost(&s->h_in1, sizeof(adj::StepIn)) != cudaSuccess ||
-      cudaMalloc(&s->argmin, 2 * sizeof(unsigned long long)) != cudaSuccess) {
+      cudaMalloc(&s->argmin, 4 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMemset(s->argmin, 0xFF, 4 * sizeof(unsigned long long)) != cudaSuccess) {
     cudaGetLastError();
     free_scratch(s);
     set_error("Hydro adjoint: scratch allocation failed");
@@ -635,15 +676,19 @@ template <class R> static adj::Fields<R> F4(void *const *p) {
   return adj::Fields<R>{{(R *)p[0], (R *)p[1], (R *)p[2], (R *)p[3]}};
 }
 
-// kernels of one adjoint step (the three tile kernels and the dt kernel)
-constexpr int kVjpLaunches = 4;
+// kernels of one adjoint step (the two tile kernels; the dt cotangent of a
+// step is applied by the next step's first kernel, or by adj_dt after the
+// last step of a run)
+constexpr int kVjpLaunches = 2;
 
 // The kernels of one adjoint step, reading the step's dt, state and tape
-// from s->d_in: ub (4 device arrays, cotangent of the state after the step)
-// -> pb_out (4 device arrays, cotangent of the state before it).
+// from s->d_in: ub (4 device arrays, cotangent of the state after the step,
+// less the previous reverse step's pending dt part) -> pb_out (4 device
+// arrays, cotangent of the state before it, less this step's dt part, which
+// is left pending in the parity-`par` partials and arg-min).
 template <class R>
 static om_status vjp_kernels(Handle *h, AdjointScratch *s, void *const *ub, void *const *pb_out,
-                             double cfl) {
+                             double cfl, int par) {
   const cudaStream_t st = h->stream;
   const HydroScalars *hs_ = (const HydroScalars *)h->h_scalars;
   const int cheap = h->size[0] >= adj::kCheapWrap && h->size[1] >= adj::kCheapWrap;
@@ -651,19 +696,38 @@ static om_status vjp_kernels(Handle *h, AdjointScratch *s, void *const *ub, void
                 s->d_in,    cheap};
   const int nt = s->ntiles;
   constexpr int TX = adj::AdjTile<R>::TX, TY = adj::AdjTile<R>::TY;
-  const auto U = F4<R>(ub), U2b = F4<R>(s->u2b), U1b = F4<R>(s->u1b), Pbase = F4<R>(s->pbase),
-             Pb = F4<R>(pb_out);
-  // argmin[0]: arg-min cell, argmin[1]: minimum timescale bits
-  OM_CUDA_CHECK(cudaMemsetAsync(s->argmin, 0xFF, 2 * sizeof(unsigned long long), st));
-  adj::adj_update2_rev<R, TX, TY><<<nt, 256, 0, st>>>(U, U2b, Pbase, G, s->partials,
-                                                      s->argmin + 1);
+  (void)cfl;
+  const auto U = F4<R>(ub), U1b = F4<R>(s->u1b), Pbase = F4<R>(s->pbase), Pb = F4<R>(pb_out);
+  // argmin[2 par]: arg-min cell, argmin[2 par + 1]: minimum timescale bits
+  unsigned long long *am = s->argmin + 2 * par;
+  double *part = s->partials + (size_t)par * nt;
+  const adj::PendingDt pend{s->partials + (size_t)(1 - par) * nt, nt, s->argmin + 2 * (1 - par)};
+  OM_CUDA_CHECK(cudaMemsetAsync(am, 0xFF, 2 * sizeof(unsigned long long), st));
   adj::adj_stage2_tile<R, TX, TY><<<nt, 256, sizeof(adj::Stage2Smem<R, TX, TY>), st>>>(
-      U2b, U1b, Pbase, G, s->partials + nt);
-  adj::adj_stage1_tile<R, TX, TY><<<nt, 256, 0, st>>>(U1b, Pbase, Pb, G, s->argmin + 1,
-                                                      s->argmin);
-  adj::adj_dt<R><<<1, 1024, 0, st>>>(Pb, G, s->partials, 2 * nt, (R)cfl, s->argmin);
+      U, U1b, Pbase, G, part, am + 1, pend);
+  adj::adj_stage1_tile<R, TX, TY><<<nt, 256, 0, st>>>(U1b, Pbase, Pb, G, am + 1, am);
   OM_CUDA_CHECK(cudaGetLastError());
   return OM_OK;
+}
+
+// The dt cotangent left pending by the last reverse step of a run (parity
+// par, its record in s->d_in) added to its output pb.
+template <class R>
+static om_status final_dt(Handle *h, AdjointScratch *s, void *const *pb, double cfl, int par) {
+  const HydroScalars *hs_ = (const HydroScalars *)h->h_scalars;
+  const int cheap = h->size[0] >= adj::kCheapWrap && h->size[1] >= adj::kCheapWrap;
+  adj::Geo<R> G{h->size[0], h->size[1], (R)h->cfg.gamma, (R)hs_->dR0, (R)hs_->dR1, R(0),
+                s->d_in,    cheap};
+  adj::adj_dt<R><<<1, 256, 0, h->stream>>>(F4<R>(pb), G, s->partials + (size_t)par * s->ntiles,
+                                           s->ntiles, (R)cfl, s->argmin + 2 * par);
+  OM_CUDA_CHECK(cudaGetLastError());
+  h->launches++;
+  return OM_OK;
+}
+
+static om_status run_final_dt(Handle *h, AdjointScratch *s, void *const *pb, double cfl,
+                              int par) {
+  return s->fp64 ? final_dt<double>(h, s, pb, cfl, par) : final_dt<float>(h, s, pb, cfl, par);
 }
 
 // One taped forward step between explicit buffers, in[4] -> out[4], with the
@@ -717,14 +781,17 @@ static om_status tape_current(Handle *h, AdjointScratch *s, adj::StepIn *in) {
   in->tsbits = &s->sc->tsmin[0];
   in->cfl = ((HydroScalars *)h->h_scalars)->cfl;
   for (int k = 0; k < 4; ++k) in->state[k] = cur[k];
-  for (int k = 0; k < 20; ++k) in->tape[k] = s->tape1.p[k];
+  for (int k = 0; k < kTapeArrays; ++k) in->tape[k] = s->tape1.p[k];
+  in->has_prev = 0;
+  for (int k = 0; k < 4; ++k) in->prev_state[k] = nullptr;
   return OM_OK;
 }
 
 // One adjoint step.  `slot` (pinned host memory, left untouched until the
-// stream has passed this step) holds the step's dt, state and tape; it is
-// copied to s->d_in, then the kernel sequence runs from a CUDA graph
-// captured once per pair of cotangent buffers (and per cfl, dR0, dR1).
+// stream has passed this step) holds the step's record; it is copied to
+// s->d_in, then the kernel sequence runs from a CUDA graph captured once per
+// pair of cotangent buffers (and per cfl, dR0, dR1).  The step's parity is
+// which of s->ub / s->pb it reads.
 template <class R>
 static om_status vjp_step(Handle *h, AdjointScratch *s, const adj::StepIn *slot,
                           void *const *ub, void *const *pb_out, double cfl) {
@@ -741,7 +808,7 @@ static om_status vjp_step(Handle *h, AdjointScratch *s, const adj::StepIn *slot,
     s->graph[key] = nullptr;
     cudaGraph_t g = nullptr;
     OM_CUDA_CHECK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    om_status r = vjp_kernels<R>(h, s, ub, pb_out, cfl);
+    om_status r = vjp_kernels<R>(h, s, ub, pb_out, cfl, key);
     cudaError_t ce = cudaStreamEndCapture(st, &g);
     if (r != OM_OK) { if (g) cudaGraphDestroy(g); return r; }
     if (ce != cudaSuccess) {
@@ -808,10 +875,11 @@ extern "C" om_status om_hydro_vjp(om_handle H, void *const *cot_next, void *cons
   const double cfl = ((HydroScalars *)h->h_scalars)->cfl;
   OM_CUDA_CHECK(cudaMemcpyAsync(s->d_in, s->h_in1, sizeof(adj::StepIn), cudaMemcpyHostToDevice,
                                 h->stream));
-  om_status st = fp64 ? vjp_kernels<double>(h, s, cot_next, cot_prev, cfl)
-                      : vjp_kernels<float>(h, s, cot_next, cot_prev, cfl);
+  om_status st = fp64 ? vjp_kernels<double>(h, s, cot_next, cot_prev, cfl, 0)
+                      : vjp_kernels<float>(h, s, cot_next, cot_prev, cfl, 0);
   OM_TRY(st);
   h->launches += kVjpLaunches;
+  OM_TRY(run_final_dt(h, s, cot_prev, cfl, 0));
   OM_CUDA_CHECK(cudaStreamSynchronize(h->stream));
   return OM_OK;
 }
@@ -861,7 +929,8 @@ extern "C" om_status om_hydro_forward(om_handle H, int steps, int checkpoint_eve
       cudaGetLastError();
       free_b = 0;
     }
-    if ((double)bytes * 20.0 * t->seg <= 0.5 * (double)free_b && !injected_alloc_failure()) {
+    if ((double)bytes * kTapeArrays * t->seg <= 0.5 * (double)free_b &&
+        !injected_alloc_failure()) {
       t->tapes.resize(t->seg);
       for (auto &tp : t->tapes)
         if (!tape_alloc(bytes, &tp)) {
@@ -905,6 +974,7 @@ static om_status backward_core(om_hydro_tape t, AdjointScratch *s, void **result
     pb[k] = s->pb[k];
   }
   const double cfl = ((HydroScalars *)h->h_scalars)->cfl;
+  const adj::StepIn *prev = nullptr;  // the step reversed last
   for (int j = t->nck - 1; j >= 0; --j) {
     const int len = std::min(t->seg, t->steps - j * t->seg);
     const bool taped = (int)t->tapes.size() >= len;
@@ -921,7 +991,7 @@ static om_status backward_core(om_hydro_tape t, AdjointScratch *s, void **result
       in.cfl = cfl;
       for (int q = 0; q < 4; ++q) in.state[q] = cur[q];
       const StepTape &tp = taped ? t->tapes[m] : s->tape1;
-      for (int q = 0; q < 20; ++q) in.tape[q] = tp.p[q];
+      for (int q = 0; q < kTapeArrays; ++q) in.tape[q] = tp.p[q];
       OM_TRY(launch_tape(h, s, cur, nxt, m & 1, tp.out()));
     }
     for (int m = len - 1; m >= 0; --m) {
@@ -932,10 +1002,18 @@ static om_status backward_core(om_hydro_tape t, AdjointScratch *s, void **result
                                       cudaMemcpyDeviceToDevice, h->stream));
         OM_TRY(launch_tape(h, s, in.state, s->next, 0, s->tape1.out()));
       }
+      // its state stays in place until this step has run: a segment start
+      // is a checkpoint, and a segment's buffers are refilled only after its
+      // walk
+      in.has_prev = prev != nullptr;
+      for (int k = 0; k < 4; ++k) in.prev_state[k] = prev ? prev->state[k] : nullptr;
       OM_TRY(run_vjp_step(h, s, &in, ub, pb, cfl));
+      prev = &in;
       for (int k = 0; k < 4; ++k) std::swap(ub[k], pb[k]);
     }
   }
+  // the last step's dt cotangent (its parity: the buffer it read, now pb)
+  OM_TRY(run_final_dt(h, s, ub, cfl, pb[0] == s->ub[0] ? 0 : 1));
   OM_TRY(hydro_restore(h, &t->ck[t->nck]));
   for (int k = 0; k < 4; ++k) result[k] = ub[k];
   return OM_OK;
@@ -1062,8 +1140,20 @@ extern "C" om_status om_hydro_time_vjp(om_handle H, int reps, float *ms) {
   const size_t bytes = h->memory_size_total() * (fp64 ? 8 : 4);
   for (int k = 0; k < 4; ++k) OM_CUDA_CHECK(cudaMemsetAsync(s->ub[k], 0, bytes, h->stream));
   const double cfl = ((HydroScalars *)h->h_scalars)->cfl;
-  // one step outside the timed region captures the graph
-  OM_TRY(run_vjp_step(h, s, s->h_in1, s->ub, s->pb, cfl));
+  // steps alternate the cotangent buffers as a backward pass does, each
+  // applying the pending dt cotangent of the one before; two steps outside
+  // the timed region capture both graphs
+  s->h_in1->has_prev = 1;
+  for (int k = 0; k < 4; ++k) s->h_in1->prev_state[k] = s->h_in1->state[k];
+  void *ub[4], *pb[4];
+  for (int k = 0; k < 4; ++k) {
+    ub[k] = s->ub[k];
+    pb[k] = s->pb[k];
+  }
+  for (int r = 0; r < 2; ++r) {
+    OM_TRY(run_vjp_step(h, s, s->h_in1, ub, pb, cfl));
+    for (int k = 0; k < 4; ++k) std::swap(ub[k], pb[k]);
+  }
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   om_status st = OM_OK;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess ||
@@ -1071,8 +1161,10 @@ extern "C" om_status om_hydro_time_vjp(om_handle H, int reps, float *ms) {
     set_error("om_hydro_time_vjp: event setup failed");
     st = OM_ERR_CUDA;
   }
-  for (int r = 0; st == OM_OK && r < reps; ++r)
-    st = run_vjp_step(h, s, s->h_in1, s->ub, s->pb, cfl);
+  for (int r = 0; st == OM_OK && r < reps; ++r) {
+    st = run_vjp_step(h, s, s->h_in1, ub, pb, cfl);
+    for (int k = 0; k < 4; ++k) std::swap(ub[k], pb[k]);
+  }
   if (st == OM_OK && (cudaEventRecord(e1, h->stream) != cudaSuccess ||
                       cudaEventSynchronize(e1) != cudaSuccess ||
                       cudaEventElapsedTime(ms, e0, e1) != cudaSuccess)) {

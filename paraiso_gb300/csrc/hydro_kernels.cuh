@@ -38,14 +38,16 @@ struct HydroStepArgs {
 };
 
 // What a taped step keeps for the reverse sweep (periodic grids; arrays of
-// n0 x n1 values of the OM's Real type): the stage-1 state q, and per stage
-// the flux differences (left wall - right wall) of each axis that the
+// n0 x n1 values of the OM's Real type): the stage-1 state q; per stage the
+// flux differences (left wall - right wall) of each axis that the
 // conservative update adds, d[4 * axis + k] for k = density, momentum 0,
-// momentum 1, energy.
+// momentum 1, energy; and the stage-2 conserved state before the primitive
+// recovery, u2 (density, momentum 0, momentum 1, energy).
 struct HydroTapeOut {
   void *q[4];
   void *d1[8];
   void *d2[8];
+  void *u2[4];
 };
 
 namespace hk {
@@ -329,13 +331,17 @@ __device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
       if (gy >= n1 || gx >= n0) continue;
       const int py = oy + 3, px = ox + 3;
       const hs::Prim<R> b{s.P[0][py][px], s.P[1][py][px], s.P[2][py][px], s.P[3][py][px]};
+      R cons[4];
       const hs::Prim<R> q =
           hs::update(g, b, dtdx0, dtdx1, s.fx[oy * (TX + 1) + ox], s.fx[oy * (TX + 1) + ox + 1],
-                     s.fy[oy * TX + ox], s.fy[(oy + 1) * TX + ox]);
+                     s.fy[oy * TX + ox], s.fy[(oy + 1) * TX + ox], TAPE ? cons : nullptr);
       const size_t gi = OPEN ? (size_t)(gy + a.lm) * a.ms0 + (gx + a.lm) : (size_t)gy * n0 + gx;
-      if (TAPE)
+      if (TAPE) {
         hk::tape_diffs<R>(tape->d2, gi, s.fx[oy * (TX + 1) + ox], s.fx[oy * (TX + 1) + ox + 1],
                           s.fy[oy * TX + ox], s.fy[(oy + 1) * TX + ox]);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) ((R *)tape->u2[c])[gi] = cons[c];
+      }
       orho[gi] = q.rho;
       ovx[gi] = q.v0;
       ovy[gi] = q.v1;

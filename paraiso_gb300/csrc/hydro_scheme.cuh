@@ -129,11 +129,13 @@ __device__ __forceinline__ void muscl(R x0, R x1, R x2, R x3, R &l, R &r) {
 
 // Conservative update of base state b by the axis-1 walls, then the axis-0
 // walls (foldl1 (.) over the axes applies axis 1 first), then
-// bindPrimitive (max 1e-2 rho) v (max 1e-2 p).
+// bindPrimitive (max 1e-2 rho) v (max 1e-2 p).  cons (optional): the new
+// conserved state (rho, m0, m1, E) before the primitive recovery.
 template <class R>
 __device__ __forceinline__ Prim<R> update(R g, const Prim<R> &b, R dtdx0, R dtdx1,
                                           const Flux<R> &l0, const Flux<R> &r0,
-                                          const Flux<R> &l1, const Flux<R> &r1) {
+                                          const Flux<R> &l1, const Flux<R> &r1,
+                                          R *cons = nullptr) {
   const R m0 = b.rho * b.v0, m1 = b.rho * b.v1;
   const R e = kinetic(b.v0, b.v1, m0, m1) + (R(1) / (g - R(1))) * b.p;
   const R d1 = b.rho + dtdx1 * (l1.fd - r1.fd);
@@ -144,6 +146,12 @@ __device__ __forceinline__ Prim<R> update(R g, const Prim<R> &b, R dtdx0, R dtdx
   const R b0 = a0 + dtdx0 * (l0.fm0 - r0.fm0);
   const R b1 = a1 + dtdx0 * (l0.fm1 - r0.fm1);
   const R e2 = e1 + dtdx0 * (l0.fe - r0.fe);
+  if (cons) {
+    cons[0] = d2;
+    cons[1] = b0;
+    cons[2] = b1;
+    cons[3] = e2;
+  }
   const R v0 = b0 / d2, v1 = b1 / d2;
   const R pn = (g - R(1)) * (e2 - kinetic(v0, v1, b0, b1));
   Prim<R> q;
