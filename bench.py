@@ -543,9 +543,9 @@ def adjoint_workload(args, dist: Dist) -> dict:
         h.set_state(st0)
     # forward step and adjoint step, device time on the handle's stream
     h.proceed(max(args.warmup, 1))
-    fwd_ms = h.time_run("proceed", 20) / 20
-    vjp_ms = h.time_vjp(10)      # reverse sweep of one step from its tape
-    tape_ms = h.time_tape(10)    # the taped forward step of the recompute
+    fwd_ms = h.time_run("proceed", 50) / 50
+    vjp_ms = h.time_vjp(50)      # reverse sweep of one step from its tape
+    tape_ms = h.time_tape(50)    # the taped forward step of the recompute
     # the full gradient: forward with sqrt(T) checkpoints, recompute, backward
     h.set_state(st0)
     h.set_scalar("time", 0.0)

@@ -573,11 +573,8 @@ struct AdjointScratch {
   StepTape tape1;                 // the tape of a single step
   HydroScalars *sc = nullptr;     // scalar block a single taped step updates
   double *dt_scratch = nullptr;
-  adj::StepIn *d_in = nullptr;    // the step being reversed (device)
-  adj::StepIn *h_in1 = nullptr;   // pinned slot for single steps
-  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // by cotangent buffer parity
-  void *graph_io[2][8] = {};        // ub[4], pb[4] each graph was captured with
-  double graph_scalars[2][3] = {};  // cfl, dR0, dR1 each graph was captured with
+  adj::StepIn *d_in = nullptr;    // the record of a single step (device)
+  adj::StepIn *h_in1 = nullptr;   // its pinned host copy
   // by step parity (the cotangent buffer a step reads): block partials of
   // the dt cotangent (ntiles each) and {arg-min cell, minimum bits}
   double *partials = nullptr;
@@ -589,8 +586,6 @@ struct AdjointScratch {
 
 static void free_scratch(AdjointScratch *s) {
   if (!s) return;
-  for (int k = 0; k < 2; ++k)
-    if (s->graph[k]) cudaGraphExecDestroy(s->graph[k]);
   cudaFree(s->d_in);
   cudaFreeHost(s->h_in1);
   for (void *p : s->all) cudaFree(p);
@@ -676,27 +671,27 @@ template <class R> static adj::Fields<R> F4(void *const *p) {
   return adj::Fields<R>{{(R *)p[0], (R *)p[1], (R *)p[2], (R *)p[3]}};
 }
 
-// kernels of one adjoint step (the two tile kernels; the dt cotangent of a
-// step is applied by the next step's first kernel, or by adj_dt after the
-// last step of a run)
+// kernels of one adjoint step, launched directly (the two tile kernels; the
+// dt cotangent of a step is applied by the next step's first kernel, or by
+// adj_dt after the last step of a run)
 constexpr int kVjpLaunches = 2;
 
-// The kernels of one adjoint step, reading the step's dt, state and tape
-// from s->d_in: ub (4 device arrays, cotangent of the state after the step,
-// less the previous reverse step's pending dt part) -> pb_out (4 device
-// arrays, cotangent of the state before it, less this step's dt part, which
-// is left pending in the parity-`par` partials and arg-min).
+// The kernels of one adjoint step, reading the step's record `rec` (device
+// memory): ub (4 device arrays, cotangent of the state after the step, less
+// the previous reverse step's pending dt part) -> pb_out (4 device arrays,
+// cotangent of the state before it, less this step's dt part, which is left
+// pending in the parity-`par` partials and arg-min).  `par` is which of
+// s->ub / s->pb the step reads.
 template <class R>
-static om_status vjp_kernels(Handle *h, AdjointScratch *s, void *const *ub, void *const *pb_out,
-                             double cfl, int par) {
+static om_status vjp_kernels(Handle *h, AdjointScratch *s, const adj::StepIn *rec,
+                             void *const *ub, void *const *pb_out, int par) {
   const cudaStream_t st = h->stream;
   const HydroScalars *hs_ = (const HydroScalars *)h->h_scalars;
   const int cheap = h->size[0] >= adj::kCheapWrap && h->size[1] >= adj::kCheapWrap;
-  adj::Geo<R> G{h->size[0], h->size[1], (R)h->cfg.gamma, (R)hs_->dR0, (R)hs_->dR1, R(0),
-                s->d_in,    cheap};
+  adj::Geo<R> G{h->size[0], h->size[1], (R)h->cfg.gamma, (R)hs_->dR0, (R)hs_->dR1, R(0), rec,
+                cheap};
   const int nt = s->ntiles;
   constexpr int TX = adj::AdjTile<R>::TX, TY = adj::AdjTile<R>::TY;
-  (void)cfl;
   const auto U = F4<R>(ub), U1b = F4<R>(s->u1b), Pbase = F4<R>(s->pbase), Pb = F4<R>(pb_out);
   // argmin[2 par]: arg-min cell, argmin[2 par + 1]: minimum timescale bits
   unsigned long long *am = s->argmin + 2 * par;
@@ -707,17 +702,26 @@ static om_status vjp_kernels(Handle *h, AdjointScratch *s, void *const *ub, void
       U, U1b, Pbase, G, part, am + 1, pend);
   adj::adj_stage1_tile<R, TX, TY><<<nt, 256, 0, st>>>(U1b, Pbase, Pb, G, am + 1, am);
   OM_CUDA_CHECK(cudaGetLastError());
+  h->launches += kVjpLaunches;
   return OM_OK;
 }
 
+static om_status run_vjp(Handle *h, AdjointScratch *s, const adj::StepIn *rec, void *const *ub,
+                         void *const *pb) {
+  const int par = ub[0] == s->ub[0] ? 0 : 1;
+  return s->fp64 ? vjp_kernels<double>(h, s, rec, ub, pb, par)
+                 : vjp_kernels<float>(h, s, rec, ub, pb, par);
+}
+
 // The dt cotangent left pending by the last reverse step of a run (parity
-// par, its record in s->d_in) added to its output pb.
+// par, record rec) added to its output pb.
 template <class R>
-static om_status final_dt(Handle *h, AdjointScratch *s, void *const *pb, double cfl, int par) {
+static om_status final_dt(Handle *h, AdjointScratch *s, const adj::StepIn *rec,
+                          void *const *pb, double cfl, int par) {
   const HydroScalars *hs_ = (const HydroScalars *)h->h_scalars;
   const int cheap = h->size[0] >= adj::kCheapWrap && h->size[1] >= adj::kCheapWrap;
-  adj::Geo<R> G{h->size[0], h->size[1], (R)h->cfg.gamma, (R)hs_->dR0, (R)hs_->dR1, R(0),
-                s->d_in,    cheap};
+  adj::Geo<R> G{h->size[0], h->size[1], (R)h->cfg.gamma, (R)hs_->dR0, (R)hs_->dR1, R(0), rec,
+                cheap};
   adj::adj_dt<R><<<1, 256, 0, h->stream>>>(F4<R>(pb), G, s->partials + (size_t)par * s->ntiles,
                                            s->ntiles, (R)cfl, s->argmin + 2 * par);
   OM_CUDA_CHECK(cudaGetLastError());
@@ -725,9 +729,10 @@ static om_status final_dt(Handle *h, AdjointScratch *s, void *const *pb, double 
   return OM_OK;
 }
 
-static om_status run_final_dt(Handle *h, AdjointScratch *s, void *const *pb, double cfl,
-                              int par) {
-  return s->fp64 ? final_dt<double>(h, s, pb, cfl, par) : final_dt<float>(h, s, pb, cfl, par);
+static om_status run_final_dt(Handle *h, AdjointScratch *s, const adj::StepIn *rec,
+                              void *const *pb, double cfl, int par) {
+  return s->fp64 ? final_dt<double>(h, s, rec, pb, cfl, par)
+                 : final_dt<float>(h, s, rec, pb, cfl, par);
 }
 
 // One taped forward step between explicit buffers, in[4] -> out[4], with the
@@ -787,54 +792,6 @@ static om_status tape_current(Handle *h, AdjointScratch *s, adj::StepIn *in) {
   return OM_OK;
 }
 
-// One adjoint step.  `slot` (pinned host memory, left untouched until the
-// stream has passed this step) holds the step's record; it is copied to
-// s->d_in, then the kernel sequence runs from a CUDA graph captured once per
-// pair of cotangent buffers (and per cfl, dR0, dR1).  The step's parity is
-// which of s->ub / s->pb it reads.
-template <class R>
-static om_status vjp_step(Handle *h, AdjointScratch *s, const adj::StepIn *slot,
-                          void *const *ub, void *const *pb_out, double cfl) {
-  const cudaStream_t st = h->stream;
-  OM_CUDA_CHECK(
-      cudaMemcpyAsync(s->d_in, slot, sizeof(adj::StepIn), cudaMemcpyHostToDevice, st));
-  const int key = ub[0] == s->ub[0] ? 0 : 1;
-  void *io[8] = {ub[0], ub[1], ub[2], ub[3], pb_out[0], pb_out[1], pb_out[2], pb_out[3]};
-  const HydroScalars *hs_ = (const HydroScalars *)h->h_scalars;
-  const double baked[3] = {cfl, hs_->dR0, hs_->dR1};
-  if (!s->graph[key] || std::memcmp(io, s->graph_io[key], sizeof(io)) != 0 ||
-      std::memcmp(baked, s->graph_scalars[key], sizeof(baked)) != 0) {
-    if (s->graph[key]) cudaGraphExecDestroy(s->graph[key]);
-    s->graph[key] = nullptr;
-    cudaGraph_t g = nullptr;
-    OM_CUDA_CHECK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    om_status r = vjp_kernels<R>(h, s, ub, pb_out, cfl, key);
-    cudaError_t ce = cudaStreamEndCapture(st, &g);
-    if (r != OM_OK) { if (g) cudaGraphDestroy(g); return r; }
-    if (ce != cudaSuccess) {
-      set_error(std::string("adjoint graph capture: ") + cudaGetErrorString(ce));
-      return OM_ERR_CUDA;
-    }
-    ce = cudaGraphInstantiate(&s->graph[key], g, 0);
-    cudaGraphDestroy(g);
-    if (ce != cudaSuccess) {
-      set_error(std::string("adjoint graph instantiate: ") + cudaGetErrorString(ce));
-      return OM_ERR_CUDA;
-    }
-    std::memcpy(s->graph_io[key], io, sizeof(io));
-    std::memcpy(s->graph_scalars[key], baked, sizeof(baked));
-  }
-  OM_CUDA_CHECK(cudaGraphLaunch(s->graph[key], st));
-  h->launches += kVjpLaunches;
-  return OM_OK;
-}
-
-static om_status run_vjp_step(Handle *h, AdjointScratch *s, const adj::StepIn *slot,
-                              void *const *ub, void *const *pb, double cfl) {
-  return s->fp64 ? vjp_step<double>(h, s, slot, ub, pb, cfl)
-                 : vjp_step<float>(h, s, slot, ub, pb, cfl);
-}
-
 }  // namespace om
 
 using namespace om;
@@ -848,12 +805,14 @@ struct om_hydro_tape_s {
   std::vector<StepTape> tapes;         // tapes of one recomputed segment (empty:
                                        // each step is taped again before its reverse)
   adj::StepIn *h_in = nullptr;         // pinned: one record per step
+  adj::StepIn *d_recs = nullptr;       // the same, on the device (per segment)
   unsigned long long *d_ts = nullptr;  // CFL minimum of each step's state
   ~om_hydro_tape_s() {
     for (auto &c : ck) hydro_checkpoint_free(&c);
     for (auto &c : segst) hydro_checkpoint_free(&c);
     for (auto &t : tapes) tape_free(&t);
     if (h_in) cudaFreeHost(h_in);
+    cudaFree(d_recs);
     cudaFree(d_ts);
   }
 };
@@ -875,11 +834,10 @@ extern "C" om_status om_hydro_vjp(om_handle H, void *const *cot_next, void *cons
   const double cfl = ((HydroScalars *)h->h_scalars)->cfl;
   OM_CUDA_CHECK(cudaMemcpyAsync(s->d_in, s->h_in1, sizeof(adj::StepIn), cudaMemcpyHostToDevice,
                                 h->stream));
-  om_status st = fp64 ? vjp_kernels<double>(h, s, cot_next, cot_prev, cfl, 0)
-                      : vjp_kernels<float>(h, s, cot_next, cot_prev, cfl, 0);
+  om_status st = fp64 ? vjp_kernels<double>(h, s, s->d_in, cot_next, cot_prev, 0)
+                      : vjp_kernels<float>(h, s, s->d_in, cot_next, cot_prev, 0);
   OM_TRY(st);
-  h->launches += kVjpLaunches;
-  OM_TRY(run_final_dt(h, s, cot_prev, cfl, 0));
+  OM_TRY(run_final_dt(h, s, s->d_in, cot_prev, cfl, 0));
   OM_CUDA_CHECK(cudaStreamSynchronize(h->stream));
   return OM_OK;
 }
@@ -941,6 +899,7 @@ extern "C" om_status om_hydro_forward(om_handle H, int steps, int checkpoint_eve
     }
   }
   if (cudaMallocHost(&t->h_in, sizeof(adj::StepIn) * (size_t)steps) != cudaSuccess ||
+      cudaMalloc(&t->d_recs, sizeof(adj::StepIn) * (size_t)steps) != cudaSuccess ||
       cudaMalloc(&t->d_ts, sizeof(unsigned long long) * (size_t)steps) != cudaSuccess) {
     cudaGetLastError();
     set_error("om_hydro_forward: allocation failed");
@@ -974,7 +933,6 @@ static om_status backward_core(om_hydro_tape t, AdjointScratch *s, void **result
     pb[k] = s->pb[k];
   }
   const double cfl = ((HydroScalars *)h->h_scalars)->cfl;
-  const adj::StepIn *prev = nullptr;  // the step reversed last
   for (int j = t->nck - 1; j >= 0; --j) {
     const int len = std::min(t->seg, t->steps - j * t->seg);
     const bool taped = (int)t->tapes.size() >= len;
@@ -992,28 +950,36 @@ static om_status backward_core(om_hydro_tape t, AdjointScratch *s, void **result
       for (int q = 0; q < 4; ++q) in.state[q] = cur[q];
       const StepTape &tp = taped ? t->tapes[m] : s->tape1;
       for (int q = 0; q < kTapeArrays; ++q) in.tape[q] = tp.p[q];
+      // the step reversed before this one is the next in time: its state is
+      // the next segment buffer, or the next segment's checkpoint; both stay
+      // in place until this step has run
+      in.has_prev = m + 1 < len || j + 1 < t->nck;
+      for (int q = 0; q < 4; ++q)
+        in.prev_state[q] = m + 1 < len ? t->segst[m + 1].f[q]
+                                       : (j + 1 < t->nck ? t->ck[j + 1].f[q] : nullptr);
       OM_TRY(launch_tape(h, s, cur, nxt, m & 1, tp.out()));
     }
+    // the segment's records, on the device for its reverse steps (the host
+    // copies are not touched again in this pass)
+    OM_CUDA_CHECK(cudaMemcpyAsync(t->d_recs + (size_t)j * t->seg, t->h_in + (size_t)j * t->seg,
+                                  sizeof(adj::StepIn) * (size_t)len, cudaMemcpyHostToDevice,
+                                  h->stream));
     for (int m = len - 1; m >= 0; --m) {
-      adj::StepIn &in = t->h_in[j * t->seg + m];
+      const int k = j * t->seg + m;
       if (!taped) {
         // one tape buffer: tape this step again from its kept state
+        const adj::StepIn &in = t->h_in[k];
         OM_CUDA_CHECK(cudaMemcpyAsync(&s->sc->tsmin[0], in.tsbits, sizeof(unsigned long long),
                                       cudaMemcpyDeviceToDevice, h->stream));
         OM_TRY(launch_tape(h, s, in.state, s->next, 0, s->tape1.out()));
       }
-      // its state stays in place until this step has run: a segment start
-      // is a checkpoint, and a segment's buffers are refilled only after its
-      // walk
-      in.has_prev = prev != nullptr;
-      for (int k = 0; k < 4; ++k) in.prev_state[k] = prev ? prev->state[k] : nullptr;
-      OM_TRY(run_vjp_step(h, s, &in, ub, pb, cfl));
-      prev = &in;
-      for (int k = 0; k < 4; ++k) std::swap(ub[k], pb[k]);
+      OM_TRY(run_vjp(h, s, t->d_recs + k, ub, pb));
+      for (int q = 0; q < 4; ++q) std::swap(ub[q], pb[q]);
     }
   }
-  // the last step's dt cotangent (its parity: the buffer it read, now pb)
-  OM_TRY(run_final_dt(h, s, ub, cfl, pb[0] == s->ub[0] ? 0 : 1));
+  // the last step's dt cotangent (step 0; its parity: the buffer it read,
+  // now pb)
+  OM_TRY(run_final_dt(h, s, t->d_recs, ub, cfl, pb[0] == s->ub[0] ? 0 : 1));
   OM_TRY(hydro_restore(h, &t->ck[t->nck]));
   for (int k = 0; k < 4; ++k) result[k] = ub[k];
   return OM_OK;
@@ -1139,19 +1105,20 @@ extern "C" om_status om_hydro_time_vjp(om_handle H, int reps, float *ms) {
   OM_TRY(tape_current(h, s, s->h_in1));
   const size_t bytes = h->memory_size_total() * (fp64 ? 8 : 4);
   for (int k = 0; k < 4; ++k) OM_CUDA_CHECK(cudaMemsetAsync(s->ub[k], 0, bytes, h->stream));
-  const double cfl = ((HydroScalars *)h->h_scalars)->cfl;
   // steps alternate the cotangent buffers as a backward pass does, each
-  // applying the pending dt cotangent of the one before; two steps outside
-  // the timed region capture both graphs
+  // applying the pending dt cotangent of the one before; two steps run
+  // outside the timed region
   s->h_in1->has_prev = 1;
   for (int k = 0; k < 4; ++k) s->h_in1->prev_state[k] = s->h_in1->state[k];
+  OM_CUDA_CHECK(cudaMemcpyAsync(s->d_in, s->h_in1, sizeof(adj::StepIn), cudaMemcpyHostToDevice,
+                                h->stream));
   void *ub[4], *pb[4];
   for (int k = 0; k < 4; ++k) {
     ub[k] = s->ub[k];
     pb[k] = s->pb[k];
   }
   for (int r = 0; r < 2; ++r) {
-    OM_TRY(run_vjp_step(h, s, s->h_in1, ub, pb, cfl));
+    OM_TRY(run_vjp(h, s, s->d_in, ub, pb));
     for (int k = 0; k < 4; ++k) std::swap(ub[k], pb[k]);
   }
   cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -1162,7 +1129,7 @@ extern "C" om_status om_hydro_time_vjp(om_handle H, int reps, float *ms) {
     st = OM_ERR_CUDA;
   }
   for (int r = 0; st == OM_OK && r < reps; ++r) {
-    st = run_vjp_step(h, s, s->h_in1, ub, pb, cfl);
+    st = run_vjp(h, s, s->d_in, ub, pb);
     for (int k = 0; k < 4; ++k) std::swap(ub[k], pb[k]);
   }
   if (st == OM_OK && (cudaEventRecord(e1, h->stream) != cudaSuccess ||
