@@ -47,6 +47,8 @@ def parse(text: str) -> dict:
             om["kernels"][w[1]] = cur
         elif w[0] == "end":
             cur = None
+        elif w[0] == "manifest":
+            continue   # an allocation choice: the values are the same
         else:
             cur.append(w)
     return om

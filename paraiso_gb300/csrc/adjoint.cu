@@ -63,7 +63,10 @@ struct StepIn {
   const unsigned long long *tsbits;  // CFL minimum of the state (hk::ts_bits)
   double cfl;
   void *state[4];
-  void *tape[24];   // the step's HydroTapeOut: q[4], d1[8], d2[8], u2[4]
+  // the step's tape: its arrays (hydro_kernels.cuh HydroTapeOut order:
+  // q[4], d1[8], d2[8], u2[4]) lie `tape_pitch` bytes apart
+  const void *tape;
+  size_t tape_pitch;
   // the reverse step run just before this one (the step after it in time)
   // left its dt cotangent pending: it is added to this step's incoming
   // cotangent at that step's arg-min cell, whose state is prev_state
@@ -79,14 +82,23 @@ struct PendingDt {
   const unsigned long long *argmin;
 };
 
-// eight taped arrays of flux differences, D[4 * axis + k] at a cell
-template <class R> struct Diffs {
-  const R *f[8];
-  __device__ __forceinline__ void get(size_t i, R D[8]) const {
+// The taped arrays of a step: array k starts k * pitch elements after base.
+// Array indices: stage-1 state 0..3, stage-1 differences 4..11, stage-2
+// differences 12..19 (D[4 * axis + k]), stage-2 conserved state 20..23.
+template <class R> struct TapeView {
+  const R *base;
+  size_t pitch;
+  __device__ __forceinline__ const R *array(int k) const { return base + (size_t)k * pitch; }
+  __device__ __forceinline__ void get8(int first, size_t i, R v[8]) const {
 #pragma unroll
-    for (int k = 0; k < 8; ++k) D[k] = f[k][i];
+    for (int k = 0; k < 8; ++k) v[k] = base[(size_t)(first + k) * pitch + i];
+  }
+  __device__ __forceinline__ Fields<R> fields(int first) const {
+    return Fields<R>{{(R *)array(first), (R *)array(first + 1), (R *)array(first + 2),
+                      (R *)array(first + 3)}};
   }
 };
+constexpr int kTapeQ = 0, kTapeD1 = 4, kTapeD2 = 12, kTapeU2 = 20;
 
 template <class R> struct Geo {
   int n0, n1;
@@ -100,25 +112,10 @@ template <class R> struct Geo {
     return Fields<R>{{(R *)in->state[0], (R *)in->state[1], (R *)in->state[2],
                       (R *)in->state[3]}};
   }
-  // the tape: stage-1 state, stage-1 and stage-2 flux differences, the
-  // stage-2 conserved state before the primitive recovery
-  __device__ __forceinline__ Fields<R> q() const {
-    return Fields<R>{{(R *)in->tape[0], (R *)in->tape[1], (R *)in->tape[2], (R *)in->tape[3]}};
-  }
-  __device__ __forceinline__ Fields<R> u2() const {
-    return Fields<R>{
-        {(R *)in->tape[20], (R *)in->tape[21], (R *)in->tape[22], (R *)in->tape[23]}};
-  }
-  // the arrays of the stage-1 (d1) and stage-2 (d2) flux differences; read
-  // once per kernel (the record is in global memory, so accesses through it
-  // after a store would be reloaded)
-  __device__ __forceinline__ Diffs<R> d1() const { return diffs(4); }
-  __device__ __forceinline__ Diffs<R> d2() const { return diffs(12); }
-  __device__ __forceinline__ Diffs<R> diffs(int first) const {
-    Diffs<R> d;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) d.f[k] = (const R *)in->tape[first + k];
-    return d;
+  // the step's tape; read once per kernel (the record is in global memory,
+  // so accesses through it after a store would be reloaded)
+  __device__ __forceinline__ TapeView<R> tape() const {
+    return TapeView<R>{(const R *)in->tape, in->tape_pitch / sizeof(R)};
   }
   // periodic index of a cell at most 4 cells (or one tile plus 3 cells)
   // outside the mesh
@@ -239,8 +236,9 @@ adj_stage2_tile(Fields<R> Ub, Fields<R> U1b, Fields<R> Pbase, Geo<R> G, double *
   __shared__ unsigned long long pend_j;
   __shared__ R pend[4];
   G.dt = G.step_dt();
-  const Fields<R> P = G.state(), Q = G.q(), U2 = G.u2();
-  const Diffs<R> D1 = G.d1(), D2 = G.d2();
+  const Fields<R> P = G.state();
+  const TapeView<R> T = G.tape();
+  const Fields<R> Q = T.fields(kTapeQ), U2 = T.fields(kTapeU2);
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int nt0 = (G.n0 + TX - 1) / TX;
   const int X0 = (int)(blockIdx.x % nt0) * TX, Y0 = (int)(blockIdx.x / nt0) * TY;
@@ -367,7 +365,7 @@ adj_stage2_tile(Fields<R> Ub, Fields<R> U1b, Fields<R> Pbase, Geo<R> G, double *
     }
     const size_t gi = (size_t)y * G.n0 + x;
     R D[8];
-    D1.get(gi, D);
+    T.get8(kTapeD1, gi, D);
     const Prim<R> b = P.get(gi);
     R u[4];
     ha::update_cons_d(G.g, b, e0, e1, D, u);
@@ -388,7 +386,7 @@ adj_stage2_tile(Fields<R> Ub, Fields<R> U1b, Fields<R> Pbase, Geo<R> G, double *
     const R t1 = U[0] * D[4] + U[1] * D[5] + U[2] * D[6] + U[3] * D[7];
     // dtdx = (dt / 2) / dR
     dtb += (double)(R(0.5) * (t0 * rdR0 + t1 * rdR1));
-    D2.get(gi, D);
+    T.get8(kTapeD2, gi, D);
     const R s0 = U2[0] * D[0] + U2[1] * D[1] + U2[2] * D[2] + U2[3] * D[3];
     const R s1 = U2[0] * D[4] + U2[1] * D[5] + U2[2] * D[6] + U2[3] * D[7];
     dtb += (double)(s0 * rdR0 + s1 * rdR1);
@@ -533,10 +531,12 @@ adj_loss(const R *rho, const R *target, R *rhob, size_t n, double *partial) {
 // host side
 // ---------------------------------------------------------------------------
 
-// The tape of one step: HydroTapeOut's 24 arrays (q[4], d1[8], d2[8], u2[4]).
+// The tape of one step: HydroTapeOut's 24 arrays (q[4], d1[8], d2[8], u2[4])
+// in one allocation, `pitch` bytes apart.
 constexpr int kTapeArrays = 24;
 struct StepTape {
   void *p[kTapeArrays] = {};
+  size_t pitch = 0;
   HydroTapeOut out() const {
     HydroTapeOut t;
     for (int k = 0; k < 4; ++k) t.q[k] = p[k];
@@ -563,6 +563,7 @@ static bool tape_alloc(size_t bytes, StepTape *t) {
     return false;
   }
   for (int k = 0; k < kTapeArrays; ++k) t->p[k] = base + pitch * k;
+  t->pitch = pitch;
   return true;
 }
 
@@ -786,7 +787,8 @@ static om_status tape_current(Handle *h, AdjointScratch *s, adj::StepIn *in) {
   in->tsbits = &s->sc->tsmin[0];
   in->cfl = ((HydroScalars *)h->h_scalars)->cfl;
   for (int k = 0; k < 4; ++k) in->state[k] = cur[k];
-  for (int k = 0; k < kTapeArrays; ++k) in->tape[k] = s->tape1.p[k];
+  in->tape = s->tape1.p[0];
+  in->tape_pitch = s->tape1.pitch;
   in->has_prev = 0;
   for (int k = 0; k < 4; ++k) in->prev_state[k] = nullptr;
   return OM_OK;
@@ -949,7 +951,8 @@ static om_status backward_core(om_hydro_tape t, AdjointScratch *s, void **result
       in.cfl = cfl;
       for (int q = 0; q < 4; ++q) in.state[q] = cur[q];
       const StepTape &tp = taped ? t->tapes[m] : s->tape1;
-      for (int q = 0; q < kTapeArrays; ++q) in.tape[q] = tp.p[q];
+      in.tape = tp.p[0];
+      in.tape_pitch = tp.pitch;
       // the step reversed before this one is the next in time: its state is
       // the next segment buffer, or the next segment's checkpoint; both stay
       // in place until this step has run

@@ -93,9 +93,11 @@ __device__ __forceinline__ Flux<R> hllc(R g, const Prim<R> &L, R cl, const Prim<
   const R soundMid = (cl + cr) / R(2);
   const R uL = AX == 0 ? L.v0 : L.v1;
   const R uR = AX == 0 ? Rt.v0 : Rt.v1;
-  const R presStar = omax(R(0), (L.p + Rt.p) / R(2) - densMid * soundMid * (uR - uL));
-  const R shockLeft = uL - cl * hllc_q(g, presStar, L.p);
-  const R shockRight = uR + cr * hllc_q(g, presStar, Rt.p);
+  const R psraw = (L.p + Rt.p) / R(2) - densMid * soundMid * (uR - uL);
+  const R presStar = omax(R(0), psraw);
+  const R qL = hllc_q(g, presStar, L.p), qR = hllc_q(g, presStar, Rt.p);
+  const R shockLeft = uL - cl * qL;
+  const R shockRight = uR + cr * qR;
   const R shockStar = (Rt.p - L.p + L.rho * uL * (shockLeft - uL) -
                        Rt.rho * uR * (shockRight - uR)) /
                       (L.rho * (shockLeft - uL) - Rt.rho * (shockRight - uR));

@@ -24,6 +24,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <set>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -65,6 +66,7 @@ struct KernelDef {
   std::vector<Node> nodes;
   std::map<int, int> at;  // node id -> index in nodes
   std::vector<Store> stores;
+  std::set<int> manifest;  // array nodes marked Manifest (stored once per run)
   const Node &node(int id) const { return nodes[at.at(id)]; }
 };
 
@@ -190,6 +192,14 @@ static om_status parse(const char *text, Graph *g) {
       if (v.array != g->statics[s].array || v.type != g->statics[s].type)
         return perr(ln, "store of a value whose realm or type differs from " + w[1]);
       k->stores.push_back(Store{s, id});
+      continue;
+    }
+    if (w[0] == "manifest") {
+      if (w.size() != 2) return perr(ln, "manifest NODE");
+      const int id = std::atoi(w[1].c_str());
+      if (!k->at.count(id)) return perr(ln, "unknown node " + w[1]);
+      if (!k->node(id).array) return perr(ln, "manifest of an array node");
+      k->manifest.insert(id);
       continue;
     }
     if (w.size() < 4) return perr(ln, "ID OP REALM TYPE ...");
@@ -352,11 +362,19 @@ constexpr int kMaxVectorStatements = 400;
 
 // Emits the statements computing (node, offset) values of one kernel, each
 // once, into a block of code.
+// Where the manifests of a kernel are: node id -> {stage that computes it,
+// its array among the handle's temporaries}.
+struct ManifestAt {
+  int stage;
+  int tmp;
+};
+
 class Emitter {
  public:
   Emitter(const Graph &g, const KernelDef &k, const Layout &L,
-          const std::map<int, int> &slot_of_reduce)
-      : g_(g), k_(k), L_(L), slots_(slot_of_reduce) {}
+          const std::map<int, int> &slot_of_reduce,
+          const std::map<int, ManifestAt> *manifests = nullptr, int stage = 0)
+      : g_(g), k_(k), L_(L), slots_(slot_of_reduce), man_(manifests), stage_(stage) {}
 
   std::string code;
 
@@ -368,7 +386,15 @@ class Emitter {
     if (it != memo_.end()) return it->second;
     std::string expr;
     const std::string T = ctype(n.type);
-    if (n.op == "load") {
+    const ManifestAt *m = nullptr;
+    if (man_) {
+      auto mi = man_->find(id);
+      if (mi != man_->end() && mi->second.stage < stage_) m = &mi->second;
+    }
+    if (m) {
+      // a manifest computed by an earlier stage of this kernel run
+      expr = "((const " + T + " *)P.tmp[" + std::to_string(m->tmp) + "])[" + addr(o0, o1) + "]";
+    } else if (n.op == "load") {
       const int s = g_.find_static(n.sarg);
       if (g_.statics[s].array)
         expr = "((const " + T + " *)P.cur[" + std::to_string(array_index(s)) + "])[" +
@@ -493,6 +519,8 @@ class Emitter {
   const KernelDef &k_;
   const Layout &L_;
   const std::map<int, int> &slots_;
+  const std::map<int, ManifestAt> *man_;
+  int stage_;
   std::map<std::tuple<int, int, int>, std::string> memo_;
   std::map<int, std::string> cols_, rows_;
 };
@@ -520,20 +548,22 @@ static bool region_is_all(const Region &r, const Layout &L) {
 }
 
 struct StagePlan {
-  std::vector<int> stores;   // indices into KernelDef::stores (array stores)
-  std::vector<int> reduces;  // reduce node ids
+  std::vector<int> stores;     // indices into KernelDef::stores (array stores)
+  std::vector<int> reduces;    // reduce node ids
+  std::vector<int> manifests;  // manifest node ids computed by this stage
   std::string fn;
 };
 
 struct KernelPlan {
   std::vector<StagePlan> stages;
+  std::vector<std::pair<int, Type>> manifest_types;  // temporary array -> element type
   std::vector<int> scalar_stores;  // indices into KernelDef::stores
   std::vector<int> stored_arrays;  // static indices of arrays written
   std::string commit_fn;
 };
 
 static const char *kPrelude =
-    "struct OMPtrs { const void *cur[32]; void *nxt[32]; };\n"
+    "struct OMPtrs { const void *cur[32]; void *nxt[32]; void *tmp[64]; };\n"
     "__device__ __forceinline__ float om_inf_f() { return __int_as_float(0x7f800000); }\n"
     "__device__ __forceinline__ double om_inf_d() {\n"
     "  return __longlong_as_double(0x7ff0000000000000LL); }\n";
@@ -555,55 +585,88 @@ static std::string combine(const std::string &op, const std::string &acc, const 
 
 // Builds the plan and the CUDA source of every kernel of the graph.
 static std::string generate(const Graph &g, const Layout &L, std::vector<KernelPlan> *plans,
-                            std::map<std::pair<int, int>, int> *slot_map, int *nslots) {
+                            std::map<std::pair<int, int>, int> *slot_map, int *nslots,
+                            int *ntmp) {
   std::ostringstream src;
   src << kPrelude;
   int slot = 0;
+  *ntmp = 0;
   for (size_t ki = 0; ki < g.kernels.size(); ++ki) {
     const KernelDef &k = g.kernels[ki];
     KernelPlan kp;
     const std::vector<Region> reg = regions(k);
-    // reduce depth of every node
-    std::vector<int> depth(k.nodes.size(), 0);
-    std::map<int, int> slots;
-    for (size_t i = 0; i < k.nodes.size(); ++i) {
-      const Node &n = k.nodes[i];
-      int d = 0;
-      for (int a : n.args) d = std::max(d, depth[k.at.at(a)]);
-      if (n.op == "reduce") {
-        d += 1;
-        slots[n.id] = slot;
-        (*slot_map)[{(int)ki, n.id}] = slot++;
-      }
-      depth[i] = d;
-    }
     // the last store to each static wins (manifests are copied in order)
     std::vector<int> last(g.statics.size(), -1);
     for (size_t s = 0; s < k.stores.size(); ++s) last[k.stores[s].stat] = (int)s;
+    // manifests in use: reachable from a store that counts or a reduce
+    std::set<int> live;
+    {
+      std::vector<int> todo;
+      for (size_t s = 0; s < k.stores.size(); ++s)
+        if (last[k.stores[s].stat] == (int)s) todo.push_back(k.stores[s].node);
+      for (const Node &n : k.nodes)
+        if (n.op == "reduce") todo.push_back(n.id);
+      while (!todo.empty()) {
+        const int id = todo.back();
+        todo.pop_back();
+        if (!live.insert(id).second) continue;
+        for (int a : k.node(id).args) todo.push_back(a);
+      }
+    }
+    // the stage (kernel pass) in which each value is first available: a
+    // reduce's or a manifest's value only in the pass after the one that
+    // computes it; other values wherever their operands are
+    std::vector<int> avail(k.nodes.size(), 0);
+    std::map<int, int> slots;
+    std::map<int, ManifestAt> man;
+    for (size_t i = 0; i < k.nodes.size(); ++i) {
+      const Node &n = k.nodes[i];
+      int d = 0;
+      for (int a : n.args) d = std::max(d, avail[k.at.at(a)]);
+      if (n.op == "reduce") {
+        slots[n.id] = slot;
+        (*slot_map)[{(int)ki, n.id}] = slot++;
+        d += 1;
+      } else if (k.manifest.count(n.id) && live.count(n.id)) {
+        man[n.id] = ManifestAt{d, (*ntmp)++};
+        d += 1;
+      }
+      avail[i] = d;
+    }
+    // the pass that computes a value a store, a reduce or a manifest needs
+    auto comp = [&](int id) {
+      auto mi = man.find(id);
+      return mi != man.end() ? mi->second.stage : avail[k.at.at(id)];
+    };
     int nst = 0;
     for (size_t s = 0; s < k.stores.size(); ++s) {
       if (last[k.stores[s].stat] != (int)s) continue;
       const int id = k.stores[s].node;
       if (g.statics[k.stores[s].stat].array) {
-        nst = std::max(nst, depth[k.at.at(id)] + 1);
+        nst = std::max(nst, comp(id) + 1);
         kp.stored_arrays.push_back(k.stores[s].stat);
       } else {
         kp.scalar_stores.push_back((int)s);
       }
     }
     for (const Node &n : k.nodes)
-      if (n.op == "reduce") nst = std::max(nst, depth[k.at.at(n.args[0])] + 1);
+      if (n.op == "reduce") nst = std::max(nst, comp(n.args[0]) + 1);
+    for (const auto &m : man) nst = std::max(nst, m.second.stage + 1);
     kp.stages.resize(nst);
     for (size_t s = 0; s < k.stores.size(); ++s)
       if (last[k.stores[s].stat] == (int)s && g.statics[k.stores[s].stat].array)
-        kp.stages[depth[k.at.at(k.stores[s].node)]].stores.push_back((int)s);
+        kp.stages[comp(k.stores[s].node)].stores.push_back((int)s);
     for (const Node &n : k.nodes)
-      if (n.op == "reduce") kp.stages[depth[k.at.at(n.args[0])]].reduces.push_back(n.id);
+      if (n.op == "reduce") kp.stages[comp(n.args[0])].reduces.push_back(n.id);
+    for (const auto &m : man) {
+      kp.stages[m.second.stage].manifests.push_back(m.first);
+      kp.manifest_types.push_back({m.second.tmp, k.node(m.first).type});
+    }
 
     for (int st = 0; st < nst; ++st) {
       StagePlan &sp = kp.stages[st];
       sp.fn = "om_k" + std::to_string(ki) + "_s" + std::to_string(st);
-      Emitter em(g, k, L, slots);
+      Emitter em(g, k, L, slots, &man, st);
       std::ostringstream body;
       src << "extern \"C\" __global__ void __launch_bounds__(256)\n" << sp.fn
           << "(OMPtrs P, const unsigned char *SC, unsigned char *slots, unsigned char *part,\n"
@@ -618,6 +681,7 @@ static std::string generate(const Graph &g, const Layout &L, std::vector<KernelP
       std::vector<std::string> tests;
       for (int s : sp.stores) tests.push_back(region_test(reg[k.at.at(k.stores[s].node)], L));
       for (int id : sp.reduces) tests.push_back(region_test(reg[k.at.at(k.node(id).args[0])], L));
+      for (int id : sp.manifests) tests.push_back(region_test(reg[k.at.at(id)], L));
       bool one_region = !tests.empty();
       for (const std::string &t : tests) one_region = one_region && t == tests[0];
       bool all_cells = true;
@@ -629,9 +693,10 @@ static std::string generate(const Graph &g, const Layout &L, std::vector<KernelP
       // are whole multiples of 256 V cells)
       int V = 1;
       if (shared && L.ms[0] % (256 * kCellsPerThread) == 0) {
-        Emitter trial(g, k, L, slots);
+        Emitter trial(g, k, L, slots, &man, st);
         for (int s : sp.stores) trial.value(k.stores[s].node, 0, 0);
         for (int id : sp.reduces) trial.value(k.node(id).args[0], 0, 0);
+        for (int id : sp.manifests) trial.value(id, 0, 0);
         if (std::count(trial.code.begin(), trial.code.end(), '\n') <= kMaxVectorStatements)
           V = kCellsPerThread;
       }
@@ -649,11 +714,12 @@ static std::string generate(const Graph &g, const Layout &L, std::vector<KernelP
       src << "    const long long i = (long long)c1 * " << L.ms[0] << " + c0;\n"
           << "    (void)c0; (void)c1;\n";
       if (shared) {
-        Emitter e(g, k, L, slots);
+        Emitter e(g, k, L, slots, &man, st);
         std::vector<std::string> vals;
         for (int c = 0; c < V; ++c) {
           for (int s : sp.stores) vals.push_back(e.value(k.stores[s].node, c, 0));
           for (int id : sp.reduces) vals.push_back(e.value(k.node(id).args[0], c, 0));
+          for (int id : sp.manifests) vals.push_back(e.value(id, c, 0));
         }
         src << "    {\n" << e.code;
         size_t v = 0;
@@ -667,14 +733,26 @@ static std::string generate(const Graph &g, const Layout &L, std::vector<KernelP
             src << "      " << acc << " = " << combine(k.node(sp.reduces[r]).sarg, acc, vals[v++])
                 << ";\n";
           }
+          for (int id : sp.manifests)
+            src << "      ((" << ctype(k.node(id).type) << " *)P.tmp[" << man.at(id).tmp << "])["
+                << at << "] = " << vals[v++] << ";\n";
         }
         src << "    }\n";
       } else {
+        // a manifest is written on its region (other cells are never read)
+        for (int id : sp.manifests) {
+          const std::string T = ctype(k.node(id).type);
+          Emitter e(g, k, L, slots, &man, st);
+          const std::string val = e.value(id, 0, 0);
+          src << "    {\n      if (" << region_test(reg[k.at.at(id)], L) << ") {\n" << e.code
+              << "      ((" << T << " *)P.tmp[" << man.at(id).tmp << "])[i] = " << val << ";\n"
+              << "      }\n    }\n";
+        }
         for (int s : sp.stores) {
           const Store &so = k.stores[s];
           const Node &v = k.node(so.node);
           const std::string T = ctype(v.type);
-          Emitter e(g, k, L, slots);
+          Emitter e(g, k, L, slots, &man, st);
           const std::string val = e.value(so.node, 0, 0);
           src << "    {\n      " << T << " out = (" << T << ")0;\n"
               << "      if (" << region_test(reg[k.at.at(so.node)], L) << ") {\n"
@@ -685,7 +763,7 @@ static std::string generate(const Graph &g, const Layout &L, std::vector<KernelP
         for (size_t r = 0; r < sp.reduces.size(); ++r) {
           const Node &n = k.node(sp.reduces[r]);
           const int in = n.args[0];
-          Emitter e(g, k, L, slots);
+          Emitter e(g, k, L, slots, &man, st);
           const std::string val = e.value(in, 0, 0);
           const std::string acc = "acc" + std::to_string(r);
           src << "    {\n      if (" << region_test(reg[k.at.at(in)], L) << ") {\n" << e.code
@@ -762,10 +840,15 @@ static std::string generate(const Graph &g, const Layout &L, std::vector<KernelP
 // the handle kind
 // ---------------------------------------------------------------------------
 
+// at most this many manifest values in use across a graph's kernels
+constexpr int kMaxManifests = 64;
+
 struct GraphState {
   Graph g;
   Layout L;
   std::vector<KernelPlan> plans;
+  std::vector<Type> tmp_types;   // element type of each manifest array
+  std::vector<void *> tmp;       // the manifest arrays (memory-sized)
   cudaLibrary_t lib = nullptr;
   std::vector<std::vector<cudaKernel_t>> stage_k;
   std::vector<cudaKernel_t> commit_k;
@@ -784,6 +867,7 @@ static void graph_free(Handle *h) {
   GraphState *st = gst(h);
   if (!st) return;
   if (st->lib) cudaLibraryUnload(st->lib);
+  for (void *p : st->tmp) cudaFree(p);
   cudaFree(st->slots);
   cudaFree(st->part);
   cudaFree(st->done);
@@ -794,6 +878,7 @@ static void graph_free(Handle *h) {
 struct OMPtrs {
   const void *cur[32];
   void *nxt[32];
+  void *tmp[kMaxManifests];
 };
 
 static om_status graph_run(Handle *h, int n) {
@@ -807,6 +892,7 @@ static om_status graph_run(Handle *h, int n) {
       P.cur[a] = h->arrays[a].d();
       P.nxt[a] = h->arrays[a].d_next();
     }
+    for (size_t t = 0; t < st->tmp.size(); ++t) P.tmp[t] = st->tmp[t];
     unsigned char *SC = (unsigned char *)h->d_scalars;
     for (size_t s = 0; s < kp.stages.size(); ++s) {
       unsigned int *done = st->done + st->done_index[ki][s];
@@ -921,7 +1007,16 @@ static om_status plan(GraphState *st, int *nslots) {
   }
   std::map<std::pair<int, int>, int> slot_map;
   st->plans.clear();
-  st->source = generate(g, L, &st->plans, &slot_map, nslots);
+  int ntmp = 0;
+  st->source = generate(g, L, &st->plans, &slot_map, nslots, &ntmp);
+  if (ntmp > kMaxManifests) {
+    set_error("om_create_graph: at most " + std::to_string(kMaxManifests) +
+              " manifest values in use");
+    return OM_ERR_UNSUPPORTED;
+  }
+  st->tmp_types.assign(ntmp, TInt);
+  for (const KernelPlan &kp : st->plans)
+    for (const auto &m : kp.manifest_types) st->tmp_types[m.first] = m.second;
   return OM_OK;
 }
 
@@ -960,6 +1055,16 @@ static om_status graph_setup(Handle *h, void *ctx) {
       maxred = std::max(maxred, (int)sp.reduces.size());
       st->done_index[k].push_back(nstages++);
     }
+  for (Type t : st->tmp_types) {
+    void *p = nullptr;
+    if (injected_alloc_failure() ||
+        cudaMalloc(&p, (size_t)tsize(t) * h->memory_size_total()) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("om_create_graph: cannot allocate the manifest arrays");
+      return OM_ERR_NOMEM;
+    }
+    st->tmp.push_back(p);
+  }
   if (cudaMalloc(&st->slots, 8 * (size_t)std::max(nslots, 1)) != cudaSuccess ||
       cudaMalloc(&st->part, 8 * (size_t)maxred * st->grid) != cudaSuccess ||
       cudaMalloc(&st->done, sizeof(unsigned int) * std::max(nstages, 1)) != cudaSuccess ||

@@ -225,6 +225,16 @@ class Kernel:
     def bind(self, v: Value) -> Value:
         return v
 
+    def manifest(self, v: Value) -> Value:
+        """Anot.add Alloc.Manifest <?> v: the value is computed once per
+        kernel run into an array that later uses read (at any shift), instead
+        of being recomputed where it is used (Alloc.Delayed).  The values are
+        the same either way."""
+        if v.realm != "array":
+            raise OMGraphError("manifest of an array value")
+        self.lines.append(f"manifest {v.node}")
+        return v
+
     def __enter__(self):
         return self
 

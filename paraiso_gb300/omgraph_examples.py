@@ -237,7 +237,8 @@ def hydro(size=(1024, 1024), gamma=5.0 / 3.0, boundary="open", typ=og.Double) ->
                       k.imm(0.6, T))
     out_of = ((icoord[0] < 0) | (icoord[1] < 0)) | ((icoord[0] >= isize[0]) |
                                                     (icoord[1] >= isize[1]))
-    cell = _zip_records([jet, cell0], lambda a, b: og.select(out_of, a, b))
+    # Anot.add Alloc.Manifest <?> (select outOf a b), per field
+    cell = _zip_records([jet, cell0], lambda a, b: k.manifest(og.select(out_of, a, b)))
 
     # CFL (HydroMain.hs:150-154)
     ts = [dR[i] / (cell.sound + og.abs_(cell.velocity[i])) for i in range(2)]
@@ -300,9 +301,9 @@ def hydro(size=(1024, 1024), gamma=5.0 / 3.0, boundary="open", typ=og.Double) ->
         lesta = star(shock_star, shock_l, left)
         rista = star(shock_star, shock_r, right)
 
-        def selector(a, b, c, d):
-            return og.select(0 < shock_l, a,
-                             og.select(0 < shock_star, b, og.select(0 < shock_r, c, d)))
+        def selector(a, b, c, d):   # Anot.add Alloc.Manifest <?> select ...
+            return k.manifest(og.select(0 < shock_l, a,
+                                        og.select(0 < shock_star, b, og.select(0 < shock_r, c, d))))
         return _zip_records([left, lesta, rista, right], selector)
 
     def add_flux(dt_, dR_, wall, ex, rec):

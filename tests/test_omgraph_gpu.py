@@ -242,3 +242,46 @@ def test_semantics_graph_long_rows(om_lib, boundary):
     assert_same(g, m, ["i", "b", "smin", "ssum", "f"])
     assert_same(g, m, ["d", "smax"], rtol=1e-12)
     g.close()
+
+
+def manifest_graph(boundary, mark):
+    """Values marked Manifest (computed once into an array) and read at
+    shifts, by a second manifest, a reduce and stores; unmarked, the same
+    graph recomputes them where they are used."""
+    om = og.OM("Man", (70, 41), boundary)
+    a = om.static_array("a", og.Double)
+    b = om.static_array("b", og.Double)
+    s = om.static_scalar("s", og.Double)
+    k = om.kernel("step")
+    x = k.load(a)
+    m1 = x * 2 + k.shift(x, (1, 0))
+    if mark:
+        k.manifest(m1)
+    m2 = k.shift(m1, (0, -1)) - k.shift(m1, (-2, 1)) * 0.5
+    if mark:
+        k.manifest(m2)
+    r = k.reduce("sum", m2)
+    k.store(b, m2 + k.broadcast(r) * 1e-3 + k.shift(m1, (1, 1)))
+    k.store(a, m1)
+    k.store(s, r)
+    return om
+
+
+@pytest.mark.parametrize("boundary", ["cyclic", "open"])
+def test_manifests(om_lib, boundary):
+    rng = np.random.default_rng(5)
+    out = []
+    for mark in (True, False):
+        om = manifest_graph(boundary, mark)
+        m0 = R.Machine(om.to_text())
+        init = {"a": rng.standard_normal(m0.shape)} if not out else {"a": out[0][2]}
+        g, m = both(om_lib, om, ["step", "step"], init=init)
+        if mark:
+            assert "P.tmp[" in g.source
+        assert_same(g, m, ["a"])
+        assert_same(g, m, ["b", "s"], rtol=1e-12)
+        out.append((g.read("a"), g.read("b"), init["a"], g.get_scalar("s")))
+        g.close()
+    # marked or not, the executor computes the same values
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert out[0][3] == out[1][3]
