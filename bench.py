@@ -6,7 +6,7 @@ int32 cells Bernoulli(0.3) from seed 1; one step = 100 generations with the
 population reduce after every generation.  Metric: Gcell-updates/s.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload life16k|life128|lifegraph|hydro4k|ensemble|adjoint]
+                  [--workload life16k|life128|lifegraph|hydro4k|hydrograph|ensemble|adjoint]
 
 Prints one JSON line (rank 0).  Under torchrun (N > 1) every rank advances
 its own independent replica (no data-path collective; weak scaling).
@@ -305,6 +305,68 @@ def lifegraph_workload(args, dist: Dist) -> dict:
         "roofline": {"bound": "hbm", "kernel": "om_k1_s0 (generated)", "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 3),
                      "traffic": None, "algorithmic_bytes_per_launch": 8.0 * cells},
+        "gpu_launches": launches, "clocks": clk,
+    }
+
+
+def hydrograph_workload(args, dist: Dist) -> dict:
+    """examples/Hydro (HydroMain.hs with its Manifest annotations) as a
+    general OM graph, compiled at run time, on the Hydro 4096^2 periodic
+    Kelvin-Helmholtz workload in FP32.  Also checks a few steps against the
+    hand-written exact FP32 step (both compute without multiply-add
+    contraction in the generator's operation order)."""
+    import numpy as np
+    import paraiso_gb300 as pg
+    from paraiso_gb300 import build as pgbuild
+    from paraiso_gb300 import omgraph as og
+    from paraiso_gb300 import omgraph_examples as ex
+    pgbuild.build()
+    n = args.size or 4096
+    cells = n * n
+    h = pg.Hydro((n, n), precision=32, variant=2, gamma=1.4, device=dist.local_rank)
+    h.init_kh(1 + dist.rank)
+    h.set_scalar("cfl", 0.4)
+    st = h.state()
+    m = pg.GraphMachine(ex.hydro((n, n), 1.4, "cyclic", og.Float), device=dist.local_rank)
+    f = np.float32
+    for name, v in (("cfl", f(0.4)), ("dR0", f(1) / f(n)), ("dR1", f(1) / f(n)),
+                    ("extent0", f(1)), ("extent1", f(1)), ("time", f(0))):
+        m.set_scalar(name, float(v))
+    for name, a in zip(("density", "velocity0", "velocity1", "pressure"), st):
+        m.write(name, a)
+    check = 5
+    m.run("proceed", check)
+    h.proceed(check)
+    same = all(np.array_equal(m.read(k), a)
+               for k, a in zip(("density", "velocity0", "velocity1", "pressure"), h.state()))
+    h.close()
+    m.run("proceed", max(args.warmup, 1))
+    clocks = ClockSampler(dist.local_rank)
+    clocks.start()
+    dist.barrier()
+    ms = m.time_run("proceed", args.steps)
+    launches = m.last_launch_count()
+    dist.barrier()
+    clk = clocks.stop()
+    ms = dist.max(ms)
+    value = cells * args.steps * dist.world / (ms * 1e-3) / 1e9
+    peak, _ = peaks()
+    achieved = 32.0 * cells / (ms / args.steps * 1e-3) / 1e9
+    m.close()
+    return {
+        "metric": "Hydro cell-updates/s (Gcell-updates/s) through the general OM graph executor",
+        "value": round(value, 3), "unit": "Gcell-updates/s", "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"examples/Hydro graph (HydroMain.hs, Manifest annotations) {n}x{n} "
+                               "periodic Kelvin-Helmholtz, gamma 1.4, CFL 0.4, FP32",
+                   "n0": n, "n1": n, "parallelism": f"replicas x{dist.world}"},
+        "bit_identical_to_exact_fused_step": {"steps": check, "equal": bool(same)},
+        "roofline": {"bound": "hbm", "kernel": "om_k1_s* (generated)", "achieved": round(achieved, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 3),
+                     "traffic": None, "algorithmic_bytes_per_launch": 32.0 * cells,
+                     "note": "state in + out per step; the manifest arrays add traffic"},
         "gpu_launches": launches, "clocks": clk,
     }
 
@@ -635,7 +697,7 @@ def reference_arm(args, dist: Dist) -> dict | None:
     if args.workload == "adjoint":
         return {"impl": "reference",
                 "unavailable": "the reference has no adjoint of the Hydro step to time"}
-    if args.workload in ("hydro4k", "ensemble"):
+    if args.workload in ("hydro4k", "hydrograph", "ensemble"):
         return reference_hydro(args, dist)
     from oracle import pyoracle as O
     O.build()
@@ -683,10 +745,12 @@ def reference_hydro(args, dist: Dist) -> dict:
     import paraiso_gb300 as pg
     from oracle import pyoracle as O
     O.build()
-    if args.workload == "hydro4k":
+    if args.workload in ("hydro4k", "hydrograph"):
         n = args.size or 4096
         grids = [(n, n, 1)]
-        metric = "Hydro cell-updates/s (Gcell-updates/s), FP32 bulk, FP64 dt/totals"
+        metric = ("Hydro cell-updates/s (Gcell-updates/s) through the general OM graph executor"
+                  if args.workload == "hydrograph"
+                  else "Hydro cell-updates/s (Gcell-updates/s), FP32 bulk, FP64 dt/totals")
         workload = f"hydro {n}x{n} periodic Kelvin-Helmholtz, gamma 1.4, CFL 0.4"
     else:
         sizes = pg.ensemble_sizes(args.count, 1)
@@ -733,7 +797,8 @@ def main() -> int:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="life16k",
-                    choices=["life16k", "life128", "lifegraph", "hydro4k", "ensemble", "adjoint"])
+                    choices=["life16k", "life128", "lifegraph", "hydro4k", "hydrograph",
+                             "ensemble", "adjoint"])
     ap.add_argument("--adj-steps", type=int, default=200)
     ap.add_argument("--adj-precision", type=int, default=32)
     ap.add_argument("--tie-noise", type=float, default=0.0)
@@ -767,6 +832,8 @@ def main() -> int:
             out = adjoint_workload(args, dist)
         elif args.workload == "lifegraph":
             out = lifegraph_workload(args, dist)
+        elif args.workload == "hydrograph":
+            out = hydrograph_workload(args, dist)
         else:
             out = life_workload(args, dist)
         if out is not None and dist.rank == 0:

@@ -282,6 +282,9 @@ om_status om_hydro_write_snapshot(om_handle h, const char *path);
  *     div mod neg inv not and or eq ne lt le gt ge select max min abs signum
  *     sqrt exp log sin cos tan asin acos atan atan2 pow cast)
  *   store STATIC NODE
+ *   manifest NODE     (Alloc.Manifest: the array value is computed once per
+ *                      run into a temporary array that later passes read,
+ *                      instead of being recomputed where it is used)
  *   end
  *
  * (paraiso_gb300/omgraph.py writes it from Builder-style Python.)  The

@@ -287,32 +287,6 @@ om_status hydro_tsmin_device(Handle *h, unsigned long long **ptr) {
   return OM_OK;
 }
 
-// dt of the next step and the CFL minimum bits of the current state
-om_status hydro_current_dt(Handle *h, double *dt, unsigned long long *bits) {
-  HydroState *st = hst(h);
-  OM_TRY(upload_scalars(h));
-  OM_TRY(ensure_tsmin(h));
-  unsigned long long b = 0;
-  OM_CUDA_CHECK(cudaMemcpyAsync(&b, &hsc_dev(h)->tsmin[st->slot], sizeof(b),
-                                cudaMemcpyDeviceToHost, h->stream));
-  OM_CUDA_CHECK(cudaStreamSynchronize(h->stream));
-  // keep the host mirror's copy of the slot consistent with the device
-  hsc_host(h)->tsmin[st->slot] = b;
-  const double cfl = hsc_host(h)->cfl;
-  if (st->fp64) {
-    double t;
-    std::memcpy(&t, &b, sizeof(t));
-    *dt = cfl * t;
-  } else {
-    const uint32_t lo = (uint32_t)b;
-    float t;
-    std::memcpy(&t, &lo, sizeof(t));
-    *dt = (double)((float)cfl * t);
-  }
-  *bits = b;
-  return OM_OK;
-}
-
 struct HydroCkState {
   bool ts_valid;
   int slot;

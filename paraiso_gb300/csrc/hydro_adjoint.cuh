@@ -333,25 +333,8 @@ __device__ __forceinline__ void cons_of_prim_rev(R g, const Prim<R> &b, const R 
 }
 
 // The update's new conserved state (d2, b0, b1, e2) before the primitive
-// recovery, with the same operation order as hs::update.
-template <class R>
-__device__ __forceinline__ void update_cons(R g, const Prim<R> &b, R dtdx0, R dtdx1,
-                                            const Flux<R> &l0, const Flux<R> &r0,
-                                            const Flux<R> &l1, const Flux<R> &r1, R out[4]) {
-  const R m0 = b.rho * b.v0, m1 = b.rho * b.v1;
-  const R e = hs::kinetic(b.v0, b.v1, m0, m1) + (R(1) / (g - R(1))) * b.p;
-  const R d1 = b.rho + dtdx1 * (l1.fd - r1.fd);
-  const R a0 = m0 + dtdx1 * (l1.fm0 - r1.fm0);
-  const R a1 = m1 + dtdx1 * (l1.fm1 - r1.fm1);
-  const R e1 = e + dtdx1 * (l1.fe - r1.fe);
-  out[0] = d1 + dtdx0 * (l0.fd - r0.fd);
-  out[1] = a0 + dtdx0 * (l0.fm0 - r0.fm0);
-  out[2] = a1 + dtdx0 * (l0.fm1 - r0.fm1);
-  out[3] = e1 + dtdx0 * (l0.fe - r0.fe);
-}
-
-// update_cons from the taped flux differences D (D[4 * axis + k], left
-// wall - right wall), in the same operation order
+// recovery, from the taped flux differences D (D[4 * axis + k], left wall -
+// right wall), with the same operation order as hs::update
 template <class R>
 __device__ __forceinline__ void update_cons_d(R g, const Prim<R> &b, R dtdx0, R dtdx1,
                                               const R D[8], R out[4]) {

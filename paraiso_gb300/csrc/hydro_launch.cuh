@@ -80,8 +80,6 @@ om_status hydro_checkpoint_alloc(Handle *h, HydroCheckpoint *c);
 void hydro_checkpoint_free(HydroCheckpoint *c);
 om_status hydro_save(Handle *h, HydroCheckpoint *c);
 om_status hydro_restore(Handle *h, const HydroCheckpoint *c);
-// dt of the next step and the CFL minimum bits of the current state
-om_status hydro_current_dt(Handle *h, double *dt, unsigned long long *bits);
 // the device address of the CFL minimum of h's current state (computed first
 // when the cached one does not belong to it)
 om_status hydro_tsmin_device(Handle *h, unsigned long long **ptr);
