@@ -10,6 +10,10 @@
 // one: 1024 x 1024 with the open boundary of the generator's default setup
 // (Language/Paraiso/Generator/Native.hs:36): 3-cell margins that take the
 // jet state every step (HydroMain.hs:105-131).
+//
+// The earlier generator's members (static_0_generation .. static_10_pressure,
+// size0(), memorySize0(), lowerMargin0(), ...) are here too, so
+// examples/Hydro/main-kh.cu builds unchanged as well.
 #pragma once
 
 #include "om_shim.hpp"
@@ -26,7 +30,12 @@ class Hydro : public om_shim::machine {
   Hydro(int n0, int n1, double gamma = 5.0 / 3.0, int boundary = OM_BOUNDARY_OPEN)
       : om_shim::machine(OM_KIND_HYDRO, n0, n1, config(gamma, boundary)),
         density_(h_, "density"), velocity0_(h_, "velocity0"),
-        velocity1_(h_, "velocity1"), pressure_(h_, "pressure") {}
+        velocity1_(h_, "velocity1"), pressure_(h_, "pressure"),
+        static_0_generation(h_, "generation"), static_1_time(h_, "time"),
+        static_2_cfl(h_, "cfl"), static_3_dR0(h_, "dR0"), static_4_dR1(h_, "dR1"),
+        static_5_extent0(h_, "extent0"), static_6_extent1(h_, "extent1"),
+        static_7_density(h_, "density"), static_8_velocity0(h_, "velocity0"),
+        static_9_velocity1(h_, "velocity1"), static_10_pressure(h_, "pressure") {}
 
   int &generation() { return scalar<int>("generation"); }
   double &time() { return scalar<double>("time"); }
@@ -49,6 +58,17 @@ class Hydro : public om_shim::machine {
   void proceed() { run("proceed"); }
 
  private:
+  om_shim::host_array<Real> density_, velocity0_, velocity1_, pressure_;
+
+ public:
+  // the earlier generator's statics (examples-old/Hydro-exampled/dist/Hydro.hpp)
+  om_shim::scalar_member<int> static_0_generation;
+  om_shim::scalar_member<double> static_1_time, static_2_cfl, static_3_dR0, static_4_dR1,
+      static_5_extent0, static_6_extent1;
+  om_shim::array_member<Real> static_7_density, static_8_velocity0, static_9_velocity1,
+      static_10_pressure;
+
+ private:
   static om_config config(double gamma, int boundary) {
     om_config c;
     om_config_default(&c);
@@ -61,5 +81,4 @@ class Hydro : public om_shim::machine {
 #endif
     return c;
   }
-  om_shim::host_array<Real> density_, velocity0_, velocity1_, pressure_;
 };

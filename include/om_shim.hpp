@@ -8,6 +8,7 @@
 #include <cstddef>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 
 #include "om_gb300.h"
 
@@ -49,6 +50,42 @@ template <class T> class host_array {
   const char *name_;
 };
 
+// The earlier generator's public static members (static_<i>_<name>, the
+// i-th static of the OM; examples-old/*/dist/*.hpp): a Scalar reads and
+// writes through the handle's host scalar block, an Array indexes the host
+// copy and converts to any container built from an iterator pair (the
+// drivers copy it into std::vector or thrust::host_vector).
+template <class T> class scalar_member {
+ public:
+  scalar_member(om_handle h, const char *name) : h_(h), name_(name) {}
+  operator T() const { return *ptr(); }
+  scalar_member &operator=(T v) {
+    *ptr() = v;
+    return *this;
+  }
+  scalar_member &operator=(const scalar_member &o) { return *this = (T)o; }
+
+ private:
+  T *ptr() const {
+    void *p;
+    check(om_scalar_ptr(h_, name_, &p, nullptr), name_);
+    return static_cast<T *>(p);
+  }
+  om_handle h_;
+  const char *name_;
+};
+
+template <class T> class array_member : public host_array<T> {
+ public:
+  array_member(om_handle h, const char *name) : host_array<T>(h, name) {}
+  template <class V, class = typename std::enable_if<
+                         std::is_constructible<V, const T *, const T *>::value>::type>
+  operator V() const {
+    const T *b = this->cdata();
+    return V(b, b + this->size());
+  }
+};
+
 // Common part of a generated OM class: the handle, sizes, margins, kernels.
 class machine {
  public:
@@ -74,6 +111,17 @@ class machine {
   int om_lower_margin_1() { return q(::om_lower_margin, 1); }
   int om_upper_margin_0() { return q(::om_upper_margin, 0); }
   int om_upper_margin_1() { return q(::om_upper_margin, 1); }
+  // the earlier generator's names for the same
+  int size() { return om_size(); }
+  int size0() { return om_size_0(); }
+  int size1() { return om_size_1(); }
+  int memorySize() { return om_memory_size(); }
+  int memorySize0() { return om_memory_size_0(); }
+  int memorySize1() { return om_memory_size_1(); }
+  int lowerMargin0() { return om_lower_margin_0(); }
+  int lowerMargin1() { return om_lower_margin_1(); }
+  int upperMargin0() { return om_upper_margin_0(); }
+  int upperMargin1() { return om_upper_margin_1(); }
 
   om_handle handle() const { return h_; }
 

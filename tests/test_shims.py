@@ -116,3 +116,23 @@ def test_graph_driver_runs_shift_example(om_lib, tmp_path, boundary):
         want.append("value: " + " ".join(str(v) for v in m.values["table"].ravel()))
     want.append(f"total: {int(m.values['total'])}")
     assert out == want
+
+
+@pytest.mark.skipif(not os.path.isdir(REFERENCE_TREE), reason="reference tree not present")
+@pytest.mark.parametrize("driver", ["examples/Life/main.cu", "examples/Hydro/main-kh.cu"])
+def test_reference_earlier_api_drivers_compile_unchanged(om_lib, tmp_path, driver):
+    # the drivers written against the earlier generator's class (public
+    # static_<i>_<name> members, memorySize0(), ...; thrust on the host)
+    import shutil
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    subprocess.run([nvcc, "-std=c++17", os.path.join(REFERENCE_TREE, driver), f"-I{INC}",
+                    f"-L{LIBDIR}", "-lom_gb300", "-Xlinker", f"-rpath={LIBDIR}",
+                    "-o", str(tmp_path / "drv")], check=True)
+
+
+@pytest.mark.gpu
+def test_earlier_api_driver_runs(om_lib, tmp_path):
+    exe = compile_cpp(os.path.join(ROOT, "tests", "cpp", "old_api_driver.cpp"), "old_api",
+                      tmp_path)
+    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
+    assert out.strip().endswith("ok"), out
