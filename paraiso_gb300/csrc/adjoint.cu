@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -598,8 +599,10 @@ static void free_scratch(AdjointScratch *s) {
   delete s;
 }
 
-// scratch hangs off the handle's kind state through a small registry
+// scratch hangs off the handle through a small registry (handles of other
+// threads may look it up at the same time)
 static std::vector<std::pair<Handle *, AdjointScratch *>> g_scratch;
+static std::mutex g_scratch_mu;
 
 template <class R> static cudaError_t allow_tile_smem() {
   constexpr int TX = adj::AdjTile<R>::TX, TY = adj::AdjTile<R>::TY;
@@ -613,6 +616,7 @@ static om_status get_scratch(Handle *h, int fp64, AdjointScratch **out) {
     set_error("Hydro adjoint: periodic grids only");
     return OM_ERR_UNSUPPORTED;
   }
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
   for (auto &kv : g_scratch)
     if (kv.first == h) {
       *out = kv.second;
@@ -660,6 +664,7 @@ static om_status get_scratch(Handle *h, int fp64, AdjointScratch **out) {
 }
 
 void adjoint_release(Handle *h) {
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
   for (size_t i = 0; i < g_scratch.size(); ++i)
     if (g_scratch[i].first == h) {
       free_scratch(g_scratch[i].second);
