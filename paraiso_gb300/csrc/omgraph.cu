@@ -356,7 +356,8 @@ static std::string lit(Type t, const std::string &s) {
 }
 
 // A stage whose per-cell code has at most kMaxVectorStatements statements
-// evaluates kCellsPerThread cells per thread.
+// evaluates kCellsPerThread cells per thread (eight per thread measured
+// slower on the Life graph: 233 against 364 Gcell-updates/s).
 constexpr int kCellsPerThread = 4;
 constexpr int kMaxVectorStatements = 400;
 
