@@ -182,13 +182,27 @@ template <class R, int TX, int TY> struct Stage2Smem {
   static constexpr int SLOTS = (TY * XF > YF * TX) ? TY * XF : YF * TX;
   R q[4][QY][QX];
   R u[4][UY][UX];
-  R slot[16][SLOTS];  // [slot * 4 + field][face]
+  R slot[16][SLOTS];  // [slot * 4 + field][face]; first the box inputs
   R qx[4][TY][TX];
+  static_assert(8 * UY * UX <= 16 * SLOTS, "the box inputs are staged in the slot buffer");
 };
 
 template <class R> struct AdjOcc;  // CTAs per SM the tile kernels are built for
 template <> struct AdjOcc<float> { static constexpr int stage2 = 3, stage1 = 4; };
 template <> struct AdjOcc<double> { static constexpr int stage2 = 2, stage1 = 2; };
+
+// 4- or 8-byte asynchronous copy global -> shared (cp.async, sm_80 and later)
+template <class R>
+__device__ __forceinline__ void cp_async(R *dst, const R *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  if (sizeof(R) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
 
 // MUSCL reverse of the four fields of one face into its 16 slot values
 template <class R>
@@ -243,12 +257,26 @@ adj_stage2_tile(Fields<R> Ub, Fields<R> U1b, Fields<R> Pbase, Geo<R> G, double *
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int nt0 = (G.n0 + TX - 1) / TX;
   const int X0 = (int)(blockIdx.x % nt0) * TX, Y0 = (int)(blockIdx.x / nt0) * TY;
+  // the stage-1 state box, and the stage-2 box's taped conserved state and
+  // incoming cotangent (staged in the slot buffer, free until the faces),
+  // copied asynchronously in one batch
+  R(*stg)[S::UY][S::UX] = reinterpret_cast<R(*)[S::UY][S::UX]>(&s.slot[0][0]);
   for (int i = tid; i < S::QY * S::QX; i += nthr) {
     const int by = i / S::QX, bx = i - by * S::QX;
     const size_t gi = G.at(X0 - 3 + bx, Y0 - 3 + by);
 #pragma unroll
-    for (int c = 0; c < 4; ++c) s.q[c][by][bx] = Q.f[c][gi];
+    for (int c = 0; c < 4; ++c) cp_async(&s.q[c][by][bx], &Q.f[c][gi]);
   }
+  for (int i = tid; i < S::UY * S::UX; i += nthr) {
+    const int by = i / S::UX, bx = i - by * S::UX;
+    const size_t gi = G.at(X0 - 2 + bx, Y0 - 2 + by);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      cp_async(&stg[c][by][bx], &U2.f[c][gi]);
+      cp_async(&stg[4 + c][by][bx], &Ub.f[c][gi]);
+    }
+  }
+  cp_async_wait_all();
   const R d0 = G.dt / G.dR0, d1 = G.dt / G.dR1;
   // the previous reverse step's dt cotangent, when its arg-min cell lies in
   // this tile's stage-2 box (blocks that find it compute the same value)
@@ -285,10 +313,8 @@ adj_stage2_tile(Fields<R> Ub, Fields<R> U1b, Fields<R> Pbase, Geo<R> G, double *
   for (int i = tid; i < S::UY * S::UX; i += nthr) {
     const int by = i / S::UX, bx = i - by * S::UX;
     const size_t gi = G.at(X0 - 2 + bx, Y0 - 2 + by);
-    const Prim<R> u_ = U2.get(gi);
-    const R u[4] = {u_.rho, u_.v0, u_.v1, u_.p};
-    const Prim<R> qb_ = Ub.get(gi);
-    PrimBar<R> qb{qb_.rho, qb_.v0, qb_.v1, qb_.p};
+    const R u[4] = {stg[0][by][bx], stg[1][by][bx], stg[2][by][bx], stg[3][by][bx]};
+    PrimBar<R> qb{stg[4][by][bx], stg[5][by][bx], stg[6][by][bx], stg[7][by][bx]};
     if (gi == pend_j) {
       qb.rho += pend[0]; qb.v0 += pend[1]; qb.v1 += pend[2]; qb.p += pend[3];
     }
