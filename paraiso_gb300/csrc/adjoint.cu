@@ -191,6 +191,14 @@ template <class R> struct AdjOcc;  // CTAs per SM the tile kernels are built for
 template <> struct AdjOcc<float> { static constexpr int stage2 = 3, stage1 = 4; };
 template <> struct AdjOcc<double> { static constexpr int stage2 = 2, stage1 = 2; };
 
+// Wait until the kernel launched before this one on the stream has finished
+// and its writes are visible (a no-op unless this kernel was launched with
+// programmatic stream serialization, when it may start while that one
+// drains).
+__device__ __forceinline__ void wait_previous_kernel() {
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
+}
+
 // 4- or 8-byte asynchronous copy global -> shared (cp.async, sm_80 and later)
 template <class R>
 __device__ __forceinline__ void cp_async(R *dst, const R *src) {
@@ -250,6 +258,7 @@ adj_stage2_tile(Fields<R> Ub, Fields<R> U1b, Fields<R> Pbase, Geo<R> G, double *
   __shared__ double sh[8];
   __shared__ unsigned long long pend_j;
   __shared__ R pend[4];
+  wait_previous_kernel();
   G.dt = G.step_dt();
   const Fields<R> P = G.state();
   const TapeView<R> T = G.tape();
@@ -427,24 +436,34 @@ adj_stage2_tile(Fields<R> Ub, Fields<R> U1b, Fields<R> Pbase, Geo<R> G, double *
   if (tid == 0) partial[blockIdx.x] = sum;
 }
 
-// E+F on one TX x TY tile: the face cotangents (left-state part 0..3,
+// E+F on one TX x TY tile (release: the other parity's arg-min slots, reset
+// for the next step): the face cotangents (left-state part 0..3,
 // right-state part 4..7) of x faces X0 .. X0+TX of each tile row and y faces
 // Y0 .. Y0+TY of each tile column, then per tile cell the previous-state
 // cotangent = base part + its own walls (right state) + the next walls
 // (left state), and the lowest index whose CFL timescale equals the minimum
 // (the arg-min that receives the dt cotangent; ties go to the lowest index).
 template <class R, int TX, int TY> struct Stage1Smem {
-  static constexpr int XF = TX + 1, YF = TY + 1;
+  static constexpr int XF = TX + 1, YF = TY + 1, BX = TX + 2, BY = TY + 2;
   R fx[8][TY][XF];
   R fy[8][YF][TX];
+  // the state (0..3) and the stage-1 cotangent (4..7) of cells X0-1 .. X0+TX,
+  // Y0-1 .. Y0+TY
+  R box[8][BY][BX];
 };
 
 template <class R, int TX, int TY>
 __global__ void __launch_bounds__(256, AdjOcc<R>::stage1)
 adj_stage1_tile(Fields<R> U1b, Fields<R> Pbase, Fields<R> Pb, Geo<R> G,
-                const unsigned long long *minbits, unsigned long long *argmin) {
+                const unsigned long long *minbits, unsigned long long *argmin,
+                unsigned long long *release) {
   using S = Stage1Smem<R, TX, TY>;
-  __shared__ S s;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  S &s = *reinterpret_cast<S *>(smem_raw);
+  wait_previous_kernel();
+  // the other parity's arg-min and minimum: read by this step's C+D kernel
+  // (the pending dt of the step before), free now for the next step
+  if (blockIdx.x == 0 && threadIdx.x == 0) release[0] = release[1] = ~0ull;
   G.dt = G.step_dt();
   const Fields<R> P = G.state();
   const int tid = threadIdx.x, nthr = blockDim.x;
@@ -452,6 +471,24 @@ adj_stage1_tile(Fields<R> U1b, Fields<R> Pbase, Fields<R> Pb, Geo<R> G,
   const int X0 = (int)(blockIdx.x % nt0) * TX, Y0 = (int)(blockIdx.x / nt0) * TY;
   const R h = G.dt / R(2);
   const R d0 = h / G.dR0, d1 = h / G.dR1;
+  // the box, copied asynchronously in one batch
+  for (int i = tid; i < S::BY * S::BX; i += nthr) {
+    const int by = i / S::BX, bx = i - by * S::BX;
+    const size_t gi = G.at(X0 - 1 + bx, Y0 - 1 + by);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      cp_async(&s.box[c][by][bx], &P.f[c][gi]);
+      cp_async(&s.box[4 + c][by][bx], &U1b.f[c][gi]);
+    }
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  auto state = [&](int bx, int by) {
+    return Prim<R>{s.box[0][by][bx], s.box[1][by][bx], s.box[2][by][bx], s.box[3][by][bx]};
+  };
+  auto cot = [&](int bx, int by) {
+    return Prim<R>{s.box[4][by][bx], s.box[5][by][bx], s.box[6][by][bx], s.box[7][by][bx]};
+  };
   constexpr int NXF = TY * S::XF, NYF = S::YF * TX;
   for (int i = tid; i < NXF + NYF; i += nthr) {
     PrimBar<R> Lb, Rb;
@@ -459,24 +496,24 @@ adj_stage1_tile(Fields<R> U1b, Fields<R> Pbase, Fields<R> Pb, Geo<R> G,
     ha::zero(Rb);
     int r, j;
     if (i < NXF) {
+      // x face left of cell (X0 + j, Y0 + r): box cells (j + 1, r + 1), (j, r + 1)
       r = i / S::XF;
       j = i - r * S::XF;
-      const size_t ic = G.at(X0 + j, Y0 + r), im = G.at(X0 + j - 1, Y0 + r);
-      const Prim<R> a = U1b.get(ic), c = U1b.get(im);
+      const Prim<R> a = cot(j + 1, r + 1), c = cot(j, r + 1);
       const Flux<R> fb{d0 * (a.rho - c.rho), d0 * (a.v0 - c.v0), d0 * (a.v1 - c.v1),
                        d0 * (a.p - c.p)};
-      ha::hllc_rev<0>(G.g, P.get(im), P.get(ic), fb, Lb, Rb);
+      ha::hllc_rev<0>(G.g, state(j, r + 1), state(j + 1, r + 1), fb, Lb, Rb);
       s.fx[0][r][j] = Lb.rho; s.fx[1][r][j] = Lb.v0; s.fx[2][r][j] = Lb.v1; s.fx[3][r][j] = Lb.p;
       s.fx[4][r][j] = Rb.rho; s.fx[5][r][j] = Rb.v0; s.fx[6][r][j] = Rb.v1; s.fx[7][r][j] = Rb.p;
     } else {
+      // y face below cell (X0 + r, Y0 + j): box cells (r + 1, j + 1), (r + 1, j)
       const int i2 = i - NXF;
       j = i2 / TX;
       r = i2 - j * TX;
-      const size_t ic = G.at(X0 + r, Y0 + j), im = G.at(X0 + r, Y0 + j - 1);
-      const Prim<R> a = U1b.get(ic), c = U1b.get(im);
+      const Prim<R> a = cot(r + 1, j + 1), c = cot(r + 1, j);
       const Flux<R> fb{d1 * (a.rho - c.rho), d1 * (a.v0 - c.v0), d1 * (a.v1 - c.v1),
                        d1 * (a.p - c.p)};
-      ha::hllc_rev<1>(G.g, P.get(im), P.get(ic), fb, Lb, Rb);
+      ha::hllc_rev<1>(G.g, state(r + 1, j), state(r + 1, j + 1), fb, Lb, Rb);
       s.fy[0][j][r] = Lb.rho; s.fy[1][j][r] = Lb.v0; s.fy[2][j][r] = Lb.v1; s.fy[3][j][r] = Lb.p;
       s.fy[4][j][r] = Rb.rho; s.fy[5][j][r] = Rb.v0; s.fy[6][j][r] = Rb.v1; s.fy[7][j][r] = Rb.p;
     }
@@ -489,7 +526,7 @@ adj_stage1_tile(Fields<R> U1b, Fields<R> Pbase, Fields<R> Pb, Geo<R> G,
     const int x = X0 + tx, y = Y0 + ty;
     if (x >= G.n0 || y >= G.n1) continue;
     const size_t gi = (size_t)y * G.n0 + x;
-    const Prim<R> q = P.get(gi);
+    const Prim<R> q = state(tx + 1, ty + 1);
     if (hk::ts_bits<R>(hs::timescale(G.g, G.dR0, G.dR1, q.rho, q.v0, q.v1, q.p)) == mb &&
         gi < best)
       best = gi;
@@ -632,9 +669,13 @@ static std::mutex g_scratch_mu;
 
 template <class R> static cudaError_t allow_tile_smem() {
   constexpr int TX = adj::AdjTile<R>::TX, TY = adj::AdjTile<R>::TY;
-  return cudaFuncSetAttribute(adj::adj_stage2_tile<R, TX, TY>,
+  const cudaError_t e = cudaFuncSetAttribute(adj::adj_stage2_tile<R, TX, TY>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)sizeof(adj::Stage2Smem<R, TX, TY>));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(adj::adj_stage1_tile<R, TX, TY>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)sizeof(adj::Stage2Smem<R, TX, TY>));
+                              (int)sizeof(adj::Stage1Smem<R, TX, TY>));
 }
 
 static om_status get_scratch(Handle *h, int fp64, AdjointScratch **out) {
@@ -703,6 +744,32 @@ template <class R> static adj::Fields<R> F4(void *const *p) {
   return adj::Fields<R>{{(R *)p[0], (R *)p[1], (R *)p[2], (R *)p[3]}};
 }
 
+// Launch of a kernel that may start while the previous kernel on the stream
+// drains (programmatic stream serialization); the kernel waits for it with
+// wait_previous_kernel before its first dependent read.
+template <class... Params, class... Args>
+static cudaError_t launch_after(void (*kernel)(Params...), int grid, size_t smem, cudaStream_t st,
+                                Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
+// both parities' arg-min slots to "none" (the start of a run)
+static om_status reset_argmin(Handle *h, AdjointScratch *s) {
+  OM_CUDA_CHECK(
+      cudaMemsetAsync(s->argmin, 0xFF, 4 * sizeof(unsigned long long), h->stream));
+  return OM_OK;
+}
+
 // kernels of one adjoint step, launched directly (the two tile kernels; the
 // dt cotangent of a step is applied by the next step's first kernel, or by
 // adj_dt after the last step of a run)
@@ -728,12 +795,16 @@ static om_status vjp_kernels(Handle *h, AdjointScratch *s, const adj::StepIn *re
   // argmin[2 par]: arg-min cell, argmin[2 par + 1]: minimum timescale bits
   unsigned long long *am = s->argmin + 2 * par;
   double *part = s->partials + (size_t)par * nt;
-  const adj::PendingDt pend{s->partials + (size_t)(1 - par) * nt, nt, s->argmin + 2 * (1 - par)};
-  OM_CUDA_CHECK(cudaMemsetAsync(am, 0xFF, 2 * sizeof(unsigned long long), st));
-  adj::adj_stage2_tile<R, TX, TY><<<nt, 256, sizeof(adj::Stage2Smem<R, TX, TY>), st>>>(
-      U, U1b, Pbase, G, part, am + 1, pend);
-  adj::adj_stage1_tile<R, TX, TY><<<nt, 256, 0, st>>>(U1b, Pbase, Pb, G, am + 1, am);
-  OM_CUDA_CHECK(cudaGetLastError());
+  unsigned long long *other = s->argmin + 2 * (1 - par);
+  const adj::PendingDt pend{s->partials + (size_t)(1 - par) * nt, nt, other};
+  // this parity's slots were reset by the previous step's E+F kernel (or by
+  // reset_argmin at the start of the run)
+  OM_CUDA_CHECK(launch_after(adj::adj_stage2_tile<R, TX, TY>, nt,
+                             sizeof(adj::Stage2Smem<R, TX, TY>), st, U, U1b, Pbase, G, part,
+                             am + 1, pend));
+  OM_CUDA_CHECK(launch_after(adj::adj_stage1_tile<R, TX, TY>, nt,
+                             sizeof(adj::Stage1Smem<R, TX, TY>), st, U1b, Pbase, Pb, G, am + 1,
+                             am, other));
   h->launches += kVjpLaunches;
   return OM_OK;
 }
@@ -867,6 +938,7 @@ extern "C" om_status om_hydro_vjp(om_handle H, void *const *cot_next, void *cons
   const double cfl = ((HydroScalars *)h->h_scalars)->cfl;
   OM_CUDA_CHECK(cudaMemcpyAsync(s->d_in, s->h_in1, sizeof(adj::StepIn), cudaMemcpyHostToDevice,
                                 h->stream));
+  OM_TRY(reset_argmin(h, s));
   om_status st = fp64 ? vjp_kernels<double>(h, s, s->d_in, cot_next, cot_prev, 0)
                       : vjp_kernels<float>(h, s, s->d_in, cot_next, cot_prev, 0);
   OM_TRY(st);
@@ -966,6 +1038,7 @@ static om_status backward_core(om_hydro_tape t, AdjointScratch *s, void **result
     pb[k] = s->pb[k];
   }
   const double cfl = ((HydroScalars *)h->h_scalars)->cfl;
+  OM_TRY(reset_argmin(h, s));
   for (int j = t->nck - 1; j >= 0; --j) {
     const int len = std::min(t->seg, t->steps - j * t->seg);
     const bool taped = (int)t->tapes.size() >= len;
@@ -1151,6 +1224,7 @@ extern "C" om_status om_hydro_time_vjp(om_handle H, int reps, float *ms) {
     ub[k] = s->ub[k];
     pb[k] = s->pb[k];
   }
+  OM_TRY(reset_argmin(h, s));
   for (int r = 0; r < 2; ++r) {
     OM_TRY(run_vjp(h, s, s->d_in, ub, pb));
     for (int k = 0; k < 4; ++k) std::swap(ub[k], pb[k]);
