@@ -291,7 +291,9 @@ def lifegraph_workload(args, dist: Dist) -> dict:
     ms = dist.max(ms)
     value = cells * gens * args.steps * dist.world / (ms * 1e-3) / 1e9
     peak, _ = peaks()
-    achieved = 8.0 * cells / (ms / (gens * args.steps) * 1e-3) / 1e9
+    per_launch_ms = ms / (gens * args.steps)
+    achieved = 8.0 * cells / (per_launch_ms * 1e-3) / 1e9
+    traffic = profile_traffic("om_graph_life_stage", n)
     m.close()
     return {
         "metric": "Life cell-updates/s (Gcell-updates/s) through the general OM graph executor",
@@ -304,7 +306,8 @@ def lifegraph_workload(args, dist: Dist) -> dict:
                    "n0": n, "n1": n, "parallelism": f"replicas x{dist.world}"},
         "roofline": {"bound": "hbm", "kernel": "om_k1_s0 (generated)", "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 3),
-                     "traffic": None, "algorithmic_bytes_per_launch": 8.0 * cells},
+                     "traffic": traffic["bytes_per_launch"] if traffic else None,
+                     "algorithmic_bytes_per_launch": 8.0 * cells},
         "gpu_launches": launches, "clocks": clk,
     }
 

@@ -394,12 +394,11 @@ class Emitter {
     }
     if (m) {
       // a manifest computed by an earlier stage of this kernel run
-      expr = "((const " + T + " *)P.tmp[" + std::to_string(m->tmp) + "])[" + addr(o0, o1) + "]";
+      expr = element("P.tmp[" + std::to_string(m->tmp) + "]", n.type, o0, o1);
     } else if (n.op == "load") {
       const int s = g_.find_static(n.sarg);
       if (g_.statics[s].array)
-        expr = "((const " + T + " *)P.cur[" + std::to_string(array_index(s)) + "])[" +
-               addr(o0, o1) + "]";
+        expr = element("P.cur[" + std::to_string(array_index(s)) + "]", n.type, o0, o1);
       else
         expr = scalar_read(g_.statics[s]);
     } else if (n.op == "imm") {
@@ -436,8 +435,62 @@ class Emitter {
     return k;
   }
 
+  // A thread evaluates cells c0 .. c0 + V - 1 of a row; V = 4 makes its
+  // loads of 4- and 8-byte arrays row vectors (below).
+  void cells_per_thread(int V) { V_ = V; }
+
+  // whether the V cells of a row of this type move as one vector
+  static bool vector_type(Type t) { return t == TInt || t == TFloat || t == TDouble; }
+
  private:
   static std::string off_name(int o) { return o < 0 ? "m" + std::to_string(-o) : std::to_string(o); }
+
+  // The element at column c0 + o0 of row c1 + o1 of a global array.  With
+  // four cells per thread, the thread's own four columns of a row come in
+  // one aligned vector load (rows are whole multiples of 1024 cells, so
+  // c0 + 4k is 16-byte aligned for 4-byte types), and the columns of the
+  // four before or after come from the neighbouring lane, which loaded
+  // them as its own.  Lanes 0 and 31 have no such neighbour in the warp
+  // and load that column themselves.  Every lane runs the shuffles (the
+  // stage body is straight-line code), and the addresses read are the
+  // ones the per-cell loads would read.
+  std::string element(const std::string &base, Type t, int o0, int o1) {
+    const std::string T = ctype(t);
+    const std::string scalar = "((const " + T + " *)" + base + ")[" + addr(o0, o1) + "]";
+    if (V_ != 4 || !vector_type(t)) return scalar;
+    const int k = o0 >= 0 ? o0 / 4 : -((3 - o0) / 4);  // floor(o0 / 4)
+    const int j = o0 - 4 * k;
+    if (k < -1 || k > 1) return scalar;
+    const std::string own = row_vector(base, t, o1)[j];
+    if (k == 0) return own;
+    const std::string name = "n" + std::to_string(nshfl_++);
+    code += "      const " + T + " " + name + " = " +
+            (k < 0 ? "__shfl_up_sync" : "__shfl_down_sync") + "(0xffffffffu, " + own + ", 1);\n";
+    return "((threadIdx.x & 31) == " + std::string(k < 0 ? "0" : "31") + " ? " + scalar + " : " +
+           name + ")";
+  }
+
+  // the four components of the thread's own vector of row c1 + o1
+  std::vector<std::string> row_vector(const std::string &base, Type t, int o1) {
+    const auto key = std::make_pair(base, o1);
+    auto it = vecs_.find(key);
+    if (it != vecs_.end()) return it->second;
+    const std::string T = ctype(t), y = row(o1);
+    const std::string name = "a" + std::to_string(vecs_.size());
+    std::vector<std::string> c;
+    if (t == TDouble) {
+      for (int h = 0; h < 2; ++h)
+        code += "      const om_v2d " + name + (h ? "h" : "l") + " = *(const om_v2d *)((const double *)" +
+                base + " + " + y + " + c0" + (h ? " + 2" : "") + ");\n";
+      c = {name + "l.x", name + "l.y", name + "h.x", name + "h.y"};
+    } else {
+      const std::string VT = t == TInt ? "om_v4i" : "om_v4f";
+      code += "      const " + VT + " " + name + " = *(const " + VT + " *)((const " + T + " *)" + base +
+              " + " + y + " + c0);\n";
+      c = {name + ".x", name + ".y", name + ".z", name + ".w"};
+    }
+    return vecs_[key] = c;
+  }
 
   std::string wrap(const std::string &c, int o, int n) const {
     if (o == 0) return c;
@@ -524,6 +577,8 @@ class Emitter {
   int stage_;
   std::map<std::tuple<int, int, int>, std::string> memo_;
   std::map<int, std::string> cols_, rows_;
+  std::map<std::pair<std::string, int>, std::vector<std::string>> vecs_;
+  int V_ = 1, nshfl_ = 0;
 };
 
 static std::string region_test(const Region &r, const Layout &L) {
@@ -567,7 +622,10 @@ static const char *kPrelude =
     "struct OMPtrs { const void *cur[32]; void *nxt[32]; void *tmp[64]; };\n"
     "__device__ __forceinline__ float om_inf_f() { return __int_as_float(0x7f800000); }\n"
     "__device__ __forceinline__ double om_inf_d() {\n"
-    "  return __longlong_as_double(0x7ff0000000000000LL); }\n";
+    "  return __longlong_as_double(0x7ff0000000000000LL); }\n"
+    "struct alignas(16) om_v4i { int x, y, z, w; };\n"
+    "struct alignas(16) om_v4f { float x, y, z, w; };\n"
+    "struct alignas(16) om_v2d { double x, y; };\n";
 
 static std::string ident(Type t, const std::string &op) {
   if (op == "sum") return std::string("(") + ctype(t) + ")0";
@@ -716,28 +774,49 @@ static std::string generate(const Graph &g, const Layout &L, std::vector<KernelP
           << "    (void)c0; (void)c1;\n";
       if (shared) {
         Emitter e(g, k, L, slots, &man, st);
-        std::vector<std::string> vals;
+        e.cells_per_thread(V);
+        // vals[c][...]: cell c's stores, reduce inputs and manifests
+        std::vector<std::vector<std::string>> vals(V);
         for (int c = 0; c < V; ++c) {
-          for (int s : sp.stores) vals.push_back(e.value(k.stores[s].node, c, 0));
-          for (int id : sp.reduces) vals.push_back(e.value(k.node(id).args[0], c, 0));
-          for (int id : sp.manifests) vals.push_back(e.value(id, c, 0));
+          for (int s : sp.stores) vals[c].push_back(e.value(k.stores[s].node, c, 0));
+          for (int id : sp.reduces) vals[c].push_back(e.value(k.node(id).args[0], c, 0));
+          for (int id : sp.manifests) vals[c].push_back(e.value(id, c, 0));
         }
         src << "    {\n" << e.code;
-        size_t v = 0;
-        for (int c = 0; c < V; ++c) {
-          const std::string at = c == 0 ? "i" : "i + " + std::to_string(c);
-          for (int s : sp.stores)
-            src << "      ((" << ctype(k.node(k.stores[s].node).type) << " *)P.nxt["
-                << em.array_index(k.stores[s].stat) << "])[" << at << "] = " << vals[v++] << ";\n";
+        // the V cells' values of one array go out as one store (a vector
+        // of 4 for 4- and 8-byte types, at 16-byte aligned i)
+        auto store = [&](Type t, const std::string &ptr, size_t slot) {
+          const std::string T = ctype(t);
+          if (V == 4 && Emitter::vector_type(t)) {
+            const std::string p = "((" + T + " *)" + ptr + " + i";
+            if (t == TDouble)
+              src << "      *(om_v2d *)" << p << ") = om_v2d{" << vals[0][slot] << ", "
+                  << vals[1][slot] << "};\n      *(om_v2d *)" << p << " + 2) = om_v2d{"
+                  << vals[2][slot] << ", " << vals[3][slot] << "};\n";
+            else
+              src << "      *(" << (t == TInt ? "om_v4i" : "om_v4f") << " *)" << p << ") = "
+                  << (t == TInt ? "om_v4i{" : "om_v4f{") << vals[0][slot] << ", " << vals[1][slot]
+                  << ", " << vals[2][slot] << ", " << vals[3][slot] << "};\n";
+            return;
+          }
+          for (int c = 0; c < V; ++c)
+            src << "      ((" << T << " *)" << ptr << ")[" << (c == 0 ? "i" : "i + " + std::to_string(c))
+                << "] = " << vals[c][slot] << ";\n";
+        };
+        size_t slot0 = 0;
+        for (int s : sp.stores)
+          store(k.node(k.stores[s].node).type, "P.nxt[" + std::to_string(em.array_index(k.stores[s].stat)) + "]",
+                slot0++);
+        // reduces fold the cells in order c = 0 .. V - 1
+        for (int c = 0; c < V; ++c)
           for (size_t r = 0; r < sp.reduces.size(); ++r) {
             const std::string acc = "acc" + std::to_string(r);
-            src << "      " << acc << " = " << combine(k.node(sp.reduces[r]).sarg, acc, vals[v++])
-                << ";\n";
+            src << "      " << acc << " = "
+                << combine(k.node(sp.reduces[r]).sarg, acc, vals[c][sp.stores.size() + r]) << ";\n";
           }
-          for (int id : sp.manifests)
-            src << "      ((" << ctype(k.node(id).type) << " *)P.tmp[" << man.at(id).tmp << "])["
-                << at << "] = " << vals[v++] << ";\n";
-        }
+        slot0 += sp.reduces.size();
+        for (int id : sp.manifests)
+          store(k.node(id).type, "P.tmp[" + std::to_string(man.at(id).tmp) + "]", slot0++);
         src << "    }\n";
       } else {
         // a manifest is written on its region (other cells are never read)

@@ -142,6 +142,22 @@ def test_examples_compile_for_sm103a(om_lib, make):
     assert "__global__" in src
 
 
+def test_row_vectors_on_rows_of_whole_chunks(om_lib):
+    # rows of 16384 cells: the Life stage loads each row once as a vector of
+    # four cells, takes the columns beside them from the neighbouring lanes
+    # (lanes 0 and 31 load those themselves) and stores four cells at once
+    status, err, src = _check(om_lib, ex.life((16384, 64)).to_text())
+    assert status == 0, err
+    stage = src[src.index("om_k1_s0"):src.index("om_k1_commit")]
+    assert stage.count("*(const om_v4i *)") == 3
+    assert stage.count("__shfl_up_sync") == 3 and stage.count("__shfl_down_sync") == 3
+    assert stage.count("*(om_v4i *)") == 1
+    # rows that are not whole chunks keep one cell per thread
+    status, err, src = _check(om_lib, ex.life((2000, 64)).to_text())
+    assert status == 0, err
+    assert "om_v4i *)" not in src and "__shfl" not in src
+
+
 def test_graph_errors_are_reported(om_lib):
     bad = [
         "om T 3 4 4 4 cyclic\n",                                   # 3-D

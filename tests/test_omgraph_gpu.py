@@ -245,6 +245,55 @@ def test_semantics_graph_long_rows(om_lib, boundary):
     g.close()
 
 
+def stencil_graph(size):
+    """Shifts from -9 to +9 columns and -1 to +1 rows of float, double, int
+    and bool arrays and of a manifest: columns inside the thread's four,
+    in the neighbouring lane's four and beyond."""
+    om = og.OM("Wide", size, "cyclic")
+    f = om.static_array("f", og.Float)
+    d = om.static_array("d", og.Double)
+    i = om.static_array("i", og.Int)
+    b = om.static_array("b", og.Bool)
+    s = om.static_scalar("s", og.Double)
+    k = om.kernel("step")
+    fv, dv, iv, bv = k.load(f), k.load(d), k.load(i), k.load(b)
+    shifts = [(-9, 0), (-5, 1), (-4, -1), (-3, 0), (-1, 1), (1, -1), (3, 0), (4, 1), (5, -1),
+              (7, 0), (8, 1), (9, -1)]
+    ff, dd, ii = fv, dv, iv
+    for n, v in enumerate(shifts):
+        ff = ff * 0.75 + k.shift(fv, v) * (0.125 * (n + 1))
+        dd = dd - k.shift(dv, v) * (0.0625 * (n + 1))
+        ii = ii + k.shift(iv, v) * (n + 1)
+    m = dd * 0.5 + og.cast(ff, og.Double)
+    k.manifest(m)
+    k.store(f, ff)
+    k.store(i, ii % 1000003)
+    k.store(b, k.shift(bv, (-1, 0)) | (k.shift(bv, (5, 1)) & (fv > 0)))
+    k.store(d, k.shift(m, (-3, 0)) + k.shift(m, (6, -1)) - k.shift(m, (1, 1)) * 0.25)
+    k.store(s, k.reduce("sum", dd))
+    return om
+
+
+@pytest.mark.parametrize("size", [(2048, 7), (1024, 3)])
+def test_row_vectors_and_lane_shuffles(om_lib, size):
+    # rows of whole 1024-cell chunks: four cells per thread, row vectors,
+    # neighbouring columns from the lanes beside; equal to the oracle
+    om = stencil_graph(size)
+    m0 = R.Machine(om.to_text())
+    rng = np.random.default_rng(21)
+    shape = m0.shape
+    init = {"f": rng.standard_normal(shape).astype(np.float32),
+            "d": rng.standard_normal(shape),
+            "i": rng.integers(-1000, 1000, shape).astype(np.int32),
+            "b": rng.random(shape) < 0.5}
+    g, m = both(om_lib, om, ["step", "step"], init=init)
+    assert "*(const om_v2d *)" in g.source and "*(const om_v4f *)" in g.source
+    assert "__shfl_down_sync" in g.source
+    assert_same(g, m, ["f", "d", "i", "b"])
+    assert_same(g, m, ["s"], rtol=1e-12)          # block-order sum
+    g.close()
+
+
 def manifest_graph(boundary, mark):
     """Values marked Manifest (computed once into an array) and read at
     shifts, by a second manifest, a reduce and stores; unmarked, the same
