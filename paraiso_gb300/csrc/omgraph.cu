@@ -12,7 +12,9 @@
 //     the partials in a fixed order;
 //   * one "commit" thread that evaluates the scalar stores.
 // Values other than stores and reduces are recomputed where they are used
-// (the generator's Delayed allocation), once per (node, offset) per cell.
+// (the generator's Delayed allocation), once per (node, offset) per cell,
+// except that a stage which reads a computed value at three or more offsets
+// computes it once per cell of a shared-memory tile (plan_tiles).
 // Semantics followed: valid regions (Optimization/BoundaryAnalysis.hs:33-94),
 // margins (OMTrans.hs:103-120), shift reads x[c - v] (PlanTrans.hs:561-562),
 // loadIndex / loadSize (PlanTrans.hs:455-466), Arith -> C (PlanTrans.hs:
@@ -370,6 +372,21 @@ struct ManifestAt {
   int tmp;
 };
 
+// A value computed once per cell of a stage's shared-memory tile (with its
+// halo) and read there at every offset the stage needs it: node id -> the
+// tile array.
+struct TileAt {
+  std::string name;
+};
+
+// The tile of a tiled stage: TX x TY cells per block, a halo of hx0/hy0
+// cells below and hx1/hy1 above each axis; RX x RY cells in all.
+struct TileShape {
+  int tx = 32, ty = 8, hx0 = 0, hx1 = 0, hy0 = 0, hy1 = 0;
+  int rx() const { return tx + hx0 + hx1; }
+  int ry() const { return ty + hy0 + hy1; }
+};
+
 class Emitter {
  public:
   Emitter(const Graph &g, const KernelDef &k, const Layout &L,
@@ -387,6 +404,14 @@ class Emitter {
     if (it != memo_.end()) return it->second;
     std::string expr;
     const std::string T = ctype(n.type);
+    if (tiles_ && tiles_->count(id)) {
+      // computed by the tile phase of this stage, for every cell of the tile
+      const std::string v = "t" + std::to_string(id) + "_" + off_name(o0) + "_" + off_name(o1);
+      code += "      const " + T + " " + v + " = " + tiles_->at(id).name + "[(ty + " +
+              std::to_string(o1 + shape_.hy0) + ") * " + std::to_string(shape_.rx()) + " + tx + " +
+              std::to_string(o0 + shape_.hx0) + "];\n";
+      return memo_[key] = v;
+    }
     const ManifestAt *m = nullptr;
     if (man_) {
       auto mi = man_->find(id);
@@ -433,6 +458,20 @@ class Emitter {
     int k = 0;
     for (int i = 0; i < s; ++i) k += g_.statics[i].array ? 1 : 0;
     return k;
+  }
+
+  // values that a tile phase computes, read from its tile (phase two of a
+  // tiled stage)
+  void tiled(const std::map<int, TileAt> *t, const TileShape &shape) {
+    tiles_ = t;
+    shape_ = shape;
+  }
+
+  // the offsets at which each node has been evaluated so far
+  std::map<int, std::set<std::pair<int, int>>> offsets() const {
+    std::map<int, std::set<std::pair<int, int>>> r;
+    for (const auto &m : memo_) r[std::get<0>(m.first)].insert({std::get<1>(m.first), std::get<2>(m.first)});
+    return r;
   }
 
   // A thread evaluates cells c0 .. c0 + V - 1 of a row; V = 4 makes its
@@ -579,6 +618,8 @@ class Emitter {
   std::map<int, std::string> cols_, rows_;
   std::map<std::pair<std::string, int>, std::vector<std::string>> vecs_;
   int V_ = 1, nshfl_ = 0;
+  const std::map<int, TileAt> *tiles_ = nullptr;
+  TileShape shape_;
 };
 
 static std::string region_test(const Region &r, const Layout &L) {
@@ -643,6 +684,164 @@ static std::string combine(const std::string &op, const std::string &acc, const 
 }
 
 // Builds the plan and the CUDA source of every kernel of the graph.
+// The outputs a stage evaluates at offset 0 of each cell: its array stores,
+// its reduce inputs and the manifests it computes.
+static std::vector<int> stage_roots(const KernelDef &k, const StagePlan &sp) {
+  std::vector<int> r;
+  for (int s : sp.stores) r.push_back(k.stores[s].node);
+  for (int id : sp.reduces) r.push_back(k.node(id).args[0]);
+  for (int id : sp.manifests) r.push_back(id);
+  return r;
+}
+
+// Tiled stages.  Where a stage evaluates a computed value at three or more
+// offsets of each cell (Hydro's stage-1 state, which each stage-2 wall
+// reads at four cells along its axis), recomputing it per offset costs more
+// than computing it once per cell of a shared-memory tile.  A tiled stage
+// runs in two phases per 32 x 8 tile of cells:
+//   1. every value of the frontier (below) for each cell of the tile and its
+//      halo, into shared memory;
+//   2. the stage's outputs for the tile's cells, reading frontier values
+//      from shared memory at their offsets.
+// The frontier is the set of values evaluated at three or more offsets that
+// an output is, or that a value evaluated at fewer offsets uses; values
+// below it are computed in phase 1 only.  The arithmetic of each value is
+// unchanged, so results are the same bit for bit (the per-thread order of a
+// reduce's terms changes, as with any change of work split).  Cyclic 2-D
+// meshes only, whose wrapped neighbours are translation invariant: the value
+// at offset o of cell c is the value at offset 0 of cell c + o.
+constexpr int kTileSmemBytes = 40 * 1024;
+
+static bool plan_tiles(const Graph &g, const KernelDef &k, const Layout &L,
+                       const std::map<int, int> &slots, const std::map<int, ManifestAt> &man,
+                       int st, const StagePlan &sp, std::map<int, TileAt> *tiles,
+                       TileShape *shape) {
+  const std::vector<int> roots = stage_roots(k, sp);
+  Emitter trial(g, k, L, slots, &man, st);
+  for (int r : roots) trial.value(r, 0, 0);
+  const auto offs = trial.offsets();
+  auto computed = [&](int id) {
+    const Node &n = k.node(id);
+    if (!n.array) return false;
+    static const std::set<std::string> leaf = {"load",     "imm",    "shift",    "loadindex",
+                                               "loadsize", "reduce", "broadcast"};
+    if (leaf.count(n.op)) return false;
+    auto mi = man.find(id);
+    return !(mi != man.end() && mi->second.stage < st);  // else read from its array
+  };
+  std::set<int> many;
+  for (const auto &o : offs)
+    if (o.second.size() >= 3 && computed(o.first)) many.insert(o.first);
+  if (many.empty()) return false;
+  std::set<int> front;
+  for (int r : roots)
+    if (many.count(r)) front.insert(r);
+  for (const auto &o : offs) {
+    if (many.count(o.first)) continue;
+    for (int a : k.node(o.first).args)
+      if (many.count(a)) front.insert(a);
+  }
+  // keep what phase 2 reads; the halo covers the offsets it reads them at
+  for (int round = 0; round < 2; ++round) {
+    tiles->clear();
+    for (int id : front) (*tiles)[id] = TileAt{"tile" + std::to_string(id)};
+    Emitter second(g, k, L, slots, &man, st);
+    second.tiled(tiles, TileShape());
+    for (int r : roots) second.value(r, 0, 0);
+    const auto used = second.offsets();
+    std::set<int> kept;
+    TileShape sh;
+    for (int id : front) {
+      auto u = used.find(id);
+      if (u == used.end()) continue;
+      kept.insert(id);
+      for (const auto &o : u->second) {
+        sh.hx0 = std::max(sh.hx0, -o.first);
+        sh.hx1 = std::max(sh.hx1, o.first);
+        sh.hy0 = std::max(sh.hy0, -o.second);
+        sh.hy1 = std::max(sh.hy1, o.second);
+      }
+    }
+    *shape = sh;
+    if (kept == front) break;
+    front = kept;
+  }
+  if (front.empty()) return false;
+  tiles->clear();
+  size_t bytes = 0;
+  double reads = 0;
+  for (int id : front) {
+    (*tiles)[id] = TileAt{"tile" + std::to_string(id)};
+    bytes += (size_t)shape->rx() * shape->ry() * tsize(k.node(id).type);
+    reads += offs.at(id).size();
+  }
+  const double cells = (double)shape->rx() * shape->ry() / (shape->tx * shape->ty);
+  if (bytes > (size_t)kTileSmemBytes || shape->hx0 > 8 || shape->hx1 > 8 || shape->hy0 > 8 ||
+      shape->hy1 > 8)
+    return false;
+  // worth it when the frontier values were evaluated at clearly more
+  // offsets per cell than the tile computes them
+  return reads / front.size() >= 1.5 * cells;
+}
+
+static void emit_tiled(std::ostringstream &src, const Graph &g, const KernelDef &k,
+                       const Layout &L, const std::map<int, int> &slots,
+                       const std::map<int, ManifestAt> &man, int st, const StagePlan &sp,
+                       const std::map<int, TileAt> &tiles, const TileShape &sh,
+                       Emitter &names) {
+  const int RX = sh.rx(), RY = sh.ry();
+  const std::string n0 = std::to_string(L.ms[0]), n1 = std::to_string(L.ms[1]);
+  for (const auto &t : tiles)
+    src << "  __shared__ " << ctype(k.node(t.first).type) << " " << t.second.name << "["
+        << RX * RY << "];\n";
+  src << "  constexpr int NTX = " << (L.ms[0] + sh.tx - 1) / sh.tx
+      << ", NTY = " << (L.ms[1] + sh.ty - 1) / sh.ty << ";\n"
+      << "  for (long long w = blockIdx.x; w < (long long)NTX * NTY; w += gridDim.x) {\n"
+      << "    const int X0 = (int)(w % NTX) * " << sh.tx << ", Y0 = (int)(w / NTX) * " << sh.ty
+      << ";\n"
+      << "    __syncthreads();  // the previous tile's phase 2 is done with the tiles\n"
+      << "    for (int e = threadIdx.x; e < " << RX * RY << "; e += 256) {\n"
+      << "      const int ry = e / " << RX << ", rx = e - ry * " << RX << ";\n"
+      << "      const int c0 = ((X0 + rx - " << sh.hx0 << ") % " << n0 << " + " << n0 << ") % "
+      << n0 << ";\n"
+      << "      const int c1 = ((Y0 + ry - " << sh.hy0 << ") % " << n1 << " + " << n1 << ") % "
+      << n1 << ";\n"
+      << "      const long long i = (long long)c1 * " << n0 << " + c0;\n"
+      << "      (void)i;\n";
+  {
+    Emitter first(g, k, L, slots, &man, st);
+    std::vector<std::string> vals;
+    for (const auto &t : tiles) vals.push_back(first.value(t.first, 0, 0));
+    src << "    {\n" << first.code;
+    size_t v = 0;
+    for (const auto &t : tiles) src << "      " << t.second.name << "[e] = " << vals[v++] << ";\n";
+    src << "    }\n";
+  }
+  src << "    }\n    __syncthreads();\n"
+      << "    for (int e = threadIdx.x; e < " << sh.tx * sh.ty << "; e += 256) {\n"
+      << "      const int ty = e / " << sh.tx << ", tx = e - ty * " << sh.tx << ";\n"
+      << "      const int c0 = X0 + tx, c1 = Y0 + ty;\n"
+      << "      if (c0 >= " << n0 << " || c1 >= " << n1 << ") continue;\n"
+      << "      const long long i = (long long)c1 * " << n0 << " + c0;\n";
+  Emitter second(g, k, L, slots, &man, st);
+  second.tiled(&tiles, sh);
+  std::vector<std::string> vals;
+  for (int r : stage_roots(k, sp)) vals.push_back(second.value(r, 0, 0));
+  src << "    {\n" << second.code;
+  size_t v = 0;
+  for (int s : sp.stores)
+    src << "      ((" << ctype(k.node(k.stores[s].node).type) << " *)P.nxt["
+        << names.array_index(k.stores[s].stat) << "])[i] = " << vals[v++] << ";\n";
+  for (size_t r = 0; r < sp.reduces.size(); ++r) {
+    const std::string acc = "acc" + std::to_string(r);
+    src << "      " << acc << " = " << combine(k.node(sp.reduces[r]).sarg, acc, vals[v++]) << ";\n";
+  }
+  for (int id : sp.manifests)
+    src << "      ((" << ctype(k.node(id).type) << " *)P.tmp[" << man.at(id).tmp << "])[i] = "
+        << vals[v++] << ";\n";
+  src << "    }\n    }\n  }\n";
+}
+
 static std::string generate(const Graph &g, const Layout &L, std::vector<KernelPlan> *plans,
                             std::map<std::pair<int, int>, int> *slot_map, int *nslots,
                             int *ntmp) {
@@ -759,102 +958,110 @@ static std::string generate(const Graph &g, const Layout &L, std::vector<KernelP
         if (std::count(trial.code.begin(), trial.code.end(), '\n') <= kMaxVectorStatements)
           V = kCellsPerThread;
       }
-      // work items: chunks of 256 V cells of a memory row, rows in order; a
-      // block takes items blockIdx.x, blockIdx.x + gridDim.x, ...
-      const int chunk = 256 * V;
-      src << "  constexpr int CX = " << (L.ms[0] + chunk - 1) / chunk << ";\n"
-          << "  const long long NW = (long long)" << L.ms[1] << " * CX;\n"
-          << "  for (long long w = blockIdx.x; w < NW; w += gridDim.x) {\n"
-          << "    const int c1 = (int)(w / CX);\n"
-          << "    const int c0 = (int)(w - (long long)c1 * CX) * " << chunk << " + (int)threadIdx.x";
-      if (V > 1) src << " * " << V;
-      src << ";\n";
-      if (V == 1) src << "    if (c0 >= " << L.ms[0] << ") continue;\n";
-      src << "    const long long i = (long long)c1 * " << L.ms[0] << " + c0;\n"
-          << "    (void)c0; (void)c1;\n";
-      if (shared) {
-        Emitter e(g, k, L, slots, &man, st);
-        e.cells_per_thread(V);
-        // vals[c][...]: cell c's stores, reduce inputs and manifests
-        std::vector<std::vector<std::string>> vals(V);
-        for (int c = 0; c < V; ++c) {
-          for (int s : sp.stores) vals[c].push_back(e.value(k.stores[s].node, c, 0));
-          for (int id : sp.reduces) vals[c].push_back(e.value(k.node(id).args[0], c, 0));
-          for (int id : sp.manifests) vals[c].push_back(e.value(id, c, 0));
-        }
-        src << "    {\n" << e.code;
-        // the V cells' values of one array go out as one store (a vector
-        // of 4 for 4- and 8-byte types, at 16-byte aligned i)
-        auto store = [&](Type t, const std::string &ptr, size_t slot) {
-          const std::string T = ctype(t);
-          if (V == 4 && Emitter::vector_type(t)) {
-            const std::string p = "((" + T + " *)" + ptr + " + i";
-            if (t == TDouble)
-              src << "      *(om_v2d *)" << p << ") = om_v2d{" << vals[0][slot] << ", "
-                  << vals[1][slot] << "};\n      *(om_v2d *)" << p << " + 2) = om_v2d{"
-                  << vals[2][slot] << ", " << vals[3][slot] << "};\n";
-            else
-              src << "      *(" << (t == TInt ? "om_v4i" : "om_v4f") << " *)" << p << ") = "
-                  << (t == TInt ? "om_v4i{" : "om_v4f{") << vals[0][slot] << ", " << vals[1][slot]
-                  << ", " << vals[2][slot] << ", " << vals[3][slot] << "};\n";
-            return;
-          }
-          for (int c = 0; c < V; ++c)
-            src << "      ((" << T << " *)" << ptr << ")[" << (c == 0 ? "i" : "i + " + std::to_string(c))
-                << "] = " << vals[c][slot] << ";\n";
-        };
-        size_t slot0 = 0;
-        for (int s : sp.stores)
-          store(k.node(k.stores[s].node).type, "P.nxt[" + std::to_string(em.array_index(k.stores[s].stat)) + "]",
-                slot0++);
-        // reduces fold the cells in order c = 0 .. V - 1
-        for (int c = 0; c < V; ++c)
-          for (size_t r = 0; r < sp.reduces.size(); ++r) {
-            const std::string acc = "acc" + std::to_string(r);
-            src << "      " << acc << " = "
-                << combine(k.node(sp.reduces[r]).sarg, acc, vals[c][sp.stores.size() + r]) << ";\n";
-          }
-        slot0 += sp.reduces.size();
-        for (int id : sp.manifests)
-          store(k.node(id).type, "P.tmp[" + std::to_string(man.at(id).tmp) + "]", slot0++);
-        src << "    }\n";
+      std::map<int, TileAt> tiles;
+      TileShape shape;
+      const bool tiled = V == 1 && shared && !L.open && g.ndim == 2 &&
+                         plan_tiles(g, k, L, slots, man, st, sp, &tiles, &shape);
+      if (tiled) {
+        emit_tiled(src, g, k, L, slots, man, st, sp, tiles, shape, em);
       } else {
-        // a manifest is written on its region (other cells are never read)
-        for (int id : sp.manifests) {
-          const std::string T = ctype(k.node(id).type);
+        // work items: chunks of 256 V cells of a memory row, rows in order; a
+        // block takes items blockIdx.x, blockIdx.x + gridDim.x, ...
+        const int chunk = 256 * V;
+        src << "  constexpr int CX = " << (L.ms[0] + chunk - 1) / chunk << ";\n"
+            << "  const long long NW = (long long)" << L.ms[1] << " * CX;\n"
+            << "  for (long long w = blockIdx.x; w < NW; w += gridDim.x) {\n"
+            << "    const int c1 = (int)(w / CX);\n"
+            << "    const int c0 = (int)(w - (long long)c1 * CX) * " << chunk << " + (int)threadIdx.x";
+        if (V > 1) src << " * " << V;
+        src << ";\n";
+        if (V == 1) src << "    if (c0 >= " << L.ms[0] << ") continue;\n";
+        src << "    const long long i = (long long)c1 * " << L.ms[0] << " + c0;\n"
+            << "    (void)c0; (void)c1;\n";
+        if (shared) {
           Emitter e(g, k, L, slots, &man, st);
-          const std::string val = e.value(id, 0, 0);
-          src << "    {\n      if (" << region_test(reg[k.at.at(id)], L) << ") {\n" << e.code
-              << "      ((" << T << " *)P.tmp[" << man.at(id).tmp << "])[i] = " << val << ";\n"
-              << "      }\n    }\n";
+          e.cells_per_thread(V);
+          // vals[c][...]: cell c's stores, reduce inputs and manifests
+          std::vector<std::vector<std::string>> vals(V);
+          for (int c = 0; c < V; ++c) {
+            for (int s : sp.stores) vals[c].push_back(e.value(k.stores[s].node, c, 0));
+            for (int id : sp.reduces) vals[c].push_back(e.value(k.node(id).args[0], c, 0));
+            for (int id : sp.manifests) vals[c].push_back(e.value(id, c, 0));
+          }
+          src << "    {\n" << e.code;
+          // the V cells' values of one array go out as one store (a vector
+          // of 4 for 4- and 8-byte types, at 16-byte aligned i)
+          auto store = [&](Type t, const std::string &ptr, size_t slot) {
+            const std::string T = ctype(t);
+            if (V == 4 && Emitter::vector_type(t)) {
+              const std::string p = "((" + T + " *)" + ptr + " + i";
+              if (t == TDouble)
+                src << "      *(om_v2d *)" << p << ") = om_v2d{" << vals[0][slot] << ", "
+                    << vals[1][slot] << "};\n      *(om_v2d *)" << p << " + 2) = om_v2d{"
+                    << vals[2][slot] << ", " << vals[3][slot] << "};\n";
+              else
+                src << "      *(" << (t == TInt ? "om_v4i" : "om_v4f") << " *)" << p << ") = "
+                    << (t == TInt ? "om_v4i{" : "om_v4f{") << vals[0][slot] << ", " << vals[1][slot]
+                    << ", " << vals[2][slot] << ", " << vals[3][slot] << "};\n";
+              return;
+            }
+            for (int c = 0; c < V; ++c)
+              src << "      ((" << T << " *)" << ptr << ")[" << (c == 0 ? "i" : "i + " + std::to_string(c))
+                  << "] = " << vals[c][slot] << ";\n";
+          };
+          size_t slot0 = 0;
+          for (int s : sp.stores)
+            store(k.node(k.stores[s].node).type, "P.nxt[" + std::to_string(em.array_index(k.stores[s].stat)) + "]",
+                  slot0++);
+          // reduces fold the cells in order c = 0 .. V - 1
+          for (int c = 0; c < V; ++c)
+            for (size_t r = 0; r < sp.reduces.size(); ++r) {
+              const std::string acc = "acc" + std::to_string(r);
+              src << "      " << acc << " = "
+                  << combine(k.node(sp.reduces[r]).sarg, acc, vals[c][sp.stores.size() + r]) << ";\n";
+            }
+          slot0 += sp.reduces.size();
+          for (int id : sp.manifests)
+            store(k.node(id).type, "P.tmp[" + std::to_string(man.at(id).tmp) + "]", slot0++);
+          src << "    }\n";
+        } else {
+          // a manifest is written on its region (other cells are never read)
+          for (int id : sp.manifests) {
+            const std::string T = ctype(k.node(id).type);
+            Emitter e(g, k, L, slots, &man, st);
+            const std::string val = e.value(id, 0, 0);
+            src << "    {\n      if (" << region_test(reg[k.at.at(id)], L) << ") {\n" << e.code
+                << "      ((" << T << " *)P.tmp[" << man.at(id).tmp << "])[i] = " << val << ";\n"
+                << "      }\n    }\n";
+          }
+          for (int s : sp.stores) {
+            const Store &so = k.stores[s];
+            const Node &v = k.node(so.node);
+            const std::string T = ctype(v.type);
+            Emitter e(g, k, L, slots, &man, st);
+            const std::string val = e.value(so.node, 0, 0);
+            src << "    {\n      " << T << " out = (" << T << ")0;\n"
+                << "      if (" << region_test(reg[k.at.at(so.node)], L) << ") {\n"
+                << e.code << "      out = " << val << ";\n      }\n"
+                << "      ((" << T << " *)P.nxt[" << em.array_index(so.stat) << "])[i] = out;\n"
+                << "    }\n";
+          }
+          for (size_t r = 0; r < sp.reduces.size(); ++r) {
+            const Node &n = k.node(sp.reduces[r]);
+            const int in = n.args[0];
+            Emitter e(g, k, L, slots, &man, st);
+            const std::string val = e.value(in, 0, 0);
+            const std::string acc = "acc" + std::to_string(r);
+            src << "    {\n      if (" << region_test(reg[k.at.at(in)], L) << ") {\n" << e.code
+                << "      " << acc << " = " << combine(n.sarg, acc, val) << ";\n      }";
+            if (!region_is_all(reg[k.at.at(in)], L))
+              src << " else {\n      " << acc << " = "
+                  << combine(n.sarg, acc, std::string("(") + ctype(n.type) + ")0") << ";\n      }";
+            src << "\n    }\n";
+          }
         }
-        for (int s : sp.stores) {
-          const Store &so = k.stores[s];
-          const Node &v = k.node(so.node);
-          const std::string T = ctype(v.type);
-          Emitter e(g, k, L, slots, &man, st);
-          const std::string val = e.value(so.node, 0, 0);
-          src << "    {\n      " << T << " out = (" << T << ")0;\n"
-              << "      if (" << region_test(reg[k.at.at(so.node)], L) << ") {\n"
-              << e.code << "      out = " << val << ";\n      }\n"
-              << "      ((" << T << " *)P.nxt[" << em.array_index(so.stat) << "])[i] = out;\n"
-              << "    }\n";
-        }
-        for (size_t r = 0; r < sp.reduces.size(); ++r) {
-          const Node &n = k.node(sp.reduces[r]);
-          const int in = n.args[0];
-          Emitter e(g, k, L, slots, &man, st);
-          const std::string val = e.value(in, 0, 0);
-          const std::string acc = "acc" + std::to_string(r);
-          src << "    {\n      if (" << region_test(reg[k.at.at(in)], L) << ") {\n" << e.code
-              << "      " << acc << " = " << combine(n.sarg, acc, val) << ";\n      }";
-          if (!region_is_all(reg[k.at.at(in)], L))
-            src << " else {\n      " << acc << " = "
-                << combine(n.sarg, acc, std::string("(") + ctype(n.type) + ")0") << ";\n      }";
-          src << "\n    }\n";
-        }
+        src << "  }\n";
       }
-      src << "  }\n";
       if (!sp.reduces.empty()) {
         // per-block fixed tree, partials, then the last block in block order
         for (size_t r = 0; r < sp.reduces.size(); ++r) {
