@@ -61,6 +61,41 @@ def initial_condition(size=(500, 500), boundary="open") -> og.OM:
     return om
 
 
+def linear_wave(n=64, boundary="cyclic") -> og.OM:
+    """examples-old/LinearWave/Convergence.hs:22-72: a 1-D linear wave
+    f' = g, g' = c^2 f'' on [0, 2 pi) and its energy
+    sum 0.5 (c^2 (df/dx)^2 + g^2) dx.  The earlier builder's Double-typed
+    loadIndex and loadSize are the index and size cast to double."""
+    import math
+    om = og.OM("LinearWave", (n,), boundary)
+    d = og.Double
+    F = om.static_array("fieldF", d)
+    G = om.static_array("fieldG", d)
+    E = om.static_scalar("energy", d)
+    k = om.kernel("initialize")
+    i = k.bind(og.cast(k.load_index(0), d))
+    nn = k.bind(og.cast(k.broadcast(k.load_size(0)), d))
+    x = k.bind(k.imm(2, d) * k.imm(math.pi, d) / nn * (i + 0.5))
+    k.store(F, og.sin(x))
+    k.store(G, og.cos(3 * x))
+    k = om.kernel("proceed")
+    c = k.bind(k.imm(3.43, d))
+    nn = k.bind(og.cast(k.broadcast(k.load_size(0)), d))
+    f0 = k.bind(k.load(F))
+    g0 = k.bind(k.load(G))
+    dx = k.bind(k.imm(2, d) * k.imm(math.pi, d) / nn)
+    dt = k.bind(dx / c)
+    f1 = k.bind(f0 + dt * g0)
+    fR = k.bind(k.shift(f1, -1))
+    fL = k.bind(k.shift(f1, 1))
+    g1 = k.bind(g0 + dt * c ** 2 / dx ** 2 * (fL + fR - 2 * f1))
+    k.store(F, f1)
+    k.store(G, g1)
+    dfdx = k.bind((fR - fL) / (2 * dx))
+    k.store(E, k.reduce("sum", 0.5 * (c ** 2 * dfdx ** 2 + ((g0 + g1) / 2) ** 2) * dx))
+    return om
+
+
 ADJ = list(zip([-1, 0, 1, -1, 1, -1, 0, 1], [-1, -1, -1, 0, 0, 1, 1, 1]))
 
 

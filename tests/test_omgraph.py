@@ -125,6 +125,22 @@ def test_hydro_graph_matches_reference_golden(oracle):
     assert np.float32(m.values["time"]) == np.float32(g["times"][-1])
 
 
+def test_linear_wave_energy_known_answer():
+    # examples-old/LinearWave: the scheme (f1 = f0 + dt g0, then g1 from the
+    # Laplacian of f1) keeps its discrete energy to rounding, and that energy
+    # is near the continuum value 0.5 pi (c^2 + 1) of f = sin x, g = cos 3x
+    import math
+    m = R.Machine(ex.linear_wave(64).to_text())
+    m.run("initialize")
+    es = []
+    for _ in range(300):
+        m.run("proceed")
+        es.append(float(m.values["energy"]))
+    es = np.array(es)
+    assert np.abs(es - es[0]).max() <= 1e-12 * es[0]
+    assert abs(es[0] / (0.5 * math.pi * (3.43 ** 2 + 1)) - 1) < 2e-3
+
+
 def _check(om_lib, text):
     L = om_lib.load_library()
     src = C.c_char_p()
@@ -135,7 +151,8 @@ def _check(om_lib, text):
 @pytest.mark.parametrize("make", [
     lambda: ex.hello_world(), lambda: ex.shift_example("open"),
     lambda: ex.shift_example("cyclic"), lambda: ex.initial_condition((64, 48)),
-    lambda: ex.life(), lambda: ex.life((64, 64), "open")])
+    lambda: ex.life(), lambda: ex.life((64, 64), "open"), lambda: ex.linear_wave(),
+    lambda: ex.linear_wave(48, "open")])
 def test_examples_compile_for_sm103a(om_lib, make):
     status, err, src = _check(om_lib, make().to_text())
     assert status == 0, err

@@ -157,6 +157,16 @@ def test_semantics_graph(om_lib, boundary):
     g.close()
 
 
+@pytest.mark.parametrize("n,boundary", [(64, "cyclic"), (1024, "cyclic"), (48, "open")])
+def test_linear_wave(om_lib, n, boundary):
+    # examples-old/LinearWave (1-D, double, sin/cos, shifts, a sum):
+    # 40 steps on the GPU against the oracle
+    om = ex.linear_wave(n, boundary)
+    g, m = both(om_lib, om, ["initialize"] + ["proceed"] * 40)
+    assert_same(g, m, ["fieldF", "fieldG", "energy"], rtol=1e-12)
+    g.close()
+
+
 def test_generated_source_is_available(om_lib):
     g = om_lib.GraphMachine(ex.hello_world())
     src = g.source

@@ -96,6 +96,19 @@ def test_reference_graph_drivers_compile_unchanged(om_lib, tmp_path, driver, mak
     subprocess.run(cmd, check=True)
 
 
+@pytest.mark.skipif(not os.path.isdir(REFERENCE_TREE), reason="reference tree not present")
+def test_reference_hello_gpu_driver_compiles_unchanged(om_lib, tmp_path):
+    # examples/HelloGPU: the HelloWorld machine generated for CUDA, whose
+    # driver is a .cu file built by nvcc
+    import shutil
+    from paraiso_gb300 import omgraph_examples as ex
+    emit(tmp_path, ex.hello_world(), "dist")
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    subprocess.run([nvcc, "-std=c++17", os.path.join(REFERENCE_TREE, "examples/HelloGPU/main.cu"),
+                    f"-I{INC}", f"-I{tmp_path}", f"-L{LIBDIR}", "-lom_gb300",
+                    "-Xlinker", f"-rpath={LIBDIR}", "-o", str(tmp_path / "drv")], check=True)
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("boundary", ["open", "cyclic"])
 def test_graph_driver_runs_shift_example(om_lib, tmp_path, boundary):
