@@ -159,11 +159,20 @@ def test_semantics_graph(om_lib, boundary):
 
 @pytest.mark.parametrize("n,boundary", [(64, "cyclic"), (1024, "cyclic"), (48, "open")])
 def test_linear_wave(om_lib, n, boundary):
-    # examples-old/LinearWave (1-D, double, sin/cos, shifts, a sum):
-    # 40 steps on the GPU against the oracle
+    # examples-old/LinearWave (1-D, double, sin/cos, shifts, a sum).  The
+    # start differs from numpy's sin/cos by an ulp at most; the scheme runs
+    # at Courant number 1, where such differences grow, so the 40 steps start
+    # both machines from the GPU's fields: + - * / agree bit for bit
     om = ex.linear_wave(n, boundary)
-    g, m = both(om_lib, om, ["initialize"] + ["proceed"] * 40)
-    assert_same(g, m, ["fieldF", "fieldG", "energy"], rtol=1e-12)
+    g, m = both(om_lib, om, ["initialize"])
+    assert_same(g, m, ["fieldF", "fieldG"], rtol=1e-15)
+    for name in ("fieldF", "fieldG"):
+        m.values[name] = g.read(name).reshape(np.shape(m.values[name]))
+    for _ in range(40):
+        g.run("proceed")
+        m.run("proceed")
+    assert_same(g, m, ["fieldF", "fieldG"])
+    assert_same(g, m, ["energy"], rtol=1e-12)      # block-order sum
     g.close()
 
 
