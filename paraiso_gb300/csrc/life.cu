@@ -222,6 +222,52 @@ __device__ __forceinline__ void pack_rows_vec(const int32_t *__restrict__ cur, i
   }
 }
 
+// pack_rows_vec for rows of exactly 32 words (the lane-per-word kernels),
+// with the de-interleave spread over the warp: ballots of group g are kept
+// by lanes 4g .. 4g+3, and lane L builds word L of the row from byte L % 4
+// of its group's four ballots.  Per 32-word row that is 8 loads, 32
+// ballots, 32 selects and one word-building pass of all lanes, where
+// pack_rows_vec runs the word-building pass once per group on 4 lanes.
+__device__ __forceinline__ void pack_rows32(const int32_t *__restrict__ cur, int n0, int n1,
+                                            int wd, int row0, int col0, int nr, uint32_t *dst,
+                                            int warp, int nwarps, int lane) {
+  int gx0 = col0 % wd;
+  if (gx0 < 0) gx0 += wd;
+  const bool narrow = 32 > wd;
+  const int sub = lane >> 3, quad = (lane & 7) * 4;
+  const int mine = lane >> 2, byte = (lane & 3) * 8;
+  for (int r = warp; r < nr; r += nwarps) {
+    int gy = (row0 + r) % n1;
+    if (gy < 0) gy += n1;
+    const int32_t *row = cur + (size_t)gy * n0 + quad;
+    int4 v[8];
+#pragma unroll
+    for (int g = 0; g < 8; ++g) {
+      int gx = gx0 + 4 * g + sub;
+      if (narrow) gx %= wd;
+      else if (gx >= wd) gx -= wd;
+      v[g] = __ldg(reinterpret_cast<const int4 *>(row + (size_t)gx * 32));
+    }
+    uint32_t s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+#pragma unroll
+    for (int g = 0; g < 8; ++g) {
+      const uint32_t b0 = __ballot_sync(0xffffffffu, v[g].x != 0);
+      const uint32_t b1 = __ballot_sync(0xffffffffu, v[g].y != 0);
+      const uint32_t b2 = __ballot_sync(0xffffffffu, v[g].z != 0);
+      const uint32_t b3 = __ballot_sync(0xffffffffu, v[g].w != 0);
+      if (mine == g) {
+        s0 = b0;
+        s1 = b1;
+        s2 = b2;
+        s3 = b3;
+      }
+    }
+    dst[r * 32 + lane] = spread4((s0 >> byte) & 0xFFu) | (spread4((s1 >> byte) & 0xFFu) << 1) |
+                         (spread4((s2 >> byte) & 0xFFu) << 2) |
+                         (spread4((s3 >> byte) & 0xFFu) << 3);
+  }
+}
+
 // Whole grid in shared memory: all `gens` generations in one launch.
 __global__ void __launch_bounds__(512)
 life_smallgrid_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next,
@@ -509,7 +555,7 @@ life_reg_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbP
   const int kk = p.kk;
   if (tid < 32) spop[tid] = 0;
   if (VEC)
-    pack_rows_vec<8>(cur, p.n0, p.n1, p.wd, row0 - kk, col0 - 1, NC, NR, A, warp, NW, lane);
+    pack_rows32(cur, p.n0, p.n1, p.wd, row0 - kk, col0 - 1, NR, A, warp, NW, lane);
   else
     pack_rows(cur, p.n0, p.n1, p.wd, row0 - kk, col0 - 1, NC, NR, A, warp, NW, lane);
   __syncthreads();
