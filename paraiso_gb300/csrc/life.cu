@@ -570,6 +570,10 @@ life_reg_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbP
     if (gr >= 0 && gr < th_own) ownrows |= 1u << i;
   }
   const uint32_t colmask = (lane >= 1 && lane <= tw_own) ? ~0u : 0u;
+  // most warps own all their rows or none: those count every row and keep
+  // the lane's count only if the lane and the rows are owned (no per-row
+  // test); the warps on the block's halo edges test each row
+  constexpr uint32_t allrows = R == 32 ? ~0u : ((1u << R) - 1u);
   for (int g = 0; g < kk; ++g) {
     const int b = g & 1;
     ex[b][warp][0][lane] = rows[0];
@@ -582,16 +586,31 @@ life_reg_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbP
     RowSums rb = row_sums(__shfl_up_sync(0xffffffffu, rows[0], 1), rows[0],
                           __shfl_down_sync(0xffffffffu, rows[0], 1));
     uint32_t cnt = 0;
+    if (ownrows == allrows || ownrows == 0u) {
 #pragma unroll
-    for (int i = 0; i < R; ++i) {
-      const uint32_t wn = (i + 1 < R) ? rows[i + 1] : down;
-      const RowSums rc = row_sums(__shfl_up_sync(0xffffffffu, wn, 1), wn,
-                                  __shfl_down_sync(0xffffffffu, wn, 1));
-      const uint32_t out = life_from_sums(ra, rb, rc);
-      rows[i] = out;
-      if (ownrows & (1u << i)) cnt += __popc(out & colmask);
-      ra = rb;
-      rb = rc;
+      for (int i = 0; i < R; ++i) {
+        const uint32_t wn = (i + 1 < R) ? rows[i + 1] : down;
+        const RowSums rc = row_sums(__shfl_up_sync(0xffffffffu, wn, 1), wn,
+                                    __shfl_down_sync(0xffffffffu, wn, 1));
+        const uint32_t out = life_from_sums(ra, rb, rc);
+        rows[i] = out;
+        cnt += __popc(out);
+        ra = rb;
+        rb = rc;
+      }
+      cnt &= ownrows == allrows ? colmask : 0u;
+    } else {
+#pragma unroll
+      for (int i = 0; i < R; ++i) {
+        const uint32_t wn = (i + 1 < R) ? rows[i + 1] : down;
+        const RowSums rc = row_sums(__shfl_up_sync(0xffffffffu, wn, 1), wn,
+                                    __shfl_down_sync(0xffffffffu, wn, 1));
+        const uint32_t out = life_from_sums(ra, rb, rc);
+        rows[i] = out;
+        if (ownrows & (1u << i)) cnt += __popc(out & colmask);
+        ra = rb;
+        rb = rc;
+      }
     }
     cnt = __reduce_add_sync(0xffffffffu, cnt);
     if (lane == 0 && cnt) atomicAdd(&spop[g], cnt);
