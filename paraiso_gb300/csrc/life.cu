@@ -222,20 +222,19 @@ __device__ __forceinline__ void pack_rows_vec(const int32_t *__restrict__ cur, i
   }
 }
 
-// pack_rows_vec for rows of exactly 32 words (the lane-per-word kernels),
-// with the de-interleave spread over the warp: ballots of group g are kept
-// by lanes 4g .. 4g+3, and lane L builds word L of the row from byte L % 4
-// of its group's four ballots.  Per 32-word row that is 8 loads, 32
-// ballots, 32 selects and one word-building pass of all lanes, where
-// pack_rows_vec runs the word-building pass once per group on 4 lanes.
+// pack_rows_vec for rows of exactly 32 words (the register kernel), for
+// cells that are all 0 or 1: lane L loads cells 4t .. 4t+3 (t = L % 8) of
+// word 4g + L / 8 of group g, forms their nibble shifted to bit 4t with
+// multiply-adds, and the eight lanes of a word add their nibbles (disjoint
+// bits) in three butterfly steps.  Lane 8s of each word's eight stores it.
 __device__ __forceinline__ void pack_rows32(const int32_t *__restrict__ cur, int n0, int n1,
                                             int wd, int row0, int col0, int nr, uint32_t *dst,
                                             int warp, int nwarps, int lane) {
   int gx0 = col0 % wd;
   if (gx0 < 0) gx0 += wd;
   const bool narrow = 32 > wd;
-  const int sub = lane >> 3, quad = (lane & 7) * 4;
-  const int mine = lane >> 2, byte = (lane & 3) * 8;
+  const int sub = lane >> 3, t = lane & 7, quad = t * 4;
+  const uint32_t m1 = 1u << quad, m2 = m1 << 1, m4 = m1 << 2, m8 = m1 << 3;
   for (int r = warp; r < nr; r += nwarps) {
     int gy = (row0 + r) % n1;
     if (gy < 0) gy += n1;
@@ -248,23 +247,15 @@ __device__ __forceinline__ void pack_rows32(const int32_t *__restrict__ cur, int
       else if (gx >= wd) gx -= wd;
       v[g] = __ldg(reinterpret_cast<const int4 *>(row + (size_t)gx * 32));
     }
-    uint32_t s0 = 0, s1 = 0, s2 = 0, s3 = 0;
 #pragma unroll
     for (int g = 0; g < 8; ++g) {
-      const uint32_t b0 = __ballot_sync(0xffffffffu, v[g].x != 0);
-      const uint32_t b1 = __ballot_sync(0xffffffffu, v[g].y != 0);
-      const uint32_t b2 = __ballot_sync(0xffffffffu, v[g].z != 0);
-      const uint32_t b3 = __ballot_sync(0xffffffffu, v[g].w != 0);
-      if (mine == g) {
-        s0 = b0;
-        s1 = b1;
-        s2 = b2;
-        s3 = b3;
-      }
+      uint32_t w = (uint32_t)v[g].x * m1 + (uint32_t)v[g].y * m2 + (uint32_t)v[g].z * m4 +
+                   (uint32_t)v[g].w * m8;
+      w += __shfl_xor_sync(0xffffffffu, w, 1);
+      w += __shfl_xor_sync(0xffffffffu, w, 2);
+      w += __shfl_xor_sync(0xffffffffu, w, 4);
+      if (t == 0) dst[r * 32 + 4 * g + sub] = w;
     }
-    dst[r * 32 + lane] = spread4((s0 >> byte) & 0xFFu) | (spread4((s1 >> byte) & 0xFFu) << 1) |
-                         (spread4((s2 >> byte) & 0xFFu) << 2) |
-                         (spread4((s3 >> byte) & 0xFFu) << 3);
   }
 }
 
@@ -544,7 +535,9 @@ life_reg_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbP
   extern __shared__ uint32_t A[];  // NR x NC packed words
   __shared__ uint32_t ex[2][NW][2][NC];
   __shared__ uint32_t spop[32];
+  __shared__ int4 nib[16];  // nibble -> its four cells
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid < 16) nib[tid] = make_int4(tid & 1, (tid >> 1) & 1, (tid >> 2) & 1, (tid >> 3) & 1);
   const int t = blockIdx.x;
   const int t0 = t % p.nt0, t1 = t / p.nt0;
   // tiles split the grid evenly (sizes differ by at most one word / row)
@@ -625,16 +618,14 @@ life_reg_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbP
     const uint32_t *src = A + (r + kk) * NC + 1;
     int32_t *dst = next + (size_t)(row0 + r) * p.n0 + (size_t)col0 * 32;
     if (VEC) {
+      // four cells of a word per lane, as the four cells of a nibble
       for (int c0 = 0; c0 < tw_own; c0 += 16) {
 #pragma unroll
         for (int gq = 0; gq < 4; ++gq) {
           const int cw = c0 + 4 * gq + sub;
-          if (cw < tw_own) {
-            const uint32_t wv = src[cw] >> quad;
+          if (cw < tw_own)
             *reinterpret_cast<int4 *>(dst + (size_t)cw * 32 + quad) =
-                make_int4((int)(wv & 1u), (int)((wv >> 1) & 1u), (int)((wv >> 2) & 1u),
-                          (int)((wv >> 3) & 1u));
-          }
+                nib[(src[cw] >> quad) & 15u];
         }
       }
     } else {
