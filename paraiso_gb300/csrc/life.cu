@@ -878,30 +878,33 @@ static int reg_occupancy(int device, int v, bool vec) {
 }
 
 // Launch plan for the register kernel: the variant and tile grid (nt0 x nt1,
-// tiles split evenly) minimising waves x resident-blocks x block-rows, i.e.
-// the issue time of an instruction-bound kernel including the last,
-// partly empty wave.  Returns the variant.
+// tiles split evenly).  The kernel is issue-bound and a warp issues for all
+// 32 lanes however many words its tile owns, so a block costs its rows
+// (NR) whatever its width.  The plan minimises the rows the busiest SM
+// issues (ceil(tiles / SMs) x NR), then the rows issued in all (tiles x
+// NR).  The 32-row variants need more than the 64 registers a thread has
+// at their occupancy and spill: the plan leaves them out.  Returns the
+// variant.
 static int reg_plan(int device, bool vec, int wd, int n1, int kk, int *nt0_out, int *nt1_out) {
   const int sms = sm_count(device);
-  double best_cost = 1e300;
+  double best_cost = 1e300, best_work = 1e300;
   int best_v = 1, best0 = (wd + 29) / 30, best1 = 1;
   for (int v = 0; v < kNumRegVariants; ++v) {
+    if (kRegVariants[v].R > 24) continue;
     const int NR = kRegVariants[v].R * kRegVariants[v].NW;
     const int thm = NR - 2 * kk;
     if (thm < 8) continue;
-    const int occ = reg_occupancy(device, v, vec);
-    const long long slots = (long long)occ * sms;
+    if (reg_occupancy(device, v, vec) < 1) continue;
     const int nt0min = (wd + 29) / 30;
     const int nt1min = (n1 + thm - 1) / thm;
     for (int nt0 = nt0min; nt0 <= nt0min + 2 && nt0 <= wd; ++nt0)
       for (int nt1 = nt1min; nt1 <= nt1min + 24 && nt1 <= n1; ++nt1) {
         const long long tiles = (long long)nt0 * nt1;
-        const long long waves = (tiles + slots - 1) / slots;
-        // per-tile work ~ block rows x lanes in use (owned words + 2 halo)
-        const double lanes = std::min(32.0, (double)wd / nt0 + 2.0);
-        const double cost = (double)waves * occ * NR * (lanes / 32.0 * 0.25 + 0.75);
-        if (cost < best_cost - 1e-9) {
+        const double cost = (double)((tiles + sms - 1) / sms) * NR;
+        const double work = (double)tiles * NR;
+        if (cost < best_cost - 1e-9 || (cost < best_cost + 1e-9 && work < best_work - 1e-9)) {
           best_cost = cost;
+          best_work = work;
           best_v = v;
           best0 = nt0;
           best1 = nt1;
