@@ -66,8 +66,10 @@ typedef struct {
   int variant;      /* 0 = fastest path.  Life 1: integer one-cell-per-thread kernel only.
                        Hydro 1: plain unfused FP64-structured grid-stride kernels */
   int life_io;      /* Life cell I/O of the packed kernels: 0 = 128-bit, 1 = 32-bit */
-  int life_kernel;  /* Life packed kernel: 0 = register-resident blocks,
-                       k >= 1 = warp-specialised persistent kernel, variant k-1 */
+  int life_kernel;  /* Life packed kernel: k >= 1 = warp-specialised persistent
+                       kernel, variant k-1; 0 = automatic: with tile_y 0, that
+                       kernel's variant 3 on grids of at least 1.5 of its tiles
+                       per SM, else register-resident blocks */
   int reserved[5];
 } om_config;
 

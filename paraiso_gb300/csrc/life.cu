@@ -651,7 +651,9 @@ life_ws_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbPa
   extern __shared__ uint32_t buf[];  // 3 x NR x NC packed words
   __shared__ uint32_t ex[2][NWC][2][NC];
   __shared__ uint32_t spop[32];
+  __shared__ int4 nib[16];  // nibble -> its four cells
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid < 16) nib[tid] = make_int4(tid & 1, (tid >> 1) & 1, (tid >> 2) & 1, (tid >> 3) & 1);
   const int kk = p.kk;
   const int ntiles = p.nt0 * p.nt1;
   const int m = ntiles > (int)blockIdx.x ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
@@ -687,16 +689,32 @@ life_ws_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbPa
           RowSums rb = row_sums(__shfl_up_sync(0xffffffffu, rows[0], 1), rows[0],
                                 __shfl_down_sync(0xffffffffu, rows[0], 1));
           uint32_t cnt = 0;
+          constexpr uint32_t allrows = R == 32 ? ~0u : ((1u << R) - 1u);
+          if (ownrows == allrows || ownrows == 0u) {
 #pragma unroll
-          for (int i = 0; i < R; ++i) {
-            const uint32_t wn = (i + 1 < R) ? rows[i + 1] : down;
-            const RowSums rc = row_sums(__shfl_up_sync(0xffffffffu, wn, 1), wn,
-                                        __shfl_down_sync(0xffffffffu, wn, 1));
-            const uint32_t out = life_from_sums(ra, rb, rc);
-            rows[i] = out;
-            if (ownrows & (1u << i)) cnt += __popc(out & colmask);
-            ra = rb;
-            rb = rc;
+            for (int i = 0; i < R; ++i) {
+              const uint32_t wn = (i + 1 < R) ? rows[i + 1] : down;
+              const RowSums rc = row_sums(__shfl_up_sync(0xffffffffu, wn, 1), wn,
+                                          __shfl_down_sync(0xffffffffu, wn, 1));
+              const uint32_t out = life_from_sums(ra, rb, rc);
+              rows[i] = out;
+              cnt += __popc(out);
+              ra = rb;
+              rb = rc;
+            }
+            cnt &= ownrows == allrows ? colmask : 0u;
+          } else {
+#pragma unroll
+            for (int i = 0; i < R; ++i) {
+              const uint32_t wn = (i + 1 < R) ? rows[i + 1] : down;
+              const RowSums rc = row_sums(__shfl_up_sync(0xffffffffu, wn, 1), wn,
+                                          __shfl_down_sync(0xffffffffu, wn, 1));
+              const uint32_t out = life_from_sums(ra, rb, rc);
+              rows[i] = out;
+              if (ownrows & (1u << i)) cnt += __popc(out & colmask);
+              ra = rb;
+              rb = rc;
+            }
           }
           cnt = __reduce_add_sync(0xffffffffu, cnt);
           if (lane == 0 && cnt) atomicAdd(&spop[g], cnt);
@@ -709,8 +727,8 @@ life_ws_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbPa
         // producers: pack tile s
         const int t = blockIdx.x + s * gridDim.x;
         const int col0 = (t % p.nt0) * p.tw, row0 = (t / p.nt0) * p.th;
-        pack_rows_vec<8>(cur, p.n0, p.n1, p.wd, row0 - kk, col0 - 1, NC, NR,
-                         buf + (s % 3) * NR * NC, warp - NWC, NWP, lane);
+        pack_rows32(cur, p.n0, p.n1, p.wd, row0 - kk, col0 - 1, NR, buf + (s % 3) * NR * NC,
+                    warp - NWC, NWP, lane);
       }
     } else {
       if (s >= 2) {
@@ -728,12 +746,8 @@ life_ws_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbPa
 #pragma unroll
             for (int gq = 0; gq < 4; ++gq) {
               const int cw = c0 + 4 * gq + sub;
-              if (cw < tw_own) {
-                const uint32_t wv = src[cw] >> quad;
-                *reinterpret_cast<int4 *>(dst + (size_t)cw * 32) =
-                    make_int4((int)(wv & 1u), (int)((wv >> 1) & 1u), (int)((wv >> 2) & 1u),
-                              (int)((wv >> 3) & 1u));
-              }
+              if (cw < tw_own)
+                *reinterpret_cast<int4 *>(dst + (size_t)cw * 32) = nib[(src[cw] >> quad) & 15u];
             }
           }
         }
@@ -830,6 +844,9 @@ struct WsVariant {
 static const WsVariant kWsVariants[] = {{24, 16, 8, 8}, {16, 16, 8, 8}, {24, 16, 12, 4},
                                         {20, 16, 8, 8}};
 static const int kNumWsVariants = 4;
+// the variant the automatic choice takes (fastest on GB300 at 8192^2 and
+// 16384^2), and the tiles per SM a grid needs for it
+static const int kAutoWsVariant = 3;
 
 static cudaError_t launch_ws(int v, const int32_t *cur, int32_t *next, const TbParams &p,
                              uint32_t *pop, int sms, cudaStream_t s) {
@@ -1019,12 +1036,24 @@ static om_status life_proceed(Handle *h, int n) {
       if (!reg)
         OM_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem_max));
+      // the packed kernel: life_kernel >= 1 selects the warp-specialised
+      // persistent kernel (variant life_kernel - 1); 0 with no tile shape
+      // given takes it too on grids of at least 1.5 of its tiles per SM,
+      // where it overlaps one tile's loads and stores with another's
+      // generations, and the register-resident blocks on smaller grids
+      int ws = h->cfg.life_kernel;
+      if (reg && ws == 0 && st->tile_h == 0) {
+        const WsVariant wv = kWsVariants[kAutoWsVariant];
+        const int th = std::min(wv.R * wv.NWC - 2 * kmax, n1);
+        const long long tiles = (long long)((wd + 29) / 30) * ((n1 + th - 1) / th);
+        if (th > 0 && 2 * tiles >= 3LL * sm_count(h->device)) ws = kAutoWsVariant + 1;
+      }
       for (int l = 0; l < nl; ++l) {
         const int kk = rem / nl + (l < rem % nl ? 1 : 0);
         p.kk = kk;
-        if (reg && h->cfg.life_kernel >= 1) {
-          // warp-specialised persistent kernel, variant life_kernel - 1
-          const int v = std::min(h->cfg.life_kernel - 1, kNumWsVariants - 1);
+        if (reg && ws >= 1) {
+          // warp-specialised persistent kernel, variant ws - 1
+          const int v = std::min(ws - 1, kNumWsVariants - 1);
           const WsVariant wv = kWsVariants[v];
           TbParams q = p;
           q.tw = std::min(30, wd);

@@ -82,6 +82,32 @@ def test_life_warp_specialised(om_lib, oracle, kernel, depth):
     assert np.array_equal(pops, rp)
 
 
+def test_life_automatic_kernel_choice(om_lib):
+    # with no kernel or tile shape given, a grid of at least 1.5 warp-
+    # specialised tiles per SM runs on that kernel and a smaller one on the
+    # register-resident blocks; both equal the register-resident blocks
+    # forced by a tile height (pinned to the oracle above) bit for bit
+    pg = om_lib
+    for size, want in [((8192, 8192), "life_ws_kernel"), ((2048, 1024), "life_reg_kernel")]:
+        init = None
+        out = []
+        for cfg in ({}, {"tile_y": 320}):
+            life = pg.Life(size, **cfg)
+            if init is None:
+                life.fill_random(5, 0.3)
+                init = life.read("cell")
+            else:
+                life.write("cell", init)
+            life.profile(True)
+            life.proceed(70)
+            if not cfg:
+                assert life.profile_query(want)[0] >= 2
+            out.append((life.read("cell"), life.population_history(70)))
+            life.close()
+        assert np.array_equal(out[0][0], out[1][0])
+        assert np.array_equal(out[0][1], out[1][1])
+
+
 def test_life_nonbinary_first_step(om_lib, oracle):
     init = oracle.life_bernoulli(256, 96, 2, 0.3)
     init[10, 10] = 3
