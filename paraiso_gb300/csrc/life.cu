@@ -659,9 +659,42 @@ life_ws_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbPa
   const int m = ntiles > (int)blockIdx.x ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
   if (tid < 32) spop[tid] = 0;
   __syncthreads();
+  constexpr int NWT = NWC + NWP + NWS;
+  // write back the owned words of tile t from shared-memory buffer A, by
+  // warps sw .. of nsw
+  auto store_tile = [&](int t, const uint32_t *A, int sw, int nsw) {
+    const int col0 = (t % p.nt0) * p.tw, row0 = (t / p.nt0) * p.th;
+    const int tw_own = min(p.tw, p.wd - col0), th_own = min(p.th, p.n1 - row0);
+    const int sub = lane >> 3, quad = (lane & 7) * 4;
+    for (int r = sw; r < th_own; r += nsw) {
+      const uint32_t *src = A + (r + kk) * NC + 1;
+      int32_t *dst = next + (size_t)(row0 + r) * p.n0 + (size_t)col0 * 32 + quad;
+      for (int c0 = 0; c0 < tw_own; c0 += 16) {
+#pragma unroll
+        for (int gq = 0; gq < 4; ++gq) {
+          const int cw = c0 + 4 * gq + sub;
+          if (cw < tw_own)
+            *reinterpret_cast<int4 *>(dst + (size_t)cw * 32) = nib[(src[cw] >> quad) & 15u];
+        }
+      }
+    }
+  };
+  auto pack_tile = [&](int s, int pw, int npw) {
+    const int t = blockIdx.x + s * gridDim.x;
+    const int col0 = (t % p.nt0) * p.tw, row0 = (t / p.nt0) * p.th;
+    pack_rows32(cur, p.n0, p.n1, p.wd, row0 - kk, col0 - 1, NR, buf + (s % 3) * NR * NC, pw,
+                npw, lane);
+  };
+  // Stage 0 only packs and stage m + 1 only stores: there every warp of the
+  // block takes part; in stage m the producers, with no tile left to pack,
+  // help the store warps.
   for (int s = 0; s < m + 2; ++s) {
-    if (warp < NWC) {
-      if (s >= 1 && s <= m) {
+    if (s == 0) {
+      if (m > 0) pack_tile(0, warp, NWT);
+    } else if (s == m + 1) {
+      if (m > 0) store_tile(blockIdx.x + (s - 2) * gridDim.x, buf + ((s - 2) % 3) * NR * NC, warp, NWT);
+    } else if (warp < NWC) {
+      {
         // consumers: advance tile s-1
         const int t = blockIdx.x + (s - 1) * gridDim.x;
         const int col0 = (t % p.nt0) * p.tw, row0 = (t / p.nt0) * p.th;
@@ -723,35 +756,16 @@ life_ws_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbPa
         for (int i = 0; i < R; ++i) A[(warp * R + i) * NC + lane] = rows[i];
       }
     } else if (warp < NWC + NWP) {
-      if (s < m) {
-        // producers: pack tile s
-        const int t = blockIdx.x + s * gridDim.x;
-        const int col0 = (t % p.nt0) * p.tw, row0 = (t / p.nt0) * p.th;
-        pack_rows32(cur, p.n0, p.n1, p.wd, row0 - kk, col0 - 1, NR, buf + (s % 3) * NR * NC,
-                    warp - NWC, NWP, lane);
-      }
-    } else {
-      if (s >= 2) {
-        // store warps: write back tile s-2
-        const int t = blockIdx.x + (s - 2) * gridDim.x;
-        const int col0 = (t % p.nt0) * p.tw, row0 = (t / p.nt0) * p.th;
-        const int tw_own = min(p.tw, p.wd - col0), th_own = min(p.th, p.n1 - row0);
-        const uint32_t *A = buf + ((s - 2) % 3) * NR * NC;
-        const int sw = warp - NWC - NWP;
-        const int sub = lane >> 3, quad = (lane & 7) * 4;
-        for (int r = sw; r < th_own; r += NWS) {
-          const uint32_t *src = A + (r + kk) * NC + 1;
-          int32_t *dst = next + (size_t)(row0 + r) * p.n0 + (size_t)col0 * 32 + quad;
-          for (int c0 = 0; c0 < tw_own; c0 += 16) {
-#pragma unroll
-            for (int gq = 0; gq < 4; ++gq) {
-              const int cw = c0 + 4 * gq + sub;
-              if (cw < tw_own)
-                *reinterpret_cast<int4 *>(dst + (size_t)cw * 32) = nib[(src[cw] >> quad) & 15u];
-            }
-          }
-        }
-      }
+      if (s < m)
+        pack_tile(s, warp - NWC, NWP);
+      else if (s >= 2)  // s == m
+        store_tile(blockIdx.x + (s - 2) * gridDim.x, buf + ((s - 2) % 3) * NR * NC, warp - NWC,
+                   NWP + NWS);
+    } else if (s >= 2) {
+      // store warps: write back tile s - 2
+      const bool helped = s == m;
+      store_tile(blockIdx.x + (s - 2) * gridDim.x, buf + ((s - 2) % 3) * NR * NC,
+                 helped ? warp - NWC : warp - NWC - NWP, helped ? NWP + NWS : NWS);
     }
     __syncthreads();
   }
