@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -881,12 +882,14 @@ static cudaError_t launch_ws(int v, const int32_t *cur, int32_t *next, const TbP
   return cudaGetLastError();
 }
 
-// Resident blocks per SM of a register variant (queried once per device).
+// Resident blocks per SM of a register variant (queried once per device;
+// handles on other host threads may ask at the same time).
 static int reg_occupancy(int device, int v, bool vec) {
-  static int cache[64][kNumRegVariants][2];
+  static std::atomic<int> cache[64][kNumRegVariants][2];
   if (device < 0 || device >= 64) return 1;
-  int &c = cache[device][v][vec ? 1 : 0];
-  if (c) return c;
+  std::atomic<int> &c = cache[device][v][vec ? 1 : 0];
+  const int known = c.load(std::memory_order_relaxed);
+  if (known) return known;
   const RegVariant rv = kRegVariants[v];
   const size_t smem = sizeof(uint32_t) * 32 * rv.R * rv.NW;
   void (*k)(const int32_t *, int32_t *, TbParams, uint32_t *) = nullptr;
@@ -904,7 +907,7 @@ static int reg_occupancy(int device, int v, bool vec) {
     cudaGetLastError();
     n = 1;
   }
-  c = n;
+  c.store(n, std::memory_order_relaxed);
   return n;
 }
 
