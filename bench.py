@@ -177,7 +177,7 @@ def life_workload(args, dist: Dist) -> dict:
     life.time_run("proceed", gens * min(args.steps, 4))
     best = None
     for kn in ("life_reg_kernel", "life_ws_kernel", "life_tb32_kernel", "life_tb_kernel",
-               "life_smallgrid_kernel", "life_general_kernel"):
+               "life_smallreg_kernel", "life_smallgrid_kernel", "life_general_kernel"):
         q = life.profile_query(kn)
         if q[0] and (best is None or q[1] > best[1][1]):
             best = (kn, q)

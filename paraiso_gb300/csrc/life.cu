@@ -435,6 +435,75 @@ __device__ __forceinline__ uint32_t life_from_sums(const RowSums &a, const RowSu
   return ~u2 & (u1 ^ k0) & (s0 | b.raw);
 }
 
+// Whole grid in registers, one packed word per thread: all `gens`
+// generations in one launch of one CTA.  The grid is wd = n0 / 32 words
+// wide with wd dividing 32, so a warp holds 32 / wd whole rows: lane L has
+// word L % wd of row L / wd of its warp.  West and east words come from
+// the lanes beside (wrapping within the row), the row sums of the rows
+// above and below from lanes L -+ wd; the warp's top and bottom rows take
+// them from the neighbouring warps through shared memory (double-buffered
+// by generation parity, so one barrier per generation).  Each warp adds its
+// population into pop[g] (zeroed by the caller).
+__global__ void __launch_bounds__(1024)
+life_smallreg_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, int n0, int n1,
+                     int gens, uint32_t *__restrict__ pop) {
+  __shared__ uint32_t top[2][32][2][32];  // [parity][warp][f1, f2][word]: first row's sums
+  __shared__ uint32_t bot[2][32][2][32];  // last row's sums
+  const int wd = n0 >> 5, rw = 32 / wd;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int x = lane % wd, r = lane / wd, y = warp * rw + r;
+  // pack this thread's word: cells 32x .. 32x + 31 of row y
+  const int32_t *src = cur + (size_t)y * n0 + 32 * x;
+  uint32_t w = 0;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int4 v = __ldg(reinterpret_cast<const int4 *>(src) + q);
+    w |= ((uint32_t)v.x | ((uint32_t)v.y << 1) | ((uint32_t)v.z << 2) | ((uint32_t)v.w << 3))
+         << (4 * q);
+  }
+  const int west = x == 0 ? lane + wd - 1 : lane - 1;
+  const int east = x == wd - 1 ? lane - wd + 1 : lane + 1;
+  const int up = (lane - wd) & 31, down = (lane + wd) & 31;
+  const bool first = r == 0, last = r == rw - 1;
+  const int wup = warp == 0 ? nw - 1 : warp - 1, wdown = warp == nw - 1 ? 0 : warp + 1;
+  for (int g = 0; g < gens; ++g) {
+    const int b = g & 1;
+    const RowSums me = row_sums(__shfl_sync(0xffffffffu, w, west), w,
+                                __shfl_sync(0xffffffffu, w, east));
+    if (first) {
+      top[b][warp][0][x] = me.f1;
+      top[b][warp][1][x] = me.f2;
+    }
+    if (last) {
+      bot[b][warp][0][x] = me.f1;
+      bot[b][warp][1][x] = me.f2;
+    }
+    RowSums a, c;
+    a.f1 = __shfl_sync(0xffffffffu, me.f1, up);
+    a.f2 = __shfl_sync(0xffffffffu, me.f2, up);
+    c.f1 = __shfl_sync(0xffffffffu, me.f1, down);
+    c.f2 = __shfl_sync(0xffffffffu, me.f2, down);
+    __syncthreads();
+    if (first) {
+      a.f1 = bot[b][wup][0][x];
+      a.f2 = bot[b][wup][1][x];
+    }
+    if (last) {
+      c.f1 = top[b][wdown][0][x];
+      c.f2 = top[b][wdown][1][x];
+    }
+    w = life_from_sums(a, me, c);
+    const uint32_t cnt = __reduce_add_sync(0xffffffffu, __popc(w));
+    if (lane == 0 && cnt) atomicAdd(&pop[g], cnt);
+  }
+  int32_t *dst = next + (size_t)y * n0 + 32 * x;
+#pragma unroll
+  for (int q = 0; q < 8; ++q)
+    reinterpret_cast<int4 *>(dst)[q] =
+        make_int4((int)((w >> (4 * q)) & 1u), (int)((w >> (4 * q + 1)) & 1u),
+                  (int)((w >> (4 * q + 2)) & 1u), (int)((w >> (4 * q + 3)) & 1u));
+}
+
 // Temporal blocking with one lane per packed word: a tile is 32 words wide
 // (30 owned + a halo word each side) and th rows tall plus kk halo rows above
 // and below.  Each warp sweeps a contiguous band of rows per generation,
@@ -1022,7 +1091,16 @@ static om_status life_proceed(Handle *h, int n) {
   }
   if (g < n) {
     const int wd = n0 / 32;
-    if ((size_t)wd * n1 <= (size_t)kSmallMaxWords) {
+    if (32 % wd == 0 && (n1 * wd) % 32 == 0 && n1 * wd <= 1024 && n1 * wd >= 32) {
+      // one packed word per thread of one CTA, in registers
+      cudaEvent_t ev = prof_begin(h);
+      life_smallreg_kernel<<<1, n1 * wd, 0, h->stream>>>(
+          (const int32_t *)a.d(), (int32_t *)a.d_next(), n0, n1, n - g, st->d_pop + g);
+      OM_CUDA_CHECK(cudaGetLastError());
+      prof_end(h, ev, "life_smallreg_kernel", (double)n0 * n1 * (n - g));
+      h->launches++;
+      a.swap();
+    } else if ((size_t)wd * n1 <= (size_t)kSmallMaxWords) {
       const size_t smem = 2 * sizeof(uint32_t) * (size_t)wd * n1;
       OM_CUDA_CHECK(cudaFuncSetAttribute(life_smallgrid_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,

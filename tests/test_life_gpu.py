@@ -82,6 +82,24 @@ def test_life_warp_specialised(om_lib, oracle, kernel, depth):
     assert np.array_equal(pops, rp)
 
 
+@pytest.mark.parametrize("size", [(128, 128), (1024, 1), (512, 2), (256, 4), (64, 16), (32, 32),
+                                  (1024, 32), (512, 64)])
+def test_life_small_grid_in_registers(om_lib, oracle, size):
+    # grids of at most 1024 packed words with rows of 1, 2, 4, 8, 16 or 32
+    # words run in one CTA, one word per thread (life_smallreg_kernel)
+    pg = om_lib
+    init = oracle.life_bernoulli(size[0], size[1], 23, 0.35)
+    life = pg.Life(size)
+    life.write("cell", init)
+    life.profile(True)
+    life.proceed(300)
+    assert life.profile_query("life_smallreg_kernel")[0] == 1
+    rc, rp = oracle.life_run(init, 300, cyclic=True)
+    assert np.array_equal(life.read("cell"), rc)
+    assert np.array_equal(life.population_history(300), rp)
+    life.close()
+
+
 def test_life_automatic_kernel_choice(om_lib):
     # with no kernel or tile shape given, a grid of at least 1.5 warp-
     # specialised tiles per SM runs on that kernel and a smaller one on the
