@@ -285,6 +285,20 @@ adj_stage2_tile(Fields<R> Ub, Fields<R> U1b, Fields<R> Pbase, Geo<R> G, double *
       cp_async(&stg[4 + c][by][bx], &Ub.f[c][gi]);
     }
   }
+  // the last phase reads the tile's taped flux differences of both stages
+  // and its previous state per cell: bring their lines into L2 while the
+  // earlier phases run
+  {
+    constexpr int kLine = 128 / (int)sizeof(R);           // elements per 128-byte line
+    constexpr int LPR = (TX + kLine - 1) / kLine;         // lines per tile row
+    for (int k = tid; k < 20 * TY * LPR; k += nthr) {
+      const int arr = k / (TY * LPR), rem = k - arr * (TY * LPR);
+      const int ry = rem / LPR, x = X0 + (rem - ry * LPR) * kLine, y = Y0 + ry;
+      if (y >= G.n1 || x >= G.n0) continue;
+      const R *base = arr < 16 ? T.array(kTapeD1 + arr) : P.f[arr - 16];
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(base + (size_t)y * G.n0 + x));
+    }
+  }
   cp_async_wait_all();
   const R d0 = G.dt / G.dR0, d1 = G.dt / G.dR1;
   // the previous reverse step's dt cotangent, when its arg-min cell lies in
