@@ -132,6 +132,42 @@ static om_status perr(int line, const std::string &what) {
   return OM_ERR_ARG;
 }
 
+// Structurally equal nodes (same operation, realm, type, literal or static,
+// vector and operands) compute the same value: keep the first of each class
+// and point every use at it.  The Haskell builder makes a new node for each
+// application of a function, so a graph such as examples/Hydro repeats
+// literals, comparisons and whole expressions.  Merged, the field selects of
+// one HLLC wall record share their condition, which lets the emitter branch
+// on it once for the whole record.  A class is Manifest if any member was.
+static void merge_duplicates(KernelDef &k) {
+  std::map<std::string, int> first;
+  std::map<int, int> rep;
+  std::vector<Node> kept;
+  std::map<int, int> at;
+  for (Node n : k.nodes) {
+    for (int &a : n.args) a = rep.at(a);
+    std::ostringstream key;
+    key << n.op << '|' << n.array << '|' << (int)n.type << '|' << n.sarg << '|' << n.vec[0] << '|'
+        << n.vec[1];
+    for (int a : n.args) key << '|' << a;
+    const auto it = first.find(key.str());
+    if (it != first.end()) {
+      rep[n.id] = it->second;
+      continue;
+    }
+    first[key.str()] = n.id;
+    rep[n.id] = n.id;
+    at[n.id] = (int)kept.size();
+    kept.push_back(n);
+  }
+  for (Store &st : k.stores) st.node = rep.at(st.node);
+  std::set<int> man;
+  for (int m : k.manifest) man.insert(rep.at(m));
+  k.nodes = kept;
+  k.at = at;
+  k.manifest = man;
+}
+
 static om_status parse(const char *text, Graph *g) {
   std::istringstream in(text);
   std::string l;
@@ -180,6 +216,7 @@ static om_status parse(const char *text, Graph *g) {
     }
     if (w[0] == "end") {
       if (!k) return perr(ln, "end outside a kernel");
+      merge_duplicates(*k);
       k = nullptr;
       continue;
     }
@@ -392,7 +429,10 @@ class Emitter {
   Emitter(const Graph &g, const KernelDef &k, const Layout &L,
           const std::map<int, int> &slot_of_reduce,
           const std::map<int, ManifestAt> *manifests = nullptr, int stage = 0)
-      : g_(g), k_(k), L_(L), slots_(slot_of_reduce), man_(manifests), stage_(stage) {}
+      : g_(g), k_(k), L_(L), slots_(slot_of_reduce), man_(manifests), stage_(stage) {
+    for (const Node &n : k.nodes)
+      if (n.op == "select" && n.array) groups_[n.args[0]].push_back(n.id);
+  }
 
   std::string code;
 
@@ -444,6 +484,10 @@ class Emitter {
       expr = "(*(const " + T + " *)(slots + " + std::to_string(8 * slots_.at(id)) + "))";
     } else if (n.op == "broadcast") {
       return memo_[key] = value(n.args[0], 0, 0);
+    } else if (n.op == "select" && lazy_ && n.array &&
+               !open_.count(std::make_tuple(n.args[0], o0, o1))) {
+      select_group(n.args[0], o0, o1);
+      return memo_.at(key);
     } else {
       std::vector<std::string> a;
       for (int x : n.args) a.push_back(value(x, o0, o1));
@@ -459,6 +503,14 @@ class Emitter {
     for (int i = 0; i < s; ++i) k += g_.statics[i].array ? 1 : 0;
     return k;
   }
+
+  // Branch on a select's condition instead of computing both operands:
+  // every array select with that condition (the fields of one record) is
+  // assigned in one if/else, each side computing only its operands.  Values
+  // first computed inside a side stay there (the memo is restored after
+  // it), so the arithmetic of every value is unchanged.  Not for four cells
+  // per thread, whose shuffles need the whole warp.
+  void lazy_selects(bool on) { lazy_ = on; }
 
   // values that a tile phase computes, read from its tile (phase two of a
   // tiled stage)
@@ -541,6 +593,36 @@ class Emitter {
     return "((" + x + " % " + N + " + " + N + ") % " + N + ")";
   }
 
+  void select_group(int c, int o0, int o1) {
+    const std::string cv = value(c, o0, o1);
+    std::vector<int> todo;
+    for (int sid : groups_.at(c))
+      if (!memo_.count(std::make_tuple(sid, o0, o1))) todo.push_back(sid);
+    std::vector<std::string> names;
+    for (int sid : todo) {
+      const std::string v = "v" + std::to_string(sid) + "_" + off_name(o0) + "_" + off_name(o1);
+      code += "      " + std::string(ctype(k_.node(sid).type)) + " " + v + ";\n";
+      names.push_back(v);
+    }
+    open_.insert(std::make_tuple(c, o0, o1));
+    const auto memo0 = memo_;
+    const auto cols0 = cols_;
+    const auto rows0 = rows_;
+    for (int side = 1; side <= 2; ++side) {
+      code += side == 1 ? "      if (" + cv + ") {\n" : "      } else {\n";
+      for (size_t i = 0; i < todo.size(); ++i) {
+        const std::string x = value(k_.node(todo[i]).args[side], o0, o1);
+        code += "      " + names[i] + " = " + x + ";\n";
+      }
+      memo_ = memo0;
+      cols_ = cols0;
+      rows_ = rows0;
+    }
+    code += "      }\n";
+    open_.erase(std::make_tuple(c, o0, o1));
+    for (size_t i = 0; i < todo.size(); ++i) memo_[std::make_tuple(todo[i], o0, o1)] = names[i];
+  }
+
   // the column c0 + o (wrapped on a cyclic mesh) and the memory offset of
   // row c1 + o, each declared once per cell and shared by every load
   std::string col(int o) {
@@ -618,6 +700,9 @@ class Emitter {
   std::map<int, std::string> cols_, rows_;
   std::map<std::pair<std::string, int>, std::vector<std::string>> vecs_;
   int V_ = 1, nshfl_ = 0;
+  bool lazy_ = false;
+  std::map<int, std::vector<int>> groups_;     // condition -> array selects on it
+  std::set<std::tuple<int, int, int>> open_;   // (condition, offset) being emitted
   const std::map<int, TileAt> *tiles_ = nullptr;
   TileShape shape_;
 };
@@ -810,6 +895,7 @@ static void emit_tiled(std::ostringstream &src, const Graph &g, const KernelDef 
       << "      (void)i;\n";
   {
     Emitter first(g, k, L, slots, &man, st);
+    first.lazy_selects(true);
     std::vector<std::string> vals;
     for (const auto &t : tiles) vals.push_back(first.value(t.first, 0, 0));
     src << "    {\n" << first.code;
@@ -824,6 +910,7 @@ static void emit_tiled(std::ostringstream &src, const Graph &g, const KernelDef 
       << "      if (c0 >= " << n0 << " || c1 >= " << n1 << ") continue;\n"
       << "      const long long i = (long long)c1 * " << n0 << " + c0;\n";
   Emitter second(g, k, L, slots, &man, st);
+  second.lazy_selects(true);
   second.tiled(&tiles, sh);
   std::vector<std::string> vals;
   for (int r : stage_roots(k, sp)) vals.push_back(second.value(r, 0, 0));
@@ -955,7 +1042,18 @@ static std::string generate(const Graph &g, const Layout &L, std::vector<KernelP
         for (int s : sp.stores) trial.value(k.stores[s].node, 0, 0);
         for (int id : sp.reduces) trial.value(k.node(id).args[0], 0, 0);
         for (int id : sp.manifests) trial.value(id, 0, 0);
-        if (std::count(trial.code.begin(), trial.code.end(), '\n') <= kMaxVectorStatements)
+        // a stage that selects whole records (two or more selects on one
+        // condition) stays at one cell per thread, where it can branch on
+        // the condition instead (Emitter::lazy_selects)
+        std::map<int, int> on_condition;
+        for (const auto &o : trial.offsets()) {
+          const Node &n = k.node(o.first);
+          if (n.op == "select" && n.array) ++on_condition[n.args[0]];
+        }
+        bool records = false;
+        for (const auto &c : on_condition) records = records || c.second >= 2;
+        if (!records &&
+            std::count(trial.code.begin(), trial.code.end(), '\n') <= kMaxVectorStatements)
           V = kCellsPerThread;
       }
       std::map<int, TileAt> tiles;
@@ -981,6 +1079,7 @@ static std::string generate(const Graph &g, const Layout &L, std::vector<KernelP
         if (shared) {
           Emitter e(g, k, L, slots, &man, st);
           e.cells_per_thread(V);
+          e.lazy_selects(V == 1);
           // vals[c][...]: cell c's stores, reduce inputs and manifests
           std::vector<std::vector<std::string>> vals(V);
           for (int c = 0; c < V; ++c) {
@@ -1029,6 +1128,7 @@ static std::string generate(const Graph &g, const Layout &L, std::vector<KernelP
           for (int id : sp.manifests) {
             const std::string T = ctype(k.node(id).type);
             Emitter e(g, k, L, slots, &man, st);
+            e.lazy_selects(true);
             const std::string val = e.value(id, 0, 0);
             src << "    {\n      if (" << region_test(reg[k.at.at(id)], L) << ") {\n" << e.code
                 << "      ((" << T << " *)P.tmp[" << man.at(id).tmp << "])[i] = " << val << ";\n"
@@ -1039,6 +1139,7 @@ static std::string generate(const Graph &g, const Layout &L, std::vector<KernelP
             const Node &v = k.node(so.node);
             const std::string T = ctype(v.type);
             Emitter e(g, k, L, slots, &man, st);
+            e.lazy_selects(true);
             const std::string val = e.value(so.node, 0, 0);
             src << "    {\n      " << T << " out = (" << T << ")0;\n"
                 << "      if (" << region_test(reg[k.at.at(so.node)], L) << ") {\n"
@@ -1050,6 +1151,7 @@ static std::string generate(const Graph &g, const Layout &L, std::vector<KernelP
             const Node &n = k.node(sp.reduces[r]);
             const int in = n.args[0];
             Emitter e(g, k, L, slots, &man, st);
+            e.lazy_selects(true);
             const std::string val = e.value(in, 0, 0);
             const std::string acc = "acc" + std::to_string(r);
             src << "    {\n      if (" << region_test(reg[k.at.at(in)], L) << ") {\n" << e.code
