@@ -182,7 +182,7 @@ extern "C" om_status om_load(om_handle H, const char *path) {
 // The text snapshot of examples/Hydro/main-kh.cpp:17-31 (antiAlias 1): per
 // interior cell "x y density velocity0 velocity1 pressure" with x = dR0
 // (ix + 0.5), y = dR1 (iy + 0.5), a blank line after each row, written with
-// the stream defaults the driver uses.
+// the default std::ostream formatting that main-kh.cpp uses.
 extern "C" om_status om_hydro_write_snapshot(om_handle H, const char *path) {
   Handle *h = handle_of(H);
   if (!h || !path || h->kind != OM_KIND_HYDRO) {
