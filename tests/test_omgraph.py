@@ -175,6 +175,33 @@ def test_row_vectors_on_rows_of_whole_chunks(om_lib):
     assert "om_v4i *)" not in src and "__shfl" not in src
 
 
+def test_duplicates_merged_and_records_branched(om_lib):
+    # examples/Hydro repeats literals, comparisons and expressions; merged,
+    # the field selects of an HLLC wall record share one condition, and the
+    # one-cell-per-thread wall stages branch on it once per record; the
+    # stage-2 walls read the stage-1 state from a shared-memory tile
+    g = ex.hydro((256, 256), gamma=1.4, boundary="cyclic", typ=og.Float)
+    status, err, src = _check(om_lib, g.to_text())
+    assert status == 0, err
+    stages = src.split('extern "C" __global__')
+    walls2 = [t for t in stages if "om_k1_s2(" in t][0]
+    assert "__shared__ float tile" in walls2
+    assert walls2.count("      if (v") >= 8
+    assert "threadIdx.x * 4" not in walls2
+    # merging keeps one node per distinct value: a graph whose two stores
+    # repeat one expression computes it once
+    om = og.OM("Dup", (64, 32), "cyclic")
+    a = om.static_array("a", og.Double)
+    b = om.static_array("b", og.Double)
+    k = om.kernel("step")
+    x = k.load(a)
+    k.store(a, og.sqrt(og.abs_(x) + 1) * 3)
+    k.store(b, og.sqrt(og.abs_(k.load(a)) + 1) * 3)
+    status, err, src = _check(om_lib, om.to_text())
+    assert status == 0, err
+    assert src.count("sqrt(") == 1   # rows of 64 cells: one cell per thread
+
+
 def test_graph_errors_are_reported(om_lib):
     bad = [
         "om T 3 4 4 4 cyclic\n",                                   # 3-D
