@@ -260,6 +260,60 @@ __device__ __forceinline__ void pack_rows32(const int32_t *__restrict__ cur, int
   }
 }
 
+// pack_rows32 with each lane's cells staged in shared memory by
+// asynchronous 16-byte copies, two rows in flight per warp: the loads of the
+// next row are under way while this row's nibbles are summed, and no
+// registers are held by loads in flight.  A lane reads back only the cells it
+// copied itself, so the warp needs no barrier.  `stage` is 2 x 256 int4 of
+// this warp.
+__device__ __forceinline__ void pack_rows32_async(const int32_t *__restrict__ cur, int n0, int n1,
+                                                  int wd, int row0, int col0, int nr,
+                                                  uint32_t *dst, int warp, int nwarps, int lane,
+                                                  int4 *stage) {
+  int gx0 = col0 % wd;
+  if (gx0 < 0) gx0 += wd;
+  const bool narrow = 32 > wd;
+  const int sub = lane >> 3, t = lane & 7, quad = t * 4;
+  const uint32_t m1 = 1u << quad, m2 = m1 << 1, m4 = m1 << 2, m8 = m1 << 3;
+  auto issue = [&](int r, int4 *into) {
+    int gy = (row0 + r) % n1;
+    if (gy < 0) gy += n1;
+    const int32_t *row = cur + (size_t)gy * n0 + quad;
+#pragma unroll
+    for (int g = 0; g < 8; ++g) {
+      int gx = gx0 + 4 * g + sub;
+      if (narrow) gx %= wd;
+      else if (gx >= wd) gx -= wd;
+      const unsigned d = (unsigned)__cvta_generic_to_shared(into + g * 32 + lane);
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d),
+                   "l"(row + (size_t)gx * 32)
+                   : "memory");
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  };
+  int i = 0;
+  if (warp < nr) issue(warp, stage);
+  for (int r = warp; r < nr; r += nwarps, ++i) {
+    int4 *cur_stage = stage + (i & 1) * 256;
+    if (r + nwarps < nr) {
+      issue(r + nwarps, stage + ((i + 1) & 1) * 256);
+      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    }
+#pragma unroll
+    for (int g = 0; g < 8; ++g) {
+      const int4 v = cur_stage[g * 32 + lane];
+      uint32_t w = (uint32_t)v.x * m1 + (uint32_t)v.y * m2 + (uint32_t)v.z * m4 +
+                   (uint32_t)v.w * m8;
+      w += __shfl_xor_sync(0xffffffffu, w, 1);
+      w += __shfl_xor_sync(0xffffffffu, w, 2);
+      w += __shfl_xor_sync(0xffffffffu, w, 4);
+      if (t == 0) dst[r * 32 + 4 * g + sub] = w;
+    }
+  }
+}
+
 // Whole grid in shared memory: all `gens` generations in one launch.
 __global__ void __launch_bounds__(512)
 life_smallgrid_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next,
@@ -713,6 +767,13 @@ life_reg_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbP
 // the consumers use), and store warps write tile s-2 back, so loads,
 // compute and stores of consecutive tiles overlap.  One __syncthreads ends
 // every stage; there are no spin waits.
+// whether a warp-specialised variant has room for its producers' staged rows
+// (2 x 4 KB each) beside its three tile buffers
+template <int R, int NWC, int NWP>
+__host__ __device__ constexpr bool kStagedPack() {
+  return 3 * 4 * 32 * R * NWC + 8192 * NWP <= 212992;
+}
+
 template <int R, int NWC, int NWP, int NWS>
 __global__ void __launch_bounds__((NWC + NWP + NWS) * 32, 1)
 life_ws_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbParams p,
@@ -754,6 +815,14 @@ life_ws_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbPa
     const int col0 = (t % p.nt0) * p.tw, row0 = (t / p.nt0) * p.th;
     pack_rows32(cur, p.n0, p.n1, p.wd, row0 - kk, col0 - 1, NR, buf + (s % 3) * NR * NC, pw,
                 npw, lane);
+  };
+  // the producers' staging rows follow the three tile buffers
+  int4 *stage = reinterpret_cast<int4 *>(buf + 3 * NR * NC);
+  auto pack_tile_async = [&](int s, int pw) {
+    const int t = blockIdx.x + s * gridDim.x;
+    const int col0 = (t % p.nt0) * p.tw, row0 = (t / p.nt0) * p.th;
+    pack_rows32_async(cur, p.n0, p.n1, p.wd, row0 - kk, col0 - 1, NR, buf + (s % 3) * NR * NC,
+                      pw, NWP, lane, stage + pw * 512);
   };
   // Stage 0 only packs and stage m + 1 only stores: there every warp of the
   // block takes part; in stage m the producers, with no tile left to pack,
@@ -827,7 +896,10 @@ life_ws_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbPa
       }
     } else if (warp < NWC + NWP) {
       if (s < m)
-        pack_tile(s, warp - NWC, NWP);
+        if (kStagedPack<R, NWC, NWP>())
+          pack_tile_async(s, warp - NWC);
+        else
+          pack_tile(s, warp - NWC, NWP);
       else if (s >= 2)  // s == m
         store_tile(blockIdx.x + (s - 2) * gridDim.x, buf + ((s - 2) % 3) * NR * NC, warp - NWC,
                    NWP + NWS);
@@ -935,7 +1007,10 @@ static const int kAutoWsVariant = 3;
 static cudaError_t launch_ws(int v, const int32_t *cur, int32_t *next, const TbParams &p,
                              uint32_t *pop, int sms, cudaStream_t s) {
   const WsVariant wv = kWsVariants[v];
-  const size_t smem = sizeof(uint32_t) * 3 * 32 * wv.R * wv.NWC;
+  // three tile buffers, then two staged rows (2 x 4 KB) per producer warp
+  const bool staged = 3 * 4 * 32 * wv.R * wv.NWC + 8192 * wv.NWP <= 212992;
+  const size_t smem =
+      sizeof(uint32_t) * 3 * 32 * wv.R * wv.NWC + (staged ? sizeof(int4) * 512 * wv.NWP : 0);
   void (*k)(const int32_t *, int32_t *, TbParams, uint32_t *) = nullptr;
   switch (v) {
     case 0: k = life_ws_kernel<24, 16, 8, 8>; break;
