@@ -308,16 +308,18 @@ om_status om_graph_check(const char *text, int major, int minor, const char **so
 
 /* No counterpart in the reference.  Advances a cyclic Life grid by
  * `generations` (1..OM_LIFE_NOALLOC_MAX_GENERATIONS) without allocating any
- * memory, for callers that cannot call cudaMalloc (inside a stream capture,
- * under a host framework that owns the device allocator, in a real-time
- * loop).  cells_in / cells_out: distinct device buffers of n0*n1 int32 on the
- * current device, n0 a multiple of 32, every cell 0 or 1 (otherwise
- * OM_ERR_ARG and cells_out is unspecified).  populations: caller memory (host
- * or device) receiving the population after each generation.  stream: a
- * cudaStream_t, or NULL for the default stream; the call returns with it
- * synchronised.  Scratch is a fixed device array shared by all calls: the
- * first call on each device looks up its address (make that first call
- * before any stream capture), and calls that overlap on the GPU race. */
+ * memory, for callers that cannot call cudaMalloc (under a host framework
+ * whose allocator owns all device memory, in a real-time loop that must not
+ * block on the allocator).  cells_in / cells_out: distinct device buffers of
+ * n0*n1 int32 on the current device, n0 a multiple of 32 in [32, 2^20], n1 in
+ * [1, 2^20], n0*n1 at most 2^31 - 1 (the populations are int32), every cell 0
+ * or 1 (otherwise OM_ERR_ARG and cells_out is unspecified).  populations:
+ * caller memory (host or device) receiving the population after each
+ * generation.  stream: a cudaStream_t, or NULL for the default stream; the
+ * call returns with it synchronised.  Scratch is a fixed device array shared
+ * by all calls: the first call on each device looks up its address (make
+ * that first call before any stream capture), and calls that overlap on the
+ * GPU race. */
 om_status om_life_proceed_noalloc(const int32_t *cells_in, int32_t *cells_out, int n0,
                                   int n1, int generations, int32_t *populations,
                                   void *stream);

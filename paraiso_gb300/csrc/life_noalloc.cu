@@ -1,12 +1,14 @@
 // life_noalloc.cu -- a Life entry point that allocates no memory at all.
 //
-// Some callers cannot call cudaMalloc: code running inside a CUDA stream
-// capture that must not add allocation nodes, host frameworks whose device
-// allocator owns all memory and forbids foreign allocations, or real-time
-// loops where an allocation (and its implicit synchronisation) is not
-// allowed.  They own the cell grids; this entry point only needs a few
-// per-generation counters, which live in a file-scope device array instead
-// of memory allocated per call.
+// Some callers cannot call cudaMalloc: host frameworks whose device
+// allocator owns all device memory and forbids allocations by anyone else,
+// and real-time loops that must not block on the allocator (cudaMalloc can
+// wait for the whole device).  They own the cell grids; this entry point
+// only needs a few per-generation counters, which live in a file-scope
+// device array instead of memory allocated per call.
+//
+// The call returns with the caller's stream synchronised: it reads back the
+// cell-value flag and copies the populations before it returns.
 //
 // The array is OM_LIFE_NOALLOC_MAX_GENERATIONS + 1 words: one population
 // counter per generation and a flag raised when a cell is neither 0 nor 1.
@@ -83,6 +85,13 @@ extern "C" om_status om_life_proceed_noalloc(const int32_t *cells_in, int32_t *c
   if (n0 < 32 || n1 < 1 || n0 % 32 != 0 || n0 > (1 << 20) || n1 > (1 << 20)) {
     set_error("om_life_proceed_noalloc: n0 must be a multiple of 32 in [32, 2^20] and "
               "n1 in [1, 2^20]");
+    return OM_ERR_ARG;
+  }
+  // populations are int32: a grid of more than INT32_MAX cells could report a
+  // wrapped count
+  if ((size_t)n0 * (size_t)n1 > (size_t)INT32_MAX) {
+    set_error("om_life_proceed_noalloc: n0 * n1 must be at most 2^31 - 1 cells (the "
+              "populations are int32)");
     return OM_ERR_ARG;
   }
   cudaStream_t s = (cudaStream_t)stream;
