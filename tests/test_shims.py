@@ -10,7 +10,9 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 INC = os.path.join(ROOT, "include")
 LIBDIR = os.path.join(ROOT, "paraiso_gb300")
-REFERENCE_TREE = "/root/reference"
+# the reference tree the oracle recipe reads (PARAISO_REFERENCE, else its default)
+REFERENCE_TREE = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref-path"],
+                                capture_output=True, text=True).stdout.strip()
 
 
 def compile_cpp(src, out, tmp_path):
