@@ -181,6 +181,29 @@ inline double val(Dual a) { return a.v; }
 inline double val(double a) { return a; }
 inline double val(float a) { return a; }
 
+// Operation-counting number: a double that tallies every arithmetic
+// operation the Hydro step performs on it, so the restatement itself gives
+// the scheme's floating-point work per cell-update.  Counters are global;
+// oracle_hydro_count_ops runs the step on one thread.
+enum { kOpAdd, kOpMul, kOpDiv, kOpSqrt, kOpCmp, kOpAbsNeg, kOpKinds };
+static long long g_ops[kOpKinds];
+struct Counted {
+  double v;
+  Counted() : v(0) {}
+  Counted(double x) : v(x) {}
+};
+inline Counted operator+(Counted a, Counted b) { ++g_ops[kOpAdd]; return Counted(a.v + b.v); }
+inline Counted operator-(Counted a, Counted b) { ++g_ops[kOpAdd]; return Counted(a.v - b.v); }
+inline Counted operator-(Counted a) { ++g_ops[kOpAbsNeg]; return Counted(-a.v); }
+inline Counted operator*(Counted a, Counted b) { ++g_ops[kOpMul]; return Counted(a.v * b.v); }
+inline Counted operator/(Counted a, Counted b) { ++g_ops[kOpDiv]; return Counted(a.v / b.v); }
+inline bool operator<(Counted a, Counted b) { ++g_ops[kOpCmp]; return a.v < b.v; }
+inline bool operator<=(Counted a, Counted b) { ++g_ops[kOpCmp]; return a.v <= b.v; }
+inline bool operator>(Counted a, Counted b) { ++g_ops[kOpCmp]; return a.v > b.v; }
+inline Counted dsqrt(Counted a) { ++g_ops[kOpSqrt]; return Counted(std::sqrt(a.v)); }
+inline Counted dabs(Counted a) { ++g_ops[kOpAbsNeg]; return Counted(std::fabs(a.v)); }
+inline double val(Counted a) { return a.v; }
+
 // std::max / std::min as the generated C++ calls them (PlanTrans.hs:692-693)
 template <class R> inline R omax(R a, R b) { return (a < b) ? b : a; }
 template <class R> inline R omin(R a, R b) { return (b < a) ? b : a; }
@@ -662,4 +685,30 @@ extern "C" double oracle_hydro_step_tl_f64(oracle_hydro_shape s, double cfl,
   }
   *time = t.v;
   return dt.v;
+}
+
+/* Floating-point operations of one Hydro step of the n0 x n1 periodic
+ * Kelvin-Helmholtz start (seed), counted on the restatement (one thread):
+ * out = {add/sub, mul, div, sqrt, compare, abs/neg} over the whole step. */
+extern "C" void oracle_hydro_count_ops(int n0, int n1, uint64_t seed, double gamma,
+                                       double cfl, long long *out) {
+  const size_t mem = (size_t)n0 * n1;
+  std::vector<double> r(mem), u(mem), v(mem), p(mem);
+  init_kh<double>(n0, n1, seed, r.data(), u.data(), v.data(), p.data());
+  std::vector<Counted> cr(r.begin(), r.end()), cu(u.begin(), u.end()), cv(v.begin(), v.end()),
+      cp(p.begin(), p.end());
+  oracle_hydro_shape s;
+  s.n0 = n0; s.n1 = n1; s.cyclic = 1; s.gamma = gamma;
+  Counted t(0.0);
+#ifdef _OPENMP
+  const int threads = omp_get_max_threads();
+  omp_set_num_threads(1);
+#endif
+  for (int k = 0; k < kOpKinds; ++k) g_ops[k] = 0;
+  hydro_step<Counted>(s, Counted(cfl), Counted(1.0 / n0), Counted(1.0 / n1), Counted(1.0),
+                      Counted(1.0), &t, cr.data(), cu.data(), cv.data(), cp.data());
+  for (int k = 0; k < kOpKinds; ++k) out[k] = g_ops[k];
+#ifdef _OPENMP
+  omp_set_num_threads(threads);
+#endif
 }

@@ -114,6 +114,13 @@ double oracle_hydro_step_tl_f64(oracle_hydro_shape s, double cfl, double dR0,
                                 double *d_dens, double *d_vx, double *d_vy,
                                 double *d_pres);
 
+/* Floating-point operations of one Hydro step of the n0 x n1 periodic
+ * Kelvin-Helmholtz start, counted on this restatement (each face's flux once,
+ * only the HLLC branch taken): out[6] = {add/sub, mul, div, sqrt, compare,
+ * abs/neg} summed over the step. */
+void oracle_hydro_count_ops(int n0, int n1, uint64_t seed, double gamma, double cfl,
+                            long long *out);
+
 /* Number of OpenMP threads the oracle uses (1 when built without OpenMP). */
 int oracle_num_threads(void);
 

@@ -174,6 +174,17 @@ def hydro_tl_run(state, dstate, steps: int, *, gamma: float, cfl: float, time: f
     return tuple(arrs), tuple(darrs), t.value
 
 
+def hydro_count_ops(n0: int, n1: int, seed: int, *, gamma: float, cfl: float) -> dict:
+    """Operations of one FP step of the periodic Kelvin-Helmholtz start,
+    counted on the restatement, per cell-update."""
+    out = (C.c_longlong * 6)()
+    lib().oracle_hydro_count_ops(n0, n1, C.c_uint64(seed), C.c_double(gamma),
+                                 C.c_double(cfl), out)
+    cells = n0 * n1
+    names = ("add", "mul", "div", "sqrt", "cmp", "absneg")
+    return {k: out[i] / cells for i, k in enumerate(names)}
+
+
 # ---- the reference's own pre-generated classes ----------------------------
 
 def ref_available() -> bool:

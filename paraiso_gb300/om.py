@@ -587,6 +587,12 @@ class Ensemble:
         a = np.ascontiguousarray(values, self.dtype).reshape(n1, n0)
         _check(self._L.om_ensemble_write(self._h, k, field.encode(), a.ctypes.data, a.nbytes))
 
+    def write_from_pointer(self, k: int, field: str, ptr: int, nbytes: int) -> None:
+        _check(self._L.om_ensemble_write(self._h, k, field.encode(), C.c_void_p(ptr), nbytes))
+
+    def read_to_pointer(self, k: int, field: str, ptr: int, nbytes: int) -> None:
+        _check(self._L.om_ensemble_read(self._h, k, field.encode(), C.c_void_p(ptr), nbytes))
+
     def state(self, k: int):
         return tuple(self.read(k, f) for f in self.FIELDS)
 

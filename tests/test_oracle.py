@@ -150,3 +150,25 @@ def test_hydro_oracle_vs_reference_build(oracle):
     out, t, _ = oracle.hydro_run(st, 1, cyclic=False, gamma=5 / 3, cfl=0.3, dtype=np.float32)
     for a, b in zip(ref, out):
         assert np.array_equal(a, b)
+
+
+def test_hydro_flop_count_matches_bench(oracle):
+    """The flops per cell-update bench.py reports for the Hydro step are the
+    ones the restatement performs (HydroMain.hs:134-276, one flux per wall):
+    the same on every size of the periodic Kelvin-Helmholtz start."""
+    import bench
+    for n in (64, 128):
+        ops = oracle.hydro_count_ops(n, n, 1, gamma=1.4, cfl=0.4)
+        for k, v in bench.HYDRO_OPS_PER_CELL.items():
+            # a handful of per-step scalar operations (dt, time) ride on top
+            assert abs(ops[k] - v) * n * n <= 8, (n, k, ops[k], v)
+        assert ops["cmp"] > 0
+    assert bench.HYDRO_FLOPS_PER_CELL == sum(bench.HYDRO_OPS_PER_CELL.values())
+
+
+def test_reference_arm_reports_our_config():
+    """The reference arm times the same configuration our arm names."""
+    import bench
+    assert bench.life_config(16384, 100, 1)["workload"].startswith("life 16384x16384 cyclic")
+    assert bench.life_config(16384, 100, 1) == bench.life_config(16384, 100, 1)
+    assert bench.hydro_config(4096, 1)["n0"] == 4096
