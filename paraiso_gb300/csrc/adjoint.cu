@@ -863,6 +863,7 @@ static om_status launch_tape(Handle *h, AdjointScratch *s, void *const *in, void
   a.n0 = h->size[0]; a.n1 = h->size[1];
   a.nt0 = 0;
   a.gamma = h->cfg.gamma;
+  a.gamma_f = (float)h->cfg.gamma;
   a.sc = s->sc;
   a.read_slot = read_slot;
   a.dt_hist = s->dt_scratch;

@@ -10,7 +10,7 @@
 // (kind, size, precision, device) for the life of the process:
 //   Life  : kernel family (register-resident blocks, warp-specialised,
 //           shared-memory tiles), temporal depth, block rows
-//   Hydro : fused-step tile shape (32x8, 32x16, 64x16)
+//   Hydro : fused-step tile shape (32x8, 32x16, 64x16, 32x32, 64x8)
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -122,8 +122,8 @@ extern "C" om_status om_autotune(int kind, int ndim, const int *sizes, const om_
     }
   } else {
     steps = 8;
-    const int shapes[3][2] = {{0, 8}, {0, 0}, {64, 0}};
-    const int nshapes = (b.precision == 64 || b.variant != 0) ? 1 : 3;
+    const int shapes[5][2] = {{0, 0}, {0, 8}, {64, 0}, {0, 32}, {64, 8}};
+    const int nshapes = (b.precision == 64 || b.variant != 0) ? 1 : 5;
     for (int s = 0; s < nshapes; ++s) {
       om_config c = b;
       c.tile_x = shapes[s][0];
@@ -161,8 +161,8 @@ extern "C" om_status om_autotune_ensemble(int count, const int *sizes, const om_
   }
   om_config b;
   if (base) b = *base; else om_config_default(&b);
-  const int shapes[3][2] = {{0, 8}, {0, 0}, {64, 0}};
-  const int nshapes = (b.precision == 64 || b.variant != 0) ? 1 : 3;
+  const int shapes[5][2] = {{0, 0}, {0, 8}, {64, 0}, {0, 32}, {64, 8}};
+  const int nshapes = (b.precision == 64 || b.variant != 0) ? 1 : 5;
   long long cells = 0;
   for (int k = 0; k < count; ++k) cells += (long long)sizes[2 * k] * sizes[2 * k + 1];
   double best_r = 0;

@@ -83,6 +83,7 @@ static om_status ens_upload_args(om_ensemble E) {
       x.n1 = E->n1[k];
       x.nt0 = (E->n0[k] + E->tx - 1) / E->tx;
       x.gamma = E->gamma;
+      x.gamma_f = (float)E->gamma;
       x.sc = E->d_sc + k;
       x.read_slot = p;
       x.dt_hist = &E->d_sc[k].dt_last;
@@ -148,8 +149,7 @@ om_status om_ensemble_create(int count, const int *sizes, const om_config *cfg,
   E->count = count;
   E->fp64 = c.precision == 64;
   E->exact = c.variant == 2 || E->fp64;
-  E->tile = (!E->exact && c.tile_x == 64) ? kTile64x16
-            : (!E->exact && c.tile_y == 8) ? kTile32x8 : kTile32x16;
+  E->tile = hydro_tile_of(c.tile_x, c.tile_y, !E->exact && !E->fp64);
   hydro_tile_dims(E->tile, &E->tx, &E->ty);
   E->gamma = c.gamma;
   E->device = c.device;
@@ -310,6 +310,7 @@ static om_status ens_tsmin_all(om_ensemble E) {
 
 static om_status ens_run(om_ensemble E, int n, bool use_graph) {
   OM_CUDA_CHECK(cudaSetDevice(E->device));
+  for (int k = 0; k < E->count; ++k) hydro_scalars_refresh(&E->h_sc[k]);
   OM_CUDA_CHECK(cudaMemcpyAsync(E->d_sc, E->h_sc, sizeof(HydroScalars) * E->count,
                                 cudaMemcpyHostToDevice, E->stream));
   OM_TRY(ens_tsmin_all(E));
@@ -359,6 +360,7 @@ om_status om_ensemble_time_step(om_ensemble E, int n, float *ms) {
   if (!E || n < 1 || !ms) { set_error("om_ensemble_time_step: bad arguments"); return OM_ERR_ARG; }
   OM_CUDA_CHECK(cudaSetDevice(E->device));
   // capture (or find) the graph first so the timed region is the replay
+  for (int k = 0; k < E->count; ++k) hydro_scalars_refresh(&E->h_sc[k]);
   OM_CUDA_CHECK(cudaMemcpyAsync(E->d_sc, E->h_sc, sizeof(HydroScalars) * E->count,
                                 cudaMemcpyHostToDevice, E->stream));
   OM_TRY(ens_tsmin_all(E));

@@ -141,6 +141,7 @@ static om_status proceed_fused(Handle *h, int n) {
     a.n0 = h->size[0]; a.n1 = h->size[1];
     a.nt0 = 0;
     a.gamma = h->cfg.gamma;
+    a.gamma_f = (float)h->cfg.gamma;
     a.sc = hsc_dev(h);
     a.read_slot = st->slot;
     a.dt_hist = st->d_dt + k;
@@ -400,7 +401,7 @@ om_status hydro_setup(Handle *h) {
   st->fp64 = h->cfg.precision == 64;
   st->variant = h->cfg.variant;
   st->lm = lm;
-  st->tile = (h->cfg.tile_x == 64) ? kTile64x16 : (h->cfg.tile_y == 8 ? kTile32x8 : kTile32x16);
+  st->tile = hydro_tile_of(h->cfg.tile_x, h->cfg.tile_y, !st->fp64 && st->variant == 0);
   h->impl = st;
   h->impl_free = hydro_free;
   h->ops.state_key = hydro_state_key;
@@ -411,6 +412,7 @@ om_status hydro_setup(Handle *h) {
   h->ops.graph_ok = hydro_graph_ok;
   h->ops.save_state = hydro_save_state;
   h->ops.load_state = hydro_load_state;
+  h->ops.before_upload = [](Handle *hh) { hydro_scalars_refresh(hsc_host(hh)); };
   const int es = st->fp64 ? 8 : 4;
   OM_TRY(alloc_array(h, "density", es));
   OM_TRY(alloc_array(h, "velocity0", es));

@@ -14,6 +14,8 @@ void hydro_tile_dims(int tile, int *tx, int *ty) {
   switch (tile) {
     case kTile32x8: *tx = 32; *ty = 8; break;
     case kTile64x16: *tx = 64; *ty = 16; break;
+    case kTile32x32: *tx = 32; *ty = 32; break;
+    case kTile64x8: *tx = 64; *ty = 8; break;
     default: *tx = 32; *ty = 16; break;
   }
 }

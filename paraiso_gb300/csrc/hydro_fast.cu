@@ -1,6 +1,8 @@
 // hydro_fast.cu -- the production FP32 build of the fused Hydro step:
-// same source as the exact build (hydro_kernels.cuh), compiled with
-// multiply-add contraction, in the tile shapes the tuner chooses from.
+// the tile code of the exact build (hydro_kernels.cuh) with the production
+// algebra (hf:: in hydro_scheme.cuh), compiled with multiply-add
+// contraction and fast single-precision division and square root, in the
+// tile shapes the tuner chooses from.
 #include <cuda_runtime.h>
 
 #include "hydro_launch.cuh"
@@ -15,10 +17,10 @@ static cudaError_t launch_fast(const HydroStepArgs &a0, cudaStream_t s, int *gri
   a.nt0 = (a.n0 + TX - 1) / TX;
   const int nt1 = (a.n1 + TY - 1) / TY;
   const size_t smem = sizeof(FusedSmem<float, TX, TY>);
-  cudaError_t e = cudaFuncSetAttribute(hydro_fused_kernel<float, TX, TY, NT, OPEN>,
+  cudaError_t e = cudaFuncSetAttribute(hydro_fused_kernel<float, TX, TY, NT, OPEN, true>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  hydro_fused_kernel<float, TX, TY, NT, OPEN><<<a.nt0 * nt1, NT, smem, s>>>(a);
+  hydro_fused_kernel<float, TX, TY, NT, OPEN, true><<<a.nt0 * nt1, NT, smem, s>>>(a);
   if (grid_out) *grid_out = a.nt0 * nt1;
   return cudaGetLastError();
 }
@@ -31,19 +33,19 @@ template <int TX, int TY, int NT>
 static cudaError_t launch_ens(const HydroStepArgs *args, const int *prefix, int count, int grid,
                               cudaStream_t s) {
   const size_t smem = sizeof(FusedSmem<float, TX, TY>);
-  cudaError_t e = cudaFuncSetAttribute(hydro_ensemble_kernel<float, TX, TY, NT>,
+  cudaError_t e = cudaFuncSetAttribute(hydro_ensemble_kernel<float, TX, TY, NT, true>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  hydro_ensemble_kernel<float, TX, TY, NT><<<grid, NT, smem, s>>>(args, prefix, count);
+  hydro_ensemble_kernel<float, TX, TY, NT, true><<<grid, NT, smem, s>>>(args, prefix, count);
   return cudaGetLastError();
 }
 
 template <int TX, int TY, int NT> static int occ_fast() {
   const size_t smem = sizeof(FusedSmem<float, TX, TY>);
-  cudaFuncSetAttribute(hydro_ensemble_kernel<float, TX, TY, NT>,
+  cudaFuncSetAttribute(hydro_ensemble_kernel<float, TX, TY, NT, true>,
                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, hydro_ensemble_kernel<float, TX, TY, NT>,
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, hydro_ensemble_kernel<float, TX, TY, NT, true>,
                                                     NT, smem) != cudaSuccess || n < 1) {
     cudaGetLastError();
     n = 1;
@@ -57,6 +59,8 @@ cudaError_t hydro_ensemble_f32(const HydroStepArgs *args, const int *prefix, int
   switch (tile) {
     case kTile32x8: return launch_ens<32, 8, 256>(args, prefix, count, grid, s);
     case kTile64x16: return launch_ens<64, 16, 512>(args, prefix, count, grid, s);
+    case kTile32x32: return launch_ens<32, 32, 512>(args, prefix, count, grid, s);
+    case kTile64x8: return launch_ens<64, 8, 256>(args, prefix, count, grid, s);
     default: return launch_ens<32, 16, 256>(args, prefix, count, grid, s);
   }
 }
@@ -66,6 +70,8 @@ int hydro_ensemble_occupancy(int fp64, int tile, bool exact) {
   switch (tile) {
     case kTile32x8: return occ_fast<32, 8, 256>();
     case kTile64x16: return occ_fast<64, 16, 512>();
+    case kTile32x32: return occ_fast<32, 32, 512>();
+    case kTile64x8: return occ_fast<64, 8, 256>();
     default: return occ_fast<32, 16, 256>();
   }
 }
@@ -81,10 +87,10 @@ cudaError_t hydro_fused_tape(int fp64, bool exact, const HydroStepArgs &a0, cons
   a.nt0 = (a.n0 + TX - 1) / TX;
   const int nt1 = (a.n1 + TY - 1) / TY;
   const size_t smem = sizeof(FusedSmem<float, TX, TY>);
-  cudaError_t e = cudaFuncSetAttribute(hydro_fused_tape_kernel<float, TX, TY, NT>,
+  cudaError_t e = cudaFuncSetAttribute(hydro_fused_tape_kernel<float, TX, TY, NT, true>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  hydro_fused_tape_kernel<float, TX, TY, NT><<<a.nt0 * nt1, NT, smem, s>>>(a, t);
+  hydro_fused_tape_kernel<float, TX, TY, NT, true><<<a.nt0 * nt1, NT, smem, s>>>(a, t);
   return cudaGetLastError();
 }
 
@@ -96,6 +102,8 @@ cudaError_t hydro_fused_f32(const HydroStepArgs &a, int tile, bool exact, cudaSt
   switch (tile) {
     case kTile32x8: return launch_fast<32, 8, 256>(a, s, grid_out);
     case kTile64x16: return launch_fast<64, 16, 512>(a, s, grid_out);
+    case kTile32x32: return launch_fast<32, 32, 512>(a, s, grid_out);
+    case kTile64x8: return launch_fast<64, 8, 256>(a, s, grid_out);
     default: return launch_fast<32, 16, 256>(a, s, grid_out);
   }
 }

@@ -20,7 +20,20 @@ struct HydroScalars {
   // double-buffered by step parity
   unsigned long long tsmin[2];
   double dt_last;
+  // cfl, dR0, dR1 and extent1 rounded to float by the host whenever it
+  // uploads the block (hydro_scalars_refresh), so that FP32 kernels need no
+  // per-thread conversion from double; (float)x is the same rounding either
+  // side
+  float cfl_f, dR0_f, dR1_f, ext1_f;
 };
+
+// the float copies of a scalar block (host side, before every upload)
+inline void hydro_scalars_refresh(HydroScalars *s) {
+  s->cfl_f = (float)s->cfl;
+  s->dR0_f = (float)s->dR0;
+  s->dR1_f = (float)s->dR1;
+  s->ext1_f = (float)s->extent1;
+}
 
 struct HydroStepArgs {
   const void *rho, *v0, *v1, *p;   // current state (memory-sized arrays)
@@ -28,6 +41,7 @@ struct HydroStepArgs {
   int n0, n1;                      // grid (cyclic, no margins)
   int nt0;                         // tiles along x
   double gamma;
+  float gamma_f;                   // (float)gamma
   HydroScalars *sc;
   int read_slot;                   // tsmin slot holding min of the current state
   double *dt_hist;                 // dt of this step is written to dt_hist[0]
@@ -133,10 +147,48 @@ __device__ __forceinline__ void tape_diffs(void *const *d, size_t gi, const hs::
   ((R *)d[7])[gi] = l1.fe - r1.fe;
 }
 
+// Scalars in the OM's Real type: the block's float copies for FP32, the
+// doubles themselves for FP64 (the same values (R)x would give).
+template <class R> struct Reals;
+template <> struct Reals<float> {
+  static __device__ __forceinline__ float cfl(const HydroScalars *s) { return s->cfl_f; }
+  static __device__ __forceinline__ float dR0(const HydroScalars *s) { return s->dR0_f; }
+  static __device__ __forceinline__ float dR1(const HydroScalars *s) { return s->dR1_f; }
+  static __device__ __forceinline__ float ext1(const HydroScalars *s) { return s->ext1_f; }
+  static __device__ __forceinline__ float gamma(const HydroStepArgs &a) { return a.gamma_f; }
+};
+template <> struct Reals<double> {
+  static __device__ __forceinline__ double cfl(const HydroScalars *s) { return s->cfl; }
+  static __device__ __forceinline__ double dR0(const HydroScalars *s) { return s->dR0; }
+  static __device__ __forceinline__ double dR1(const HydroScalars *s) { return s->dR1; }
+  static __device__ __forceinline__ double ext1(const HydroScalars *s) { return s->extent1; }
+  static __device__ __forceinline__ double gamma(const HydroStepArgs &a) { return a.gamma; }
+};
+
 // dt of this step in the OM's Real type: dtG = cfl * reduce Min dts
 template <class R> __device__ __forceinline__ R step_dt(const HydroStepArgs &a) {
   const R tsmin = ts_from_bits<R>(a.sc->tsmin[a.read_slot]);
-  return (R)a.sc->cfl * tsmin;
+  return Reals<R>::cfl(a.sc) * tsmin;
+}
+
+// the scheme's wall flux and update in the exact (generated order) or the
+// production algebra
+template <bool FA, int AX, class R>
+__device__ __forceinline__ hs::Flux<R> wall_flux(R g, const hf::Consts<R> &k,
+                                                 const hs::Prim<R> &L, R cl,
+                                                 const hs::Prim<R> &Rt, R cr) {
+  if (FA) return hf::hllc<AX>(k, L, cl, Rt, cr);
+  return hs::hllc<AX>(g, L, cl, Rt, cr);
+}
+
+template <bool FA, class R>
+__device__ __forceinline__ hs::Prim<R> cell_update(R g, const hf::Consts<R> &k,
+                                                   const hs::Prim<R> &b, R dtdx0, R dtdx1,
+                                                   const hs::Flux<R> &l0, const hs::Flux<R> &r0,
+                                                   const hs::Flux<R> &l1, const hs::Flux<R> &r1,
+                                                   R *cons = nullptr) {
+  if (FA) return hf::update(k, b, dtdx0, dtdx1, l0, r0, l1, r1, cons);
+  return hs::update(g, b, dtdx0, dtdx1, l0, r0, l1, r1, cons);
 }
 
 }  // namespace hk
@@ -186,7 +238,8 @@ template <class R, int TX, int TY> struct FusedSmem {
 // and the margin cells' timescale minimum joins the CFL minimum.
 // TAPE (periodic grids): the tile's stage-1 states and both stages' flux
 // differences are also written to `tape`.
-template <class R, int TX, int TY, int NT, bool OPEN = false, bool TAPE = false>
+// FA: the production algebra (hf::) instead of the generated order (hs::).
+template <class R, int TX, int TY, int NT, bool OPEN = false, bool TAPE = false, bool FA = false>
 __device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
                                            FusedSmem<R, TX, TY> &s, unsigned long long *red,
                                            const HydroTapeOut *tape = nullptr) {
@@ -195,8 +248,9 @@ __device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
   const int t0 = tile % a.nt0, t1 = tile / a.nt0;
   const int X0 = t0 * TX, Y0 = t1 * TY;
   const int n0 = a.n0, n1 = a.n1;
-  const R g = (R)a.gamma;
-  const R dR0 = (R)a.sc->dR0, dR1 = (R)a.sc->dR1;
+  const R g = hk::Reals<R>::gamma(a);
+  const hf::Consts<R> K = hf::consts<R>(g);
+  const R dR0 = hk::Reals<R>::dR0(a.sc), dR1 = hk::Reals<R>::dR1(a.sc);
   const R dtG = hk::step_dt<R>(a);
   const R dtHalf = dtG / R(2);
   const R *rho = (const R *)a.rho, *vx = (const R *)a.v0, *vy = (const R *)a.v1,
@@ -211,7 +265,7 @@ __device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
     if (OPEN) {
       const int ix = X0 + px - 3, iy = Y0 + py - 3;
       if (ix < 0 || iy < 0 || ix >= n0 || iy >= n1) {
-        const hs::Prim<R> j = hk::jet_state<R>(g, dR0, dR1, (R)a.sc->extent1, ix, iy);
+        const hs::Prim<R> j = hk::jet_state<R>(g, dR0, dR1, hk::Reals<R>::ext1(a.sc), ix, iy);
         r = j.rho; u = j.v0; v = j.v1; q = j.p;
       } else {
         const size_t gi = (size_t)(iy + a.lm) * a.ms0 + (ix + a.lm);
@@ -241,7 +295,7 @@ __device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
         const hs::Prim<R> L{s.P[0][py][fx], s.P[1][py][fx], s.P[2][py][fx], s.P[3][py][fx]};
         const hs::Prim<R> Rt{s.P[0][py][fx + 1], s.P[1][py][fx + 1], s.P[2][py][fx + 1],
                              s.P[3][py][fx + 1]};
-        s.fx[i] = hs::hllc<0>(g, L, s.C[py][fx], Rt, s.C[py][fx + 1]);
+        s.fx[i] = hk::wall_flux<FA, 0>(g, K, L, s.C[py][fx], Rt, s.C[py][fx + 1]);
       } else {
         const int j = i - NX;
         const int fy = j / S::FYX, fx = j - fy * S::FYX;
@@ -249,7 +303,7 @@ __device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
         const hs::Prim<R> L{s.P[0][fy][px], s.P[1][fy][px], s.P[2][fy][px], s.P[3][fy][px]};
         const hs::Prim<R> Rt{s.P[0][fy + 1][px], s.P[1][fy + 1][px], s.P[2][fy + 1][px],
                              s.P[3][fy + 1][px]};
-        s.fy[j] = hs::hllc<1>(g, L, s.C[fy][px], Rt, s.C[fy + 1][px]);
+        s.fy[j] = hk::wall_flux<FA, 1>(g, K, L, s.C[fy][px], Rt, s.C[fy + 1][px]);
       }
     }
   }
@@ -262,9 +316,9 @@ __device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
       const int qy = i / S::QX, qx = i - qy * S::QX;
       const int py = qy + 1, px = qx + 1;
       const hs::Prim<R> b{s.P[0][py][px], s.P[1][py][px], s.P[2][py][px], s.P[3][py][px]};
-      const hs::Prim<R> q = hs::update(g, b, dtdx0, dtdx1, s.fx[qy * S::FXX + qx],
-                                       s.fx[qy * S::FXX + qx + 1], s.fy[qy * S::FYX + qx],
-                                       s.fy[(qy + 1) * S::FYX + qx]);
+      const hs::Prim<R> q = hk::cell_update<FA>(g, K, b, dtdx0, dtdx1, s.fx[qy * S::FXX + qx],
+                                                s.fx[qy * S::FXX + qx + 1], s.fy[qy * S::FYX + qx],
+                                                s.fy[(qy + 1) * S::FYX + qx]);
       s.Q[0][qy][qx] = q.rho;
       s.Q[1][qy][qx] = q.v0;
       s.Q[2][qy][qx] = q.v1;
@@ -301,7 +355,8 @@ __device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
           (&L.rho)[f] = l;
           (&Rt.rho)[f] = r;
         }
-        s.fx[i] = hs::hllc<0>(g, L, hs::sound(g, L.rho, L.p), Rt, hs::sound(g, Rt.rho, Rt.p));
+        s.fx[i] = hk::wall_flux<FA, 0>(g, K, L, hs::sound(g, L.rho, L.p), Rt,
+                                       hs::sound(g, Rt.rho, Rt.p));
       } else {
         const int j = i - NX;
         const int sy = j / TX, sx = j - sy * TX;
@@ -314,7 +369,8 @@ __device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
           (&L.rho)[f] = l;
           (&Rt.rho)[f] = r;
         }
-        s.fy[j] = hs::hllc<1>(g, L, hs::sound(g, L.rho, L.p), Rt, hs::sound(g, Rt.rho, Rt.p));
+        s.fy[j] = hk::wall_flux<FA, 1>(g, K, L, hs::sound(g, L.rho, L.p), Rt,
+                                       hs::sound(g, Rt.rho, Rt.p));
       }
     }
   }
@@ -332,9 +388,9 @@ __device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
       const int py = oy + 3, px = ox + 3;
       const hs::Prim<R> b{s.P[0][py][px], s.P[1][py][px], s.P[2][py][px], s.P[3][py][px]};
       R cons[4];
-      const hs::Prim<R> q =
-          hs::update(g, b, dtdx0, dtdx1, s.fx[oy * (TX + 1) + ox], s.fx[oy * (TX + 1) + ox + 1],
-                     s.fy[oy * TX + ox], s.fy[(oy + 1) * TX + ox], TAPE ? cons : nullptr);
+      const hs::Prim<R> q = hk::cell_update<FA>(
+          g, K, b, dtdx0, dtdx1, s.fx[oy * (TX + 1) + ox], s.fx[oy * (TX + 1) + ox + 1],
+          s.fy[oy * TX + ox], s.fy[(oy + 1) * TX + ox], TAPE ? cons : nullptr);
       const size_t gi = OPEN ? (size_t)(gy + a.lm) * a.ms0 + (gx + a.lm) : (size_t)gy * n0 + gx;
       if (TAPE) {
         hk::tape_diffs<R>(tape->d2, gi, s.fx[oy * (TX + 1) + ox], s.fx[oy * (TX + 1) + ox + 1],
@@ -380,22 +436,22 @@ __device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
   }
 }
 
-template <class R, int TX, int TY, int NT, bool OPEN = false>
+template <class R, int TX, int TY, int NT, bool OPEN = false, bool FA = false>
 __global__ void __launch_bounds__(NT)
 hydro_fused_kernel(HydroStepArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned long long red[32];
-  fused_tile<R, TX, TY, NT, OPEN>(a, blockIdx.x,
-                                  *reinterpret_cast<FusedSmem<R, TX, TY> *>(smem_raw), red);
+  fused_tile<R, TX, TY, NT, OPEN, false, FA>(
+      a, blockIdx.x, *reinterpret_cast<FusedSmem<R, TX, TY> *>(smem_raw), red);
 }
 
 // the fused step that also writes the tape of the reverse sweep (periodic)
-template <class R, int TX, int TY, int NT>
+template <class R, int TX, int TY, int NT, bool FA = false>
 __global__ void __launch_bounds__(NT)
 hydro_fused_tape_kernel(HydroStepArgs a, const __grid_constant__ HydroTapeOut t) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned long long red[32];
-  fused_tile<R, TX, TY, NT, false, true>(
+  fused_tile<R, TX, TY, NT, false, true, FA>(
       a, blockIdx.x, *reinterpret_cast<FusedSmem<R, TX, TY> *>(smem_raw), red, &t);
 }
 
@@ -452,7 +508,7 @@ hydro_tsmin_open_kernel(const R *__restrict__ rho, const R *__restrict__ v0,
 // persistent grid strides over the flattened item list (prefix[k] = first
 // item of instance k), so instances of any size advance in one launch, each
 // with its own dt, CFL minimum and time (its HydroStepArgs).
-template <class R, int TX, int TY, int NT>
+template <class R, int TX, int TY, int NT, bool FA = false>
 __global__ void __launch_bounds__(NT)
 hydro_ensemble_kernel(const HydroStepArgs *__restrict__ args, const int *__restrict__ prefix,
                       int count) {
@@ -467,7 +523,7 @@ hydro_ensemble_kernel(const HydroStepArgs *__restrict__ args, const int *__restr
       if (prefix[mid] <= item) lo = mid;
       else hi = mid - 1;
     }
-    fused_tile<R, TX, TY, NT>(args[lo], item - prefix[lo], s, red);
+    fused_tile<R, TX, TY, NT, false, false, FA>(args[lo], item - prefix[lo], s, red);
     __syncthreads();
   }
 }

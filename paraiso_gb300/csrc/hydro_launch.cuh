@@ -10,9 +10,22 @@
 
 namespace om {
 
-// Tile shapes of the fused kernel available to the tuner.
-enum HydroTile { kTile32x8 = 0, kTile32x16 = 1, kTile64x16 = 2, kTileCount = 3 };
+// Tile shapes of the fused kernel available to the tuner (FP32 production
+// build; FP64 and the exact FP32 variant run 32x16).
+enum HydroTile {
+  kTile32x8 = 0, kTile32x16 = 1, kTile64x16 = 2, kTile32x32 = 3, kTile64x8 = 4, kTileCount = 5
+};
 void hydro_tile_dims(int tile, int *tx, int *ty);
+// the tile a configuration's tile_x / tile_y select (0 = default): x 64
+// with y 8 is 64x8, else 64x16; x 0 or 32 with y 8, 32 or other is 32x8,
+// 32x32 or 32x16
+inline int hydro_tile_of(int tile_x, int tile_y, bool production) {
+  if (!production) return kTile32x16;
+  if (tile_x == 64) return tile_y == 8 ? kTile64x8 : kTile64x16;
+  if (tile_y == 8) return kTile32x8;
+  if (tile_y == 32) return kTile32x32;
+  return kTile32x16;
+}
 
 // fused two-stage step; `exact` selects the no-contraction build
 cudaError_t hydro_fused_f32(const HydroStepArgs &a, int tile, bool exact, cudaStream_t s,

@@ -129,6 +129,7 @@ om_status bring_host(Handle *h, Array &a) {
 
 om_status upload_scalars(Handle *h) {
   if (!h->scalar_bytes) return OM_OK;
+  if (h->ops.before_upload) h->ops.before_upload(h);
   OM_CUDA_CHECK(cudaMemcpyAsync(h->d_scalars, h->h_scalars, h->scalar_bytes,
                                 cudaMemcpyHostToDevice, h->stream));
   return OM_OK;

@@ -78,6 +78,9 @@ struct KindOps {
   om_status (*reserve)(Handle *, int kernel_id, int n) = nullptr;
   // false when a kernel synchronises with the host mid-run (no graph capture)
   bool (*graph_ok)(Handle *, int kernel_id) = nullptr;
+  // derive host-side scalar fields from the user-visible ones right before
+  // the scalar block is uploaded
+  void (*before_upload)(Handle *) = nullptr;
   // host-side state a checkpoint carries besides the statics (bytes written
   // into out, at most cap; returns the size), and its restoration
   size_t (*save_state)(Handle *, void *out, size_t cap) = nullptr;
