@@ -177,7 +177,7 @@ def life_workload(args, dist: Dist) -> dict:
     gens = args.generations or (1000 if args.workload == "life128" else 100)
     cells = n * n
     life = pg.Life((n, n), device=dist.local_rank, depth=args.depth, tile_x=args.tile_x,
-                   tile_y=args.tile_y, life_io=args.life_io)
+                   tile_y=args.tile_y, life_io=args.life_io, life_kernel=args.life_kernel)
     life.fill_random(1 + dist.rank, 0.3)
     # warm-up
     for _ in range(args.warmup):
@@ -199,7 +199,8 @@ def life_workload(args, dist: Dist) -> dict:
     life.profile(True)
     life.time_run("proceed", gens * min(args.steps, 4))
     best = None
-    for kn in ("life_reg_kernel", "life_ws_kernel", "life_tb32_kernel", "life_tb_kernel",
+    for kn in ("life_reg_kernel", "life_ws_kernel", "life_ws_tma_kernel", "life_tb32_kernel",
+               "life_tb_kernel",
                "life_smallreg_kernel", "life_smallgrid_kernel", "life_general_kernel"):
         q = life.profile_query(kn)
         if q[0] and (best is None or q[1] > best[1][1]):
@@ -968,7 +969,7 @@ def life_self_check(pg, n: int, gens: int, dist: Dist, args, oracle_sample) -> d
     import numpy as np
     t0 = time.perf_counter()
     life = pg.Life((n, n), device=dist.local_rank, depth=args.depth, tile_x=args.tile_x,
-                   tile_y=args.tile_y, life_io=args.life_io)
+                   tile_y=args.tile_y, life_io=args.life_io, life_kernel=args.life_kernel)
     life.fill_random(1 + dist.rank, 0.3)
     init = life.read("cell")
     use_oracle = oracle_sample is not None and oracle_sample[0] <= gens
@@ -1109,7 +1110,7 @@ def run_configs(args, dist: Dist) -> dict:
     is reported in its place and does not stop the others."""
     runs = {
         "life128": (life_workload, dict(workload="life128", size=0, generations=0,
-                                        depth=0, tile_x=0, tile_y=0)),
+                                        depth=0, tile_x=0, tile_y=0, life_kernel=0)),
         "hydro4k": (hydro_workload, dict(workload="hydro4k", size=0, steps=1000,
                                          accuracy_steps=1000, tile_x=0, tile_y=0)),
         "ensemble": (ensemble_workload, dict(workload="ensemble", size=0, steps=200,
@@ -1159,6 +1160,8 @@ def main() -> int:
     ap.add_argument("--tile-x", type=int, default=0)
     ap.add_argument("--tile-y", type=int, default=0)
     ap.add_argument("--life-io", type=int, default=0, help="0: 128-bit cell I/O, 1: 32-bit")
+    ap.add_argument("--life-kernel", type=int, default=0,
+                    help="Life packed kernel (om_config.life_kernel; 0 = automatic)")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-self-check", action="store_true")

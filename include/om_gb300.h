@@ -67,10 +67,14 @@ typedef struct {
                        Hydro 1: plain unfused FP64-structured grid-stride kernels */
   int life_io;      /* Life cell I/O of the packed kernels: 0 = 128-bit, 1 = 32-bit */
   int life_kernel;  /* Life packed kernel: k >= 1 = warp-specialised persistent
-                       kernel, variant k-1; 0 = automatic: with tile_y 0, that
-                       kernel's variant 3 on grids of at least 1.5 of its tiles
-                       per SM, else register-resident blocks */
-  int reserved[5];
+                       kernel, variant k-1 (variants 4-10 and 13 take their rows by
+                       TMA and need rows of at least 1024 cells); 0 = automatic:
+                       with tile_y 0, that kernel on grids of at least 1.5 of its
+                       tiles per SM, else register-resident blocks */
+  int grid_limit;   /* persistent kernels (Life warp-specialised, Hydro ensemble):
+                       at most this many CTAs (0 = as many as the GPU keeps
+                       resident) */
+  int reserved[4];
 } om_config;
 
 /* Fill `cfg` with defaults: cyclic, FP32, gamma 5/3, device 0, tuned tiles. */

@@ -103,7 +103,7 @@ extern "C" om_status om_autotune(int kind, int ndim, const int *sizes, const om_
           c.life_kernel = 0;
           cands.push_back(c);
         }
-      for (int k = 1; k <= 4; ++k) {
+      for (int k = 1; k <= (sizes[0] >= 1024 ? 14 : 4); ++k) {
         om_config c = b;
         c.depth = 32;
         c.tile_x = 0;

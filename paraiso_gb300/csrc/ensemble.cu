@@ -225,6 +225,7 @@ om_status om_ensemble_create(int count, const int *sizes, const om_config *cfg,
   }
   const int occ = hydro_ensemble_occupancy(E->fp64, E->tile, E->exact);
   E->grid = std::max(1, std::min(occ * sm_count(E->device), E->prefix[count]));
+  if (c.grid_limit > 0) E->grid = std::min(E->grid, c.grid_limit);
   st = ens_upload_args(E);
   if (st != OM_OK) {
     om_ensemble_destroy(E);

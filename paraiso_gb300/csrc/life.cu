@@ -29,12 +29,14 @@
 #include <string>
 
 #include "om_internal.cuh"
+#include "tma.cuh"
 
 namespace om {
 
 struct LifeScalars {  // device/host scalar block
   int32_t population;
   int32_t generation;
+  uint32_t wait_error;  // raised by a kernel whose bounded wait ran out
 };
 
 struct LifeState {
@@ -44,7 +46,35 @@ struct LifeState {
   int pop_cap = 0;
   int last_n = 0;
   int depth = 0, tile_w = 0, tile_h = 0;  // tuned or configured
+  // tensor maps of the two cell buffers (cells x words x rows) for the TMA
+  // kernels, keyed by buffer address, and their one-word maps (32 cells x 1
+  // word x 1 row, no swizzle) for the halo word that wraps around;
+  // tmap_ok[i] false when encoding failed
+  CUtensorMap tmap[2], tpatch[2];
+  const void *tmap_ptr[2] = {nullptr, nullptr};
+  bool tmap_ok[2] = {false, false};
 };
+
+// Index of the cached maps of cell buffer `cells` (n0 x n1 int32, n0 a
+// multiple of 32), -1 when the driver does not encode them: dimensions 32
+// cells x n0/32 words x n1 rows, boxes of one row of 32 words with 128-byte
+// swizzle (st->tmap[i]) and of one word (st->tpatch[i]).
+static int life_tmap(LifeState *st, const void *cells, int n0, int n1) {
+  for (int i = 0; i < 2; ++i)
+    if (st->tmap_ptr[i] == cells) return st->tmap_ok[i] ? i : -1;
+  const int i = st->tmap_ptr[0] == nullptr ? 0 : (st->tmap_ptr[1] == nullptr ? 1 : 0);
+  const uint64_t dims[3] = {32, (uint64_t)(n0 / 32), (uint64_t)n1};
+  const uint64_t strides[2] = {128, (uint64_t)n0 * 4};
+  const uint32_t box[3] = {32, 32, 1}, box1[3] = {32, 1, 1};
+  st->tmap_ptr[i] = cells;
+  st->tmap_ok[i] = tma::encode_tiled(&st->tmap[i], CU_TENSOR_MAP_DATA_TYPE_INT32, 3,
+                                     const_cast<void *>(cells), dims, strides, box,
+                                     CU_TENSOR_MAP_SWIZZLE_128B) &&
+                   tma::encode_tiled(&st->tpatch[i], CU_TENSOR_MAP_DATA_TYPE_INT32, 3,
+                                     const_cast<void *>(cells), dims, strides, box1,
+                                     CU_TENSOR_MAP_SWIZZLE_NONE);
+  return st->tmap_ok[i] ? i : -1;
+}
 
 static LifeState *life_state(Handle *h) { return (LifeState *)h->impl; }
 
@@ -774,21 +804,40 @@ __host__ __device__ constexpr bool kStagedPack() {
   return 3 * 4 * 32 * R * NWC + 8192 * NWP <= 212992;
 }
 
-template <int R, int NWC, int NWP, int NWS>
+// TMA (the tile's rows arrive by tensor copies): producer warps pack from
+// 4 KB row boxes (32 cells x 32 words x 1 row of the grid viewed as cells x
+// words x rows, 128-byte swizzle) that land in NS slots per warp, complete
+// on an mbarrier per slot and are issued NS - 1 boxes ahead of the row being
+// packed.  Each lane packs one whole word from
+// eight 16-byte chunks of its 128-byte line (the swizzle puts chunk j of
+// line L at j ^ (L mod 8), so the warp's loads hit every bank once).  The box reads
+// zeros outside the grid; in the first and last tile columns the one halo
+// word that wraps around (word n0/32 - 1 left of word 0, word 0 right of
+// the last word) comes in as a second, one-word box (`tpatch`, no swizzle)
+// on the same mbarrier.  Words further out stay zero: with at most 32
+// generations per launch their error front never reaches an owned word.
+// Waits are bounded (tma::mbar_wait raises *err).
+template <int R, int NWC, int NWP, int NWS, bool TMA = false, int NS = 2>
 __global__ void __launch_bounds__((NWC + NWP + NWS) * 32, 1)
 life_ws_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbParams p,
-               uint32_t *__restrict__ pop) {
+               uint32_t *__restrict__ pop, const __grid_constant__ CUtensorMap tmap,
+               const __grid_constant__ CUtensorMap tpatch, uint32_t *err) {
   constexpr int NC = 32, NR = R * NWC;
-  extern __shared__ uint32_t buf[];  // 3 x NR x NC packed words
+  extern __shared__ __align__(1024) uint32_t buf[];  // 3 x NR x NC packed words
   __shared__ uint32_t ex[2][NWC][2][NC];
   __shared__ uint32_t spop[32];
   __shared__ int4 nib[16];  // nibble -> its four cells
+  __shared__ uint64_t bars[NWP][NS];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid < 16) nib[tid] = make_int4(tid & 1, (tid >> 1) & 1, (tid >> 2) & 1, (tid >> 3) & 1);
   const int kk = p.kk;
   const int ntiles = p.nt0 * p.nt1;
   const int m = ntiles > (int)blockIdx.x ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
   if (tid < 32) spop[tid] = 0;
+  if (TMA && tid < NS * NWP) {
+    tma::mbar_init(&bars[tid / NS][tid % NS], 1);
+    tma::fence_mbar_init();
+  }
   __syncthreads();
   constexpr int NWT = NWC + NWP + NWS;
   // write back the owned words of tile t from shared-memory buffer A, by
@@ -815,6 +864,64 @@ life_ws_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbPa
     const int col0 = (t % p.nt0) * p.tw, row0 = (t / p.nt0) * p.th;
     pack_rows32(cur, p.n0, p.n1, p.wd, row0 - kk, col0 - 1, NR, buf + (s % 3) * NR * NC, pw,
                 npw, lane);
+  };
+  // TMA slots: after the three tile buffers, 1024-byte aligned (the
+  // swizzle's period), NS 4 KB slots per producer warp, then NS 128-byte
+  // slots per producer warp for the wrapped halo word
+  unsigned char *slots = nullptr, *patches = nullptr;
+  if (TMA) {
+    unsigned char *after = reinterpret_cast<unsigned char *>(buf + 3 * NR * NC);
+    slots = after + ((1024u - (tma::smem_addr(after) & 1023u)) & 1023u);
+    patches = slots + (size_t)NWP * NS * 4096;
+  }
+  // rows this producer warp has packed so far; its rows run pw, pw + NWP,
+  // ... of tile 1, then of tile 2, ..., and box q of that sequence goes
+  // into slot q mod NS
+  uint32_t seq = 0;
+  // lane whose word wraps around in tile column col0 (-1: none): lane 0
+  // holds word -1 in the first column, lane wd - col0 + 1 word wd in the last
+  auto wrap_lane = [&](int col0) {
+    if (col0 == 0) return 0;
+    const int sr = p.wd - col0 + 1;
+    return sr <= 31 ? sr : -1;
+  };
+  auto row_issue = [&](int s, int r, uint32_t q) {
+    const int t = blockIdx.x + s * gridDim.x;
+    const int col0 = (t % p.nt0) * p.tw, row0 = (t / p.nt0) * p.th;
+    int gy = (row0 - kk + r) % p.n1;
+    if (gy < 0) gy += p.n1;
+    if (lane == 0) {
+      const int pw = warp - NWC;
+      const int slot = pw * NS + (int)(q % NS);
+      uint64_t *bar = &bars[pw][q % NS];
+      const int wl = wrap_lane(col0);
+      tma::mbar_arrive_expect_tx(bar, wl >= 0 ? 4096 + 128 : 4096);
+      tma::load_3d(slots + (size_t)slot * 4096, &tmap, 0, col0 - 1, gy, bar);
+      if (wl >= 0)
+        tma::load_3d(patches + (size_t)slot * 128, &tpatch, 0, wl == 0 ? p.wd - 1 : 0, gy, bar);
+    }
+  };
+  auto row_pack = [&](int s, int r, uint32_t q) {
+    const int t = blockIdx.x + s * gridDim.x;
+    const int col0 = (t % p.nt0) * p.tw;
+    const int pw = warp - NWC;
+    const int slot = pw * NS + (int)(q % NS);
+    tma::mbar_wait(&bars[pw][q % NS], (q / NS) & 1, err);
+    const bool patched = lane == wrap_lane(col0);
+    const unsigned char *line =
+        patched ? patches + (size_t)slot * 128 : slots + (size_t)slot * 4096 + lane * 128;
+    const int x7 = patched ? 0 : (lane & 7);
+    uint32_t w = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int4 c = *reinterpret_cast<const int4 *>(line + ((j ^ x7) << 4));
+      w += ((uint32_t)c.x << (4 * j)) + ((uint32_t)c.y << (4 * j + 1)) +
+           ((uint32_t)c.z << (4 * j + 2)) + ((uint32_t)c.w << (4 * j + 3));
+    }
+    buf[(s % 3) * NR * NC + r * NC + lane] = w;
+    // the slot's reads are done before the next box into it is issued
+    tma::fence_proxy_async();
+    __syncwarp();
   };
   // the producers' staging rows follow the three tile buffers
   int4 *stage = reinterpret_cast<int4 *>(buf + 3 * NR * NC);
@@ -896,7 +1003,38 @@ life_ws_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbPa
       }
     } else if (warp < NWC + NWP) {
       if (s < m)
-        if (kStagedPack<R, NWC, NWP>())
+        if (TMA) {
+          // rows pw, pw + NWP, ... of tile s, NS - 1 boxes ahead (the first
+          // rows of tile s + 1 follow the last of tile s); a slot is issued
+          // into only after the row it held was packed
+          const int pw = warp - NWC;
+          if (s == 1) {  // the sequence's first NS - 1 boxes
+            int nr = pw, ns = 1;
+            for (int k = 0; k < NS - 1 && ns < m; ++k) {
+              row_issue(ns, nr, (uint32_t)k);
+              nr += NWP;
+              if (nr >= NR) {
+                nr = pw;
+                ++ns;
+              }
+            }
+          }
+          for (int r = pw; r < NR; r += NWP) {
+            // the row NS - 1 places further on in the sequence
+            int nr = r, ns = s;
+#pragma unroll
+            for (int k = 0; k < NS - 1; ++k) {
+              nr += NWP;
+              if (nr >= NR) {
+                nr = pw;
+                ++ns;
+              }
+            }
+            if (ns < m) row_issue(ns, nr, seq + NS - 1);
+            row_pack(s, r, seq);
+            ++seq;
+          }
+        } else if (kStagedPack<R, NWC, NWP>())
           pack_tile_async(s, warp - NWC);
         else
           pack_tile(s, warp - NWC, NWP);
@@ -996,33 +1134,61 @@ static cudaError_t launch_reg(int v, const int32_t *cur, int32_t *next, const Tb
 // NWS store warps, one CTA per SM
 struct WsVariant {
   int R, NWC, NWP, NWS;
+  bool tma;  // producers take their rows by TMA
+  int ns;    // TMA slots per producer warp
 };
-static const WsVariant kWsVariants[] = {{24, 16, 8, 8}, {16, 16, 8, 8}, {24, 16, 12, 4},
-                                        {20, 16, 8, 8}};
-static const int kNumWsVariants = 4;
-// the variant the automatic choice takes (fastest on GB300 at 8192^2 and
-// 16384^2), and the tiles per SM a grid needs for it
+static const WsVariant kWsVariants[] = {
+    {24, 16, 8, 8, false, 0}, {16, 16, 8, 8, false, 0}, {24, 16, 12, 4, false, 0},
+    {20, 16, 8, 8, false, 0}, {20, 16, 8, 8, true, 2},  {24, 16, 8, 8, true, 2},
+    {20, 16, 4, 12, true, 4}, {20, 16, 6, 10, true, 3}, {24, 16, 4, 12, true, 4},
+    {21, 16, 8, 8, true, 2},  {22, 16, 8, 8, true, 2},  {21, 16, 8, 8, false, 0},
+    {22, 16, 8, 8, false, 0}, {23, 16, 8, 8, true, 2}};
+static const int kNumWsVariants = 14;
+// the variant the automatic choice takes when TMA serves the grid (rows of
+// at least 32 words; fastest on GB300 at 16384^2: 22 rows per consumer warp
+// give 990 tiles, at most 7 per SM, where 20 rows give 1098, at most 8),
+// else the staged-copy one
+static const int kAutoWsVariantTma = 10;
 static const int kAutoWsVariant = 3;
 
+// `tmap`, `tpatch`: the tensor maps of `cur` for the TMA variants (ignored
+// by the others); at most `ctas` persistent CTAs
 static cudaError_t launch_ws(int v, const int32_t *cur, int32_t *next, const TbParams &p,
-                             uint32_t *pop, int sms, cudaStream_t s) {
+                             uint32_t *pop, int ctas, const CUtensorMap &tmap,
+                             const CUtensorMap &tpatch, uint32_t *err, cudaStream_t s) {
   const WsVariant wv = kWsVariants[v];
-  // three tile buffers, then two staged rows (2 x 4 KB) per producer warp
-  const bool staged = 3 * 4 * 32 * wv.R * wv.NWC + 8192 * wv.NWP <= 212992;
-  const size_t smem =
-      sizeof(uint32_t) * 3 * 32 * wv.R * wv.NWC + (staged ? sizeof(int4) * 512 * wv.NWP : 0);
-  void (*k)(const int32_t *, int32_t *, TbParams, uint32_t *) = nullptr;
+  size_t smem = sizeof(uint32_t) * 3 * 32 * wv.R * wv.NWC;
+  if (wv.tma) {
+    // three tile buffers, alignment slack, ns 4 KB TMA slots and ns
+    // 128-byte wrapped-word slots per producer warp
+    smem += 1024 + (size_t)(4096 + 128) * wv.ns * wv.NWP;
+  } else if (3 * 4 * 32 * wv.R * wv.NWC + 8192 * wv.NWP <= 212992) {
+    // three tile buffers, then two staged rows (2 x 4 KB) per producer warp
+    smem += sizeof(int4) * 512 * wv.NWP;
+  }
+  void (*k)(const int32_t *, int32_t *, TbParams, uint32_t *, const CUtensorMap,
+            const CUtensorMap, uint32_t *) = nullptr;
   switch (v) {
     case 0: k = life_ws_kernel<24, 16, 8, 8>; break;
     case 1: k = life_ws_kernel<16, 16, 8, 8>; break;
     case 2: k = life_ws_kernel<24, 16, 12, 4>; break;
-    default: k = life_ws_kernel<20, 16, 8, 8>; break;
+    case 3: k = life_ws_kernel<20, 16, 8, 8>; break;
+    case 4: k = life_ws_kernel<20, 16, 8, 8, true, 2>; break;
+    case 5: k = life_ws_kernel<24, 16, 8, 8, true, 2>; break;
+    case 6: k = life_ws_kernel<20, 16, 4, 12, true, 4>; break;
+    case 7: k = life_ws_kernel<20, 16, 6, 10, true, 3>; break;
+    case 8: k = life_ws_kernel<24, 16, 4, 12, true, 4>; break;
+    case 9: k = life_ws_kernel<21, 16, 8, 8, true, 2>; break;
+    case 10: k = life_ws_kernel<22, 16, 8, 8, true, 2>; break;
+    case 11: k = life_ws_kernel<21, 16, 8, 8>; break;
+    case 12: k = life_ws_kernel<22, 16, 8, 8>; break;
+    default: k = life_ws_kernel<23, 16, 8, 8, true, 2>; break;
   }
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const int ntiles = p.nt0 * p.nt1;
-  const int grid = ntiles < sms ? ntiles : sms;
-  k<<<grid, (wv.NWC + wv.NWP + wv.NWS) * 32, smem, s>>>(cur, next, p, pop);
+  const int grid = ntiles < ctas ? ntiles : ctas;
+  k<<<grid, (wv.NWC + wv.NWP + wv.NWS) * 32, smem, s>>>(cur, next, p, pop, tmap, tpatch, err);
   return cudaGetLastError();
 }
 
@@ -1212,11 +1378,21 @@ static om_status life_proceed(Handle *h, int n) {
       // where it overlaps one tile's loads and stores with another's
       // generations, and the register-resident blocks on smaller grids
       int ws = h->cfg.life_kernel;
+      // TMA rows need a grid at least one box (32 words) wide whose buffers
+      // the driver describes
+      const bool tma_ok = wd >= 32 && life_tmap(st, a.d(), n0, n1) >= 0 &&
+                          life_tmap(st, a.d_next(), n0, n1) >= 0;
       if (reg && ws == 0 && st->tile_h == 0) {
-        const WsVariant wv = kWsVariants[kAutoWsVariant];
+        const int av = tma_ok ? kAutoWsVariantTma : kAutoWsVariant;
+        const WsVariant wv = kWsVariants[av];
         const int th = std::min(wv.R * wv.NWC - 2 * kmax, n1);
         const long long tiles = (long long)((wd + 29) / 30) * ((n1 + th - 1) / th);
-        if (th > 0 && 2 * tiles >= 3LL * sm_count(h->device)) ws = kAutoWsVariant + 1;
+        if (th > 0 && 2 * tiles >= 3LL * sm_count(h->device)) ws = av + 1;
+      }
+      if (ws >= 1 && kWsVariants[std::min(ws - 1, kNumWsVariants - 1)].tma && !tma_ok) {
+        set_error("Life: the TMA kernel variants need rows of at least 1024 cells and a "
+                  "tensor map of the grid");
+        return OM_ERR_UNSUPPORTED;
       }
       for (int l = 0; l < nl; ++l) {
         const int kk = rem / nl + (l < rem % nl ? 1 : 0);
@@ -1231,13 +1407,20 @@ static om_status life_proceed(Handle *h, int n) {
           q.nt0 = (wd + q.tw - 1) / q.tw;
           q.nt1 = (n1 + q.th - 1) / q.th;
           cudaEvent_t ev = prof_begin(h);
+          const int mi = wv.tma ? life_tmap(st, a.d(), n0, n1) : -1;
+          const int ctas = h->cfg.grid_limit > 0
+                               ? std::min(h->cfg.grid_limit, sm_count(h->device))
+                               : sm_count(h->device);
           cudaError_t e = launch_ws(v, (const int32_t *)a.d(), (int32_t *)a.d_next(), q,
-                                    st->d_pop + g, sm_count(h->device), h->stream);
+                                    st->d_pop + g, ctas, st->tmap[mi < 0 ? 0 : mi],
+                                    st->tpatch[mi < 0 ? 0 : mi],
+                                    &((LifeScalars *)h->d_scalars)->wait_error, h->stream);
           if (e != cudaSuccess) {
             set_error(std::string("life_ws_kernel: ") + cudaGetErrorString(e));
             return OM_ERR_CUDA;
           }
-          prof_end(h, ev, "life_ws_kernel", (double)n0 * n1 * kk);
+          prof_end(h, ev, wv.tma ? "life_ws_tma_kernel" : "life_ws_kernel",
+                   (double)n0 * n1 * kk);
           h->launches++;
           a.swap();
           g += kk;
@@ -1407,6 +1590,14 @@ om_status life_setup(Handle *h) {
   h->ops.restore_key = life_restore_key;
   h->ops.array_written = life_array_written;
   h->ops.reserve = life_reserve;
+  h->ops.after_run = [](Handle *hh) -> om_status {
+    LifeScalars *sc = (LifeScalars *)hh->h_scalars;
+    if (!sc->wait_error) return OM_OK;
+    sc->wait_error = 0;  // cleared on the device by the next upload
+    set_error("Life: a kernel's bounded wait for its tensor copies ran out; the cells of "
+              "this run are unspecified");
+    return OM_ERR_CUDA;
+  };
   OM_TRY(alloc_array(h, "cell", sizeof(int32_t)));
   if (cudaMalloc(&st->d_flag, sizeof(uint32_t)) != cudaSuccess) {
     set_error("Life: cannot allocate the cell-value flag");

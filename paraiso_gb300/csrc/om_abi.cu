@@ -376,6 +376,7 @@ static om_status finish(Handle *h) {
   prof_collect(h);
   for (auto &a : h->arrays)
     if (a.newer == Newer::kBoth && a.host) a.newer = Newer::kDevice;
+  if (h->ops.after_run) OM_TRY(h->ops.after_run(h));
   return OM_OK;
 }
 

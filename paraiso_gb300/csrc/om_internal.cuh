@@ -78,6 +78,9 @@ struct KindOps {
   om_status (*reserve)(Handle *, int kernel_id, int n) = nullptr;
   // false when a kernel synchronises with the host mid-run (no graph capture)
   bool (*graph_ok)(Handle *, int kernel_id) = nullptr;
+  // after a run has completed and its scalars are back on the host: report
+  // a failure that kernels recorded in the scalar block
+  om_status (*after_run)(Handle *) = nullptr;
   // derive host-side scalar fields from the user-visible ones right before
   // the scalar block is uploaded
   void (*before_upload)(Handle *) = nullptr;

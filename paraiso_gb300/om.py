@@ -57,7 +57,8 @@ class Config(C.Structure):
     _fields_ = [("boundary", C.c_int), ("precision", C.c_int), ("gamma", C.c_double),
                 ("device", C.c_int), ("depth", C.c_int), ("tile_x", C.c_int),
                 ("tile_y", C.c_int), ("use_graph", C.c_int), ("variant", C.c_int),
-                ("life_io", C.c_int), ("life_kernel", C.c_int), ("reserved", C.c_int * 5)]
+                ("life_io", C.c_int), ("life_kernel", C.c_int), ("grid_limit", C.c_int),
+                ("reserved", C.c_int * 4)]
 
 
 _lib = None

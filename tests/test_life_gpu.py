@@ -4,6 +4,9 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
+# the profile name of the kernel the automatic choice takes on large grids
+WANT_WS = "life_ws_tma_kernel"
+
 
 def run_gpu(pg, size, init, steps, **cfg):
     life = pg.Life(size, **cfg)
@@ -70,13 +73,15 @@ def test_life_temporal_blocking_tiles(om_lib, oracle, depth, tw, th, io):
     assert launches >= 2
 
 
-@pytest.mark.parametrize("kernel", [1, 2, 3, 4])
+@pytest.mark.parametrize("kernel", list(range(1, 15)))
 @pytest.mark.parametrize("depth", [32, 13])
 def test_life_warp_specialised(om_lib, oracle, kernel, depth):
     size = (2048, 1500)   # several tiles per CTA on a small grid, partial tiles
     init = oracle.life_bernoulli(size[0], size[1], 17, 0.3)
+    # four CTAs: each walks several tiles, so the producer, consumer and
+    # store warps all run their pipelined stages
     cells, pops, pop, gen, launches = run_gpu(om_lib, size, init, 45, depth=depth,
-                                              life_kernel=kernel)
+                                              life_kernel=kernel, grid_limit=4)
     rc, rp = oracle.life_run(init, 45, cyclic=True)
     assert np.array_equal(cells, rc)
     assert np.array_equal(pops, rp)
@@ -102,11 +107,12 @@ def test_life_small_grid_in_registers(om_lib, oracle, size):
 
 def test_life_automatic_kernel_choice(om_lib):
     # with no kernel or tile shape given, a grid of at least 1.5 warp-
-    # specialised tiles per SM runs on that kernel and a smaller one on the
+    # specialised tiles per SM runs on that kernel (WANT_WS: its TMA variant
+    # where rows hold at least 1024 cells) and a smaller one on the
     # register-resident blocks; both equal the register-resident blocks
     # forced by a tile height (pinned to the oracle above) bit for bit
     pg = om_lib
-    for size, want in [((8192, 8192), "life_ws_kernel"), ((2048, 1024), "life_reg_kernel")]:
+    for size, want in [((8192, 8192), WANT_WS), ((2048, 1024), "life_reg_kernel")]:
         init = None
         out = []
         for cfg in ({}, {"tile_y": 320}):
@@ -199,3 +205,18 @@ def test_life_full_size_properties(om_lib, oracle):
     assert np.array_equal(gen.population_history(100)[20:], tb_pops)
     assert np.array_equal(gen.read("cell"), tb_cells)
     gen.close()
+
+
+@pytest.mark.parametrize("kernel", [5, 8, 11, 14])
+@pytest.mark.parametrize("size", [(1024, 700), (3072, 333), (1984, 1111)])
+def test_life_tma_rows_edge_tiles(om_lib, oracle, kernel, size):
+    """The TMA variants on grids whose first and last tile columns wrap (the
+    wrapped halo word comes in as a one-word box), whose last tile column is
+    narrow (1984 = 62 words: 30 + 30 + 2) and whose rows are not a multiple
+    of the tile height; three CTAs, so each walks several tiles."""
+    init = oracle.life_bernoulli(size[0], size[1], 29, 0.3)
+    cells, pops, pop, gen, launches = run_gpu(om_lib, size, init, 70, life_kernel=kernel,
+                                              grid_limit=3)
+    rc, rp = oracle.life_run(init, 70, cyclic=True)
+    assert np.array_equal(cells, rc)
+    assert np.array_equal(pops, rp)
