@@ -70,96 +70,76 @@ __device__ __forceinline__ void flux_prim_rev(R g, R rho, R v0, R v1, R p, const
   xb.p += pb;
 }
 
-// flux_cons<AX> reverse: fb -> (rho, m0, m1, e)
-template <int AX, class R>
-__device__ __forceinline__ void flux_cons_rev(R g, R rho, R m0, R m1, R e, const Flux<R> &fb,
-                                              R &rhob, R &m0b, R &m1b, R &eb) {
-  const R v0 = m0 / rho, v1 = m1 / rho;
-  const R p = (g - R(1)) * (e - hs::kinetic(v0, v1, m0, m1));
-  const R h = e + p;
-  const R va = AX == 0 ? v0 : v1;
-  R v0b = 0, v1b = 0, pb = 0, vab = 0;
-  if (AX == 0) m0b += fb.fd; else m1b += fb.fd;
-  m0b += fb.fm0 * va;
-  m1b += fb.fm1 * va;
-  vab += fb.fm0 * m0 + fb.fm1 * m1;
-  pb += AX == 0 ? fb.fm0 : fb.fm1;
-  const R hb = fb.fe * va;
-  vab += fb.fe * h;
-  eb += hb;
-  pb += hb;
-  eb += (g - R(1)) * pb;
-  const R keb = -(g - R(1)) * pb;
-  kinetic_rev(v0, v1, m0, m1, keb, v0b, v1b, m0b, m1b);
-  if (AX == 0) v0b += vab; else v1b += vab;
-  m0b += v0b / rho;
-  m1b += v1b / rho;
-  rhob -= (v0b * v0 + v1b * v1) / rho;
-}
-
-// star_flux<AX> reverse: fb -> (sstar, shock, rho, v0, v1, p)
+// star_flux<AX> reverse: fb -> (sstar, shock, rho, v0, v1, p), in closed
+// form.  The star record of side K (HydroMain.hs:272-282) is density
+// d = rho (S - u) / (S - S*), velocity (S* along the wall, the side's own
+// across it: what m/rho of the record recovers) and energy density
+// d (E/rho + (S* - u)(S* + p/(rho (S - u)))); its pressure is the equation
+// of state of the record, p* = (g-1)(e - d (S*^2 + vt^2)/2), and its flux
+// (d S*, d S*^2 + p*, d vt S*, (e + p*) S*).  This is the derivative of the
+// same function as the flux of the recovered record; three reciprocals.
 template <int AX, class R>
 __device__ __forceinline__ void star_flux_rev(R g, R sstar, R shock, R rho, R v0, R v1, R p,
                                               const Flux<R> &fb, R &sstarb, R &shockb,
                                               PrimBar<R> &xb) {
-  const R speed = AX == 0 ? v0 : v1;
-  const R su = shock - speed, ss = shock - sstar;
-  const R dens = rho * su / ss;
-  const R mome0 = dens * (AX == 0 ? sstar : v0);
-  const R mome1 = dens * (AX == 1 ? sstar : v1);
-  const R m0 = rho * v0, m1 = rho * v1;
-  const R e = hs::kinetic(v0, v1, m0, m1) + (R(1) / (g - R(1))) * p;
-  const R pr = p / rho;
-  const R w = pr / su;
+  const R gm1 = g - R(1), gm1inv = R(1) / gm1;
+  const R u = AX == 0 ? v0 : v1, vt = AX == 0 ? v1 : v0;
+  const R fdb = fb.fd, fnb = AX == 0 ? fb.fm0 : fb.fm1, ftb = AX == 0 ? fb.fm1 : fb.fm0;
+  const R su = shock - u, ss = shock - sstar;
+  const R rss = R(1) / ss, rsu = R(1) / su, rr = R(1) / rho;
+  const R dens = rho * su * rss;
+  const R E = R(0.5) * rho * (u * u + vt * vt) + gm1inv * p;
+  const R w = p * rr * rsu;
   const R z = sstar + w;
-  const R y = (sstar - speed) * z;
-  const R x = e / rho + y;
+  const R y = (sstar - u) * z;
+  const R x = E * rr + y;
   const R enrg = dens * x;
-  R densb = 0, mome0b = 0, mome1b = 0, enrgb = 0;
-  flux_cons_rev<AX>(g, dens, mome0, mome1, enrg, fb, densb, mome0b, mome1b, enrgb);
-  R rhob = 0, v0b = 0, v1b = 0, pb = 0, sub = 0, ssb = 0, speedb = 0;
+  const R q2 = sstar * sstar + vt * vt;
+  const R pst = gm1 * (enrg - R(0.5) * dens * q2);
+  // flux components
+  R densb = fdb * sstar + fnb * sstar * sstar + ftb * vt * sstar;
+  R Ssb = fdb * dens + fnb * R(2) * dens * sstar + ftb * dens * vt + fb.fe * (enrg + pst);
+  R vtb = ftb * dens * sstar;
+  R enrgb = fb.fe * sstar;
+  const R pstb = fnb + fb.fe * sstar;
+  // p* = (g-1)(e - d q2 / 2)
+  enrgb += gm1 * pstb;
+  densb -= gm1 * pstb * R(0.5) * q2;
+  Ssb -= gm1 * pstb * dens * sstar;
+  vtb -= gm1 * pstb * dens * vt;
+  // e = d x, x = E/rho + (S* - u) z, z = S* + p/(rho (S - u))
   densb += enrgb * x;
   const R xbar = enrgb * dens;
-  const R ebar = xbar / rho;
-  rhob -= xbar * e / rho / rho;
-  const R ybar = xbar;
-  sstarb += ybar * z;
-  speedb -= ybar * z;
-  const R zbar = ybar * (sstar - speed);
-  sstarb += zbar;
-  const R wbar = zbar;
-  const R prb = wbar / su;
-  sub -= wbar * w / su;
-  pb += prb / rho;
-  rhob -= prb * pr / rho;
-  pb += ebar / (g - R(1));
-  R m0b = 0, m1b = 0;
-  kinetic_rev(v0, v1, m0, m1, ebar, v0b, v1b, m0b, m1b);
-  rhob += m0b * v0 + m1b * v1;
-  v0b += m0b * rho;
-  v1b += m1b * rho;
-  if (AX == 0) {
-    densb += mome0b * sstar;
-    sstarb += mome0b * dens;
-    densb += mome1b * v1;
-    v1b += mome1b * dens;
-  } else {
-    densb += mome0b * v0;
-    v0b += mome0b * dens;
-    densb += mome1b * sstar;
-    sstarb += mome1b * dens;
-  }
-  rhob += densb * su / ss;
-  sub += densb * rho / ss;
-  ssb -= densb * dens / ss;
-  shockb += sub;
-  speedb -= sub;
-  shockb += ssb;
-  sstarb -= ssb;
-  if (AX == 0) v0b += speedb; else v1b += speedb;
+  const R Eb = xbar * rr;
+  R rrb = xbar * E;
+  R ub = -xbar * z;
+  Ssb += xbar * z;
+  const R zb = xbar * (sstar - u);
+  Ssb += zb;
+  R pb = zb * rr * rsu;
+  rrb += zb * p * rsu;
+  R sub = -zb * w * rsu;
+  R rhob = -rrb * rr * rr;
+  // E = rho (u^2 + vt^2) / 2 + p/(g-1)
+  rhob += Eb * R(0.5) * (u * u + vt * vt);
+  ub += Eb * rho * u;
+  vtb += Eb * rho * vt;
+  pb += Eb * gm1inv;
+  // d = rho (S - u) / (S - S*)
+  rhob += densb * su * rss;
+  sub += densb * rho * rss;
+  const R ssb = -densb * dens * rss;
+  shockb += sub + ssb;
+  ub -= sub;
+  sstarb += Ssb - ssb;
   xb.rho += rhob;
-  xb.v0 += v0b;
-  xb.v1 += v1b;
+  if (AX == 0) {
+    xb.v0 += ub;
+    xb.v1 += vtb;
+  } else {
+    xb.v1 += ub;
+    xb.v0 += vtb;
+  }
   xb.p += pb;
 }
 
