@@ -61,7 +61,9 @@ typedef struct {
   int device;       /* CUDA device ordinal */
   int depth;        /* Life: generations per temporally blocked launch (0 = tuned) */
   int tile_x;       /* Life: tile width in 32-cell words; Hydro: tile width in cells (0 = tuned) */
-  int tile_y;       /* tile height in cells (0 = tuned) */
+  int tile_y;       /* tile height in cells (0 = tuned; Hydro FP32: 0 = 32 x 32, 8 and 16
+                       with tile_x 0 or 32, 8 and 16 with tile_x 64; a negative -k
+                       selects the column sweep of k rows per chunk, 8 or 16) */
   int use_graph;    /* capture om_run_n in a CUDA graph (default 1) */
   int variant;      /* 0 = fastest path.  Life 1: integer one-cell-per-thread kernel only.
                        Hydro 1: plain unfused FP64-structured grid-stride kernels */

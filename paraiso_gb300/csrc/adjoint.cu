@@ -230,8 +230,8 @@ __device__ __forceinline__ void face_slots(const Prim<R> st[4], const PrimBar<R>
 // HLLC and MUSCL reverse of one stage-2 face along AX: stencil st[4] (the
 // stage-1 states of cells f-2 .. f+1), wall-flux cotangent fb -> 16 slots
 template <int AX, class R>
-__device__ __forceinline__ void face2_rev(R g, const Prim<R> st[4], const Flux<R> &fb,
-                                          R out[16]) {
+__device__ __forceinline__ void face2_rev(const hf::Consts<R> &KC, const Prim<R> st[4],
+                                          const Flux<R> &fb, R out[16]) {
   Prim<R> L, Rt;
   hs::muscl(st[0].rho, st[1].rho, st[2].rho, st[3].rho, L.rho, Rt.rho);
   hs::muscl(st[0].v0, st[1].v0, st[2].v0, st[3].v0, L.v0, Rt.v0);
@@ -240,7 +240,7 @@ __device__ __forceinline__ void face2_rev(R g, const Prim<R> st[4], const Flux<R
   PrimBar<R> Lb, Rb;
   ha::zero(Lb);
   ha::zero(Rb);
-  ha::hllc_rev<AX>(g, L, Rt, fb, Lb, Rb);
+  ha::hllc_rev<AX>(KC, L, Rt, fb, Lb, Rb);
   face_slots(st, Lb, Rb, out);
 }
 
@@ -260,6 +260,7 @@ adj_stage2_tile(Fields<R> Ub, Fields<R> U1b, Fields<R> Pbase, Geo<R> G, double *
   __shared__ R pend[4];
   wait_previous_kernel();
   G.dt = G.step_dt();
+  const hf::Consts<R> KC = hf::consts<R>(G.g);
   const Fields<R> P = G.state();
   const TapeView<R> T = G.tape();
   const Fields<R> Q = T.fields(kTapeQ), U2 = T.fields(kTapeU2);
@@ -361,7 +362,7 @@ adj_stage2_tile(Fields<R> Ub, Fields<R> U1b, Fields<R> Pbase, Geo<R> G, double *
                      d0 * (s.u[2][r + 2][j + 1] - s.u[2][r + 2][j]),
                      d0 * (s.u[3][r + 2][j + 1] - s.u[3][r + 2][j])};
     R out[16];
-    face2_rev<0>(G.g, st, fb, out);
+    face2_rev<0>(KC, st, fb, out);
 #pragma unroll
     for (int k = 0; k < 16; ++k) s.slot[k][i] = out[k];
   }
@@ -391,7 +392,7 @@ adj_stage2_tile(Fields<R> Ub, Fields<R> U1b, Fields<R> Pbase, Geo<R> G, double *
                      d1 * (s.u[2][j + 1][r + 2] - s.u[2][j][r + 2]),
                      d1 * (s.u[3][j + 1][r + 2] - s.u[3][j][r + 2])};
     R out[16];
-    face2_rev<1>(G.g, st, fb, out);
+    face2_rev<1>(KC, st, fb, out);
 #pragma unroll
     for (int k = 0; k < 16; ++k) s.slot[k][i] = out[k];
   }
@@ -479,6 +480,7 @@ adj_stage1_tile(Fields<R> U1b, Fields<R> Pbase, Fields<R> Pb, Geo<R> G,
   // (the pending dt of the step before), free now for the next step
   if (blockIdx.x == 0 && threadIdx.x == 0) release[0] = release[1] = ~0ull;
   G.dt = G.step_dt();
+  const hf::Consts<R> KC = hf::consts<R>(G.g);
   const Fields<R> P = G.state();
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int nt0 = (G.n0 + TX - 1) / TX;
@@ -516,7 +518,7 @@ adj_stage1_tile(Fields<R> U1b, Fields<R> Pbase, Fields<R> Pb, Geo<R> G,
       const Prim<R> a = cot(j + 1, r + 1), c = cot(j, r + 1);
       const Flux<R> fb{d0 * (a.rho - c.rho), d0 * (a.v0 - c.v0), d0 * (a.v1 - c.v1),
                        d0 * (a.p - c.p)};
-      ha::hllc_rev<0>(G.g, state(j, r + 1), state(j + 1, r + 1), fb, Lb, Rb);
+      ha::hllc_rev<0>(KC, state(j, r + 1), state(j + 1, r + 1), fb, Lb, Rb);
       s.fx[0][r][j] = Lb.rho; s.fx[1][r][j] = Lb.v0; s.fx[2][r][j] = Lb.v1; s.fx[3][r][j] = Lb.p;
       s.fx[4][r][j] = Rb.rho; s.fx[5][r][j] = Rb.v0; s.fx[6][r][j] = Rb.v1; s.fx[7][r][j] = Rb.p;
     } else {
@@ -527,7 +529,7 @@ adj_stage1_tile(Fields<R> U1b, Fields<R> Pbase, Fields<R> Pb, Geo<R> G,
       const Prim<R> a = cot(r + 1, j + 1), c = cot(r + 1, j);
       const Flux<R> fb{d1 * (a.rho - c.rho), d1 * (a.v0 - c.v0), d1 * (a.v1 - c.v1),
                        d1 * (a.p - c.p)};
-      ha::hllc_rev<1>(G.g, state(r + 1, j), state(r + 1, j + 1), fb, Lb, Rb);
+      ha::hllc_rev<1>(KC, state(r + 1, j), state(r + 1, j + 1), fb, Lb, Rb);
       s.fy[0][j][r] = Lb.rho; s.fy[1][j][r] = Lb.v0; s.fy[2][j][r] = Lb.v1; s.fy[3][j][r] = Lb.p;
       s.fy[4][j][r] = Rb.rho; s.fy[5][j][r] = Rb.v0; s.fy[6][j][r] = Rb.v1; s.fy[7][j][r] = Rb.p;
     }
@@ -872,7 +874,9 @@ static om_status launch_tape(Handle *h, AdjointScratch *s, void *const *in, void
   a.margin_min = nullptr;
   OM_CUDA_CHECK(cudaMemsetAsync(&s->sc->tsmin[1 - read_slot], 0xFF, sizeof(unsigned long long),
                                 h->stream));
-  const cudaError_t e = hydro_fused_tape(s->fp64, h->cfg.variant == 2, a, t, h->stream);
+  const cudaError_t e = hydro_fused_tape(s->fp64, h->cfg.variant == 2, a, t, h->stream,
+                                         hydro_tile_of(h->cfg.tile_x, h->cfg.tile_y,
+                                                       !s->fp64 && h->cfg.variant == 0));
   if (e != cudaSuccess) {
     set_error(std::string("Hydro taped step: ") + cudaGetErrorString(e));
     return OM_ERR_CUDA;

@@ -10,7 +10,8 @@
 // (kind, size, precision, device) for the life of the process:
 //   Life  : kernel family (register-resident blocks, warp-specialised,
 //           shared-memory tiles), temporal depth, block rows
-//   Hydro : fused-step tile shape (32x8, 32x16, 64x16, 32x32, 64x8)
+//   Hydro : fused-step tile shape (32x8, 32x16, 64x16, 32x32, 64x8) and
+//           column sweeps (32 x 8, 32 x 16 and 64 x 8 rows per chunk)
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -122,8 +123,10 @@ extern "C" om_status om_autotune(int kind, int ndim, const int *sizes, const om_
     }
   } else {
     steps = 8;
-    const int shapes[5][2] = {{0, 0}, {0, 8}, {64, 0}, {0, 32}, {64, 8}};
-    const int nshapes = (b.precision == 64 || b.variant != 0) ? 1 : 5;
+    // tiles, then column sweeps (a negative tile_y: rows per chunk)
+    const int shapes[8][2] = {{0, 0}, {0, 8}, {64, 0}, {0, 16}, {64, 8},
+                              {0, -8}, {0, -16}, {64, -8}};
+    const int nshapes = (b.precision == 64 || b.variant != 0) ? 1 : 8;
     for (int s = 0; s < nshapes; ++s) {
       om_config c = b;
       c.tile_x = shapes[s][0];
@@ -161,7 +164,7 @@ extern "C" om_status om_autotune_ensemble(int count, const int *sizes, const om_
   }
   om_config b;
   if (base) b = *base; else om_config_default(&b);
-  const int shapes[5][2] = {{0, 0}, {0, 8}, {64, 0}, {0, 32}, {64, 8}};
+  const int shapes[5][2] = {{0, 0}, {0, 8}, {64, 0}, {0, 16}, {64, 8}};
   const int nshapes = (b.precision == 64 || b.variant != 0) ? 1 : 5;
   long long cells = 0;
   for (int k = 0; k < count; ++k) cells += (long long)sizes[2 * k] * sizes[2 * k + 1];

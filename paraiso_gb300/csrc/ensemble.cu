@@ -32,7 +32,7 @@ struct om_ensemble_s {
   int count = 0;
   int fp64 = 0;
   bool exact = false;
-  int tile = kTile32x16;
+  int tile = kTile32x32;
   int tx = 32, ty = 16;
   double gamma = 1.4;
   int device = 0;
@@ -150,6 +150,7 @@ om_status om_ensemble_create(int count, const int *sizes, const om_config *cfg,
   E->fp64 = c.precision == 64;
   E->exact = c.variant == 2 || E->fp64;
   E->tile = hydro_tile_of(c.tile_x, c.tile_y, !E->exact && !E->fp64);
+  if (hydro_tile_is_sweep(E->tile)) E->tile = kTile32x32;  // items are tiles
   hydro_tile_dims(E->tile, &E->tx, &E->ty);
   E->gamma = c.gamma;
   E->device = c.device;

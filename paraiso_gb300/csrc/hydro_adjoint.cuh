@@ -27,9 +27,10 @@ template <class R> __device__ __forceinline__ void zero(PrimBar<R> &a) {
 template <class R>
 __device__ __forceinline__ void sound_rev(R g, R rho, R p, R c, R cb, R &rhob, R &pb) {
   if (cb == R(0)) return;
-  const R tb = cb / (R(2) * c);
-  pb += tb * g / rho;
-  rhob -= tb * (g * p / rho) / rho;
+  const R tb = R(0.5) * cb / c;
+  const R gr = g / rho;
+  pb += tb * gr;
+  rhob -= tb * gr * p / rho;
 }
 
 // kinetic energy 0.5 (v0 m0 + v1 m1)
@@ -45,10 +46,10 @@ __device__ __forceinline__ void kinetic_rev(R v0, R v1, R m0, R m1, R keb, R &v0
 
 // flux_prim<AX> reverse: fb -> (rho, v0, v1, p)
 template <int AX, class R>
-__device__ __forceinline__ void flux_prim_rev(R g, R rho, R v0, R v1, R p, const Flux<R> &fb,
-                                              PrimBar<R> &xb) {
+__device__ __forceinline__ void flux_prim_rev(const hf::Consts<R> &k, R rho, R v0, R v1, R p,
+                                              const Flux<R> &fb, PrimBar<R> &xb) {
   const R m0 = rho * v0, m1 = rho * v1;
-  const R e = hs::kinetic(v0, v1, m0, m1) + (R(1) / (g - R(1))) * p;
+  const R e = hs::kinetic(v0, v1, m0, m1) + k.gm1inv * p;
   const R h = e + p;
   const R va = AX == 0 ? v0 : v1;
   R m0b = 0, m1b = 0, vab = 0, v0b = 0, v1b = 0, pb = 0;
@@ -61,7 +62,7 @@ __device__ __forceinline__ void flux_prim_rev(R g, R rho, R v0, R v1, R p, const
   vab += fb.fe * h;
   const R eb = hb;
   pb += hb;
-  pb += eb / (g - R(1));
+  pb += eb * k.gm1inv;
   kinetic_rev(v0, v1, m0, m1, eb, v0b, v1b, m0b, m1b);
   if (AX == 0) v0b += vab; else v1b += vab;
   xb.rho += m0b * v0 + m1b * v1;
@@ -79,10 +80,10 @@ __device__ __forceinline__ void flux_prim_rev(R g, R rho, R v0, R v1, R p, const
 // (d S*, d S*^2 + p*, d vt S*, (e + p*) S*).  This is the derivative of the
 // same function as the flux of the recovered record; three reciprocals.
 template <int AX, class R>
-__device__ __forceinline__ void star_flux_rev(R g, R sstar, R shock, R rho, R v0, R v1, R p,
-                                              const Flux<R> &fb, R &sstarb, R &shockb,
-                                              PrimBar<R> &xb) {
-  const R gm1 = g - R(1), gm1inv = R(1) / gm1;
+__device__ __forceinline__ void star_flux_rev(const hf::Consts<R> &k, R sstar, R shock, R rho,
+                                              R v0, R v1, R p, const Flux<R> &fb, R &sstarb,
+                                              R &shockb, PrimBar<R> &xb) {
+  const R gm1 = k.gm1, gm1inv = k.gm1inv;
   const R u = AX == 0 ? v0 : v1, vt = AX == 0 ? v1 : v0;
   const R fdb = fb.fd, fnb = AX == 0 ? fb.fm0 : fb.fm1, ftb = AX == 0 ? fb.fm1 : fb.fm0;
   const R su = shock - u, ss = shock - sstar;
@@ -143,75 +144,73 @@ __device__ __forceinline__ void star_flux_rev(R g, R sstar, R shock, R rho, R v0
   xb.p += pb;
 }
 
-// hllcQ reverse: cotangent of q -> (sp, p)
+// hllcQ reverse: cotangent of q = sqrt(t) -> (sp, p), t = 1 + qc (sp/p - 1)
+// (qc = (g+1)/(2g)); q is the forward's value
 template <class R>
-__device__ __forceinline__ void hllc_q_rev(R g, R sp, R p, R qb, R &spb, R &pb) {
+__device__ __forceinline__ void hllc_q_rev(R qc, R sp, R p, R q, R qb, R &spb, R &pb) {
   if (p <= sp) return;  // constant branch
-  const R k = (g + R(1)) / (R(2) * g);
-  const R t = R(1) + k * (sp / p - R(1));
-  const R q = sqrt(t);
-  const R tb = qb / (R(2) * q);
-  spb += tb * k / p;
-  pb -= tb * k * sp / p / p;
+  const R rp = R(1) / p;
+  const R tb = R(0.5) * qb / q;
+  spb += tb * qc * rp;
+  pb -= tb * qc * sp * rp * rp;
 }
 
 // hllc<AX> reverse: cotangent of the wall fluxes -> cotangents of the two
-// primitive states (the sound speeds' dependence on them included).
+// primitive states (the sound speeds' dependence on them included).  The
+// forward quantities are recomputed with the expressions of the production
+// algebra (hf::hllc), so the branch decisions are the FP32 forward's; the
+// derivative is that of the same function in either algebra.
 template <int AX, class R>
-__device__ __forceinline__ void hllc_rev(R g, const Prim<R> &L, const Prim<R> &Rt,
-                                         const Flux<R> &fb, PrimBar<R> &Lb, PrimBar<R> &Rb) {
+__device__ __forceinline__ void hllc_rev(const hf::Consts<R> &k, const Prim<R> &L,
+                                         const Prim<R> &Rt, const Flux<R> &fb, PrimBar<R> &Lb,
+                                         PrimBar<R> &Rb) {
+  const R g = k.g;
   const R cl = hs::sound(g, L.rho, L.p), cr = hs::sound(g, Rt.rho, Rt.p);
-  const R densMid = (L.rho + Rt.rho) / R(2);
-  const R soundMid = (cl + cr) / R(2);
+  const R densMid = R(0.5) * (L.rho + Rt.rho);
+  const R soundMid = R(0.5) * (cl + cr);
   const R uL = AX == 0 ? L.v0 : L.v1;
   const R uR = AX == 0 ? Rt.v0 : Rt.v1;
-  const R psraw = (L.p + Rt.p) / R(2) - densMid * soundMid * (uR - uL);
+  const R psraw = R(0.5) * (L.p + Rt.p) - densMid * soundMid * (uR - uL);
   const R presStar = hs::omax(R(0), psraw);
-  const R qL = hs::hllc_q(g, presStar, L.p), qR = hs::hllc_q(g, presStar, Rt.p);
+  const R tL = sqrt(R(1) + k.qc * (presStar / L.p - R(1)));
+  const R tR = sqrt(R(1) + k.qc * (presStar / Rt.p - R(1)));
+  const R qL = (L.p <= presStar) ? R(1) : tL;
+  const R qR = (Rt.p <= presStar) ? R(1) : tR;
   const R shockLeft = uL - cl * qL;
   const R shockRight = uR + cr * qR;
-  const R num = Rt.p - L.p + L.rho * uL * (shockLeft - uL) - Rt.rho * uR * (shockRight - uR);
-  const R den = L.rho * (shockLeft - uL) - Rt.rho * (shockRight - uR);
-  const R shockStar = num / den;
+  const R aL = L.rho * (shockLeft - uL), aR = Rt.rho * (shockRight - uR);
+  const R num = Rt.p - L.p + aL * uL - aR * uR;
+  const R rden = R(1) / (aL - aR);
+  const R shockStar = num * rden;
   const bool posL = R(0) < shockLeft, posS = R(0) < shockStar, posR = R(0) < shockRight;
   const bool useL = posL || posS;
   const bool star = useL ? !posL : posR;
   const Prim<R> &X = useL ? L : Rt;
   PrimBar<R> &Xb = useL ? Lb : Rb;
   if (!star) {
-    flux_prim_rev<AX>(g, X.rho, X.v0, X.v1, X.p, fb, Xb);
+    flux_prim_rev<AX>(k, X.rho, X.v0, X.v1, X.p, fb, Xb);
     return;
   }
   const R shock = useL ? shockLeft : shockRight;
   R sstarb = 0, shockb = 0;
-  star_flux_rev<AX>(g, shockStar, shock, X.rho, X.v0, X.v1, X.p, fb, sstarb, shockb, Xb);
+  star_flux_rev<AX>(k, shockStar, shock, X.rho, X.v0, X.v1, X.p, fb, sstarb, shockb, Xb);
   R SLb = useL ? shockb : R(0), SRb = useL ? R(0) : shockb;
   R rhoLb = 0, rhoRb = 0, uLb = 0, uRb = 0, pLb = 0, pRb = 0, clb = 0, crb = 0;
-  // shockStar = num / den
-  const R numb = sstarb / den;
-  const R denb = -sstarb * shockStar / den;
+  // shockStar = num / den, num = pR - pL + aL uL - aR uR, den = aL - aR
+  const R numb = sstarb * rden;
+  const R denb = -sstarb * shockStar * rden;
   pRb += numb;
   pLb -= numb;
-  rhoLb += numb * uL * (shockLeft - uL);
-  uLb += numb * L.rho * (shockLeft - uL);
-  {
-    const R t = numb * L.rho * uL;
-    SLb += t;
-    uLb -= t;
-  }
-  rhoRb -= numb * uR * (shockRight - uR);
-  uRb -= numb * Rt.rho * (shockRight - uR);
-  {
-    const R t = -numb * Rt.rho * uR;
-    SRb += t;
-    uRb -= t;
-  }
-  rhoLb += denb * (shockLeft - uL);
-  SLb += denb * L.rho;
-  uLb -= denb * L.rho;
-  rhoRb -= denb * (shockRight - uR);
-  SRb -= denb * Rt.rho;
-  uRb += denb * Rt.rho;
+  const R aLb = numb * uL + denb, aRb = -numb * uR - denb;
+  uLb += numb * aL;
+  uRb -= numb * aR;
+  // aL = rhoL (SL - uL), aR = rhoR (SR - uR)
+  rhoLb += aLb * (shockLeft - uL);
+  SLb += aLb * L.rho;
+  uLb -= aLb * L.rho;
+  rhoRb += aRb * (shockRight - uR);
+  SRb += aRb * Rt.rho;
+  uRb -= aRb * Rt.rho;
   // shock speeds
   uLb += SLb;
   clb -= SLb * qL;
@@ -220,19 +219,19 @@ __device__ __forceinline__ void hllc_rev(R g, const Prim<R> &L, const Prim<R> &R
   crb += SRb * qR;
   const R qRb = SRb * cr;
   R psb = 0;
-  hllc_q_rev(g, presStar, L.p, qLb, psb, pLb);
-  hllc_q_rev(g, presStar, Rt.p, qRb, psb, pRb);
+  hllc_q_rev(k.qc, presStar, L.p, tL, qLb, psb, pLb);
+  hllc_q_rev(k.qc, presStar, Rt.p, tR, qRb, psb, pRb);
   const R psrawb = (R(0) < psraw) ? psb : R(0);
-  pLb += psrawb / R(2);
-  pRb += psrawb / R(2);
+  pLb += R(0.5) * psrawb;
+  pRb += R(0.5) * psrawb;
   const R dmb = -psrawb * soundMid * (uR - uL);
   const R smb = -psrawb * densMid * (uR - uL);
   uRb -= psrawb * densMid * soundMid;
   uLb += psrawb * densMid * soundMid;
-  rhoLb += dmb / R(2);
-  rhoRb += dmb / R(2);
-  clb += smb / R(2);
-  crb += smb / R(2);
+  rhoLb += R(0.5) * dmb;
+  rhoRb += R(0.5) * dmb;
+  clb += R(0.5) * smb;
+  crb += R(0.5) * smb;
   sound_rev(g, L.rho, L.p, cl, clb, rhoLb, pLb);
   sound_rev(g, Rt.rho, Rt.p, cr, crb, rhoRb, pRb);
   Lb.rho += rhoLb;
@@ -277,7 +276,8 @@ __device__ __forceinline__ void muscl_rev(R x0, R x1, R x2, R x3, R lb, R rb, R 
 template <class R>
 __device__ __forceinline__ void cons_from_prim_rev(R g, R d2, R b0, R b1, R e2,
                                                    const PrimBar<R> &qb, R Ub[4]) {
-  const R v0 = b0 / d2, v1 = b1 / d2;
+  const R rd = R(1) / d2;
+  const R v0 = b0 * rd, v1 = b1 * rd;
   const R pn = (g - R(1)) * (e2 - hs::kinetic(v0, v1, b0, b1));
   R d2b = (R(1e-2) < d2) ? qb.rho : R(0);
   const R pnb = (R(1e-2) < pn) ? qb.p : R(0);
@@ -285,9 +285,9 @@ __device__ __forceinline__ void cons_from_prim_rev(R g, R d2, R b0, R b1, R e2,
   const R e2b = (g - R(1)) * pnb;
   const R keb = -(g - R(1)) * pnb;
   kinetic_rev(v0, v1, b0, b1, keb, v0b, v1b, b0b, b1b);
-  b0b += v0b / d2;
-  b1b += v1b / d2;
-  d2b -= (v0b * v0 + v1b * v1) / d2;
+  b0b += v0b * rd;
+  b1b += v1b * rd;
+  d2b -= (v0b * v0 + v1b * v1) * rd;
   Ub[0] = d2b;
   Ub[1] = b0b;
   Ub[2] = b1b;

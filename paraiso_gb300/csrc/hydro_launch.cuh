@@ -12,19 +12,30 @@ namespace om {
 
 // Tile shapes of the fused kernel available to the tuner (FP32 production
 // build; FP64 and the exact FP32 variant run 32x16).
+// The sweep shapes (kSweep*) walk strips of TX columns down the grid in
+// chunks of TY rows (hydro_sweep.cuh).
 enum HydroTile {
-  kTile32x8 = 0, kTile32x16 = 1, kTile64x16 = 2, kTile32x32 = 3, kTile64x8 = 4, kTileCount = 5
+  kTile32x8 = 0, kTile32x16 = 1, kTile64x16 = 2, kTile32x32 = 3, kTile64x8 = 4,
+  kSweep32x8 = 5, kSweep32x16 = 6, kSweep64x8 = 7, kTileCount = 8
 };
+inline bool hydro_tile_is_sweep(int tile) { return tile >= kSweep32x8; }
 void hydro_tile_dims(int tile, int *tx, int *ty);
 // the tile a configuration's tile_x / tile_y select (0 = default): x 64
 // with y 8 is 64x8, else 64x16; x 0 or 32 with y 8, 32 or other is 32x8,
 // 32x32 or 32x16
+// A negative tile_y selects a sweep of -tile_y rows per chunk (x 32 or 64).
+// The production default (0, 0) is the 32 x 32 tile, the fastest on GB300
+// at 4096^2.
 inline int hydro_tile_of(int tile_x, int tile_y, bool production) {
   if (!production) return kTile32x16;
+  if (tile_y < 0) {
+    if (tile_x == 64) return kSweep64x8;
+    return tile_y == -16 ? kSweep32x16 : kSweep32x8;
+  }
   if (tile_x == 64) return tile_y == 8 ? kTile64x8 : kTile64x16;
   if (tile_y == 8) return kTile32x8;
-  if (tile_y == 32) return kTile32x32;
-  return kTile32x16;
+  if (tile_y == 16) return kTile32x16;
+  return kTile32x32;
 }
 
 // fused two-stage step; `exact` selects the no-contraction build
@@ -34,7 +45,7 @@ cudaError_t hydro_fused_f64(const HydroStepArgs &a, int tile, cudaStream_t s, in
 // one fused step of a periodic grid that also writes the tape of the
 // reverse sweep (32x16 tiles; the build of the handle's variant)
 cudaError_t hydro_fused_tape(int fp64, bool exact, const HydroStepArgs &a, const HydroTapeOut &t,
-                             cudaStream_t s);
+                             cudaStream_t s, int tile);
 
 // ensemble step over every instance (persistent grid of `grid` blocks, 0 =
 // resident blocks x SMs); args/prefix in device memory
