@@ -12,6 +12,8 @@
 //           shared-memory tiles), temporal depth, block rows
 //   Hydro : fused-step tile shape (32x8, 32x16, 64x16, 32x32, 64x8) and
 //           column sweeps (32 x 8, 32 x 16 and 64 x 8 rows per chunk)
+//   Ensemble: tile shape and persistent grid size (all resident CTAs, or
+//           one CTA per SM)
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -168,12 +170,21 @@ extern "C" om_status om_autotune_ensemble(int count, const int *sizes, const om_
   const int nshapes = (b.precision == 64 || b.variant != 0) ? 1 : 5;
   long long cells = 0;
   for (int k = 0; k < count; ++k) cells += (long long)sizes[2 * k] * sizes[2 * k + 1];
+  int dev = b.device;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) {
+    cudaGetLastError();
+    sms = 0;
+  }
   double best_r = 0;
   om_config best_c = b;
-  for (int s = 0; s < nshapes; ++s) {
+  for (int s = 0; s < 2 * nshapes; ++s) {
     om_config c = b;
-    c.tile_x = shapes[s][0];
-    c.tile_y = shapes[s][1];
+    c.tile_x = shapes[s / 2][0];
+    c.tile_y = shapes[s / 2][1];
+    // persistent grid: every resident CTA (0), or one CTA per SM
+    c.grid_limit = (s & 1) ? sms : 0;
+    if ((s & 1) && sms == 0) continue;
     om_ensemble e = nullptr;
     if (om_ensemble_create(count, sizes, &c, &e) != OM_OK) continue;
     float ms = 0, bestms = 1e30f;

@@ -171,6 +171,21 @@ template <class R> __device__ __forceinline__ R step_dt(const HydroStepArgs &a) 
   return Reals<R>::cfl(a.sc) * tsmin;
 }
 
+// 4- or 8-byte asynchronous copy global -> shared, and its group fences
+template <class R> __device__ __forceinline__ void cp_async(R *dst, const R *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  if (sizeof(R) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
 // the scheme's wall flux and update in the exact (generated order) or the
 // production algebra
 template <bool FA, int AX, class R>
@@ -507,23 +522,31 @@ hydro_tsmin_open_kernel(const R *__restrict__ rho, const R *__restrict__ v0,
 // Ensemble step: every tile of every instance is one work item; the
 // persistent grid strides over the flattened item list (prefix[k] = first
 // item of instance k), so instances of any size advance in one launch, each
-// with its own dt, CFL minimum and time (its HydroStepArgs).
+// with its own dt, CFL minimum and time (its HydroStepArgs).  Up to
+// kEnsPrefixShared instances, the prefix is kept in shared memory.
+constexpr int kEnsPrefixShared = 1024;
+
 template <class R, int TX, int TY, int NT, bool FA = false>
 __global__ void __launch_bounds__(NT)
 hydro_ensemble_kernel(const HydroStepArgs *__restrict__ args, const int *__restrict__ prefix,
                       int count) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned long long red[32];
+  __shared__ int spref[kEnsPrefixShared + 1];
   auto &s = *reinterpret_cast<FusedSmem<R, TX, TY> *>(smem_raw);
-  const int total = prefix[count];
+  // a block's items increase, so its instance index only moves forward: it
+  // advances through the prefix (in shared memory when it fits) instead of
+  // searching global memory per item
+  const bool shared = count <= kEnsPrefixShared;
+  if (shared)
+    for (int i = threadIdx.x; i <= count; i += NT) spref[i] = prefix[i];
+  __syncthreads();
+  const int *pf = shared ? spref : prefix;
+  const int total = pf[count];
+  int lo = 0;  // instance k with prefix[k] <= item < prefix[k+1]
   for (int item = blockIdx.x; item < total; item += gridDim.x) {
-    int lo = 0, hi = count - 1;  // instance k with prefix[k] <= item < prefix[k+1]
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (prefix[mid] <= item) lo = mid;
-      else hi = mid - 1;
-    }
-    fused_tile<R, TX, TY, NT, false, false, FA>(args[lo], item - prefix[lo], s, red);
+    while (lo < count - 1 && pf[lo + 1] <= item) ++lo;
+    fused_tile<R, TX, TY, NT, false, false, FA>(args[lo], item - pf[lo], s, red);
     __syncthreads();
   }
 }

@@ -42,21 +42,6 @@ namespace sw {
 // ring slot of row y (y >= -8)
 template <int N> __device__ __forceinline__ int slot(int y) { return (y + 8 * N) % N; }
 
-// 4- or 8-byte asynchronous copy global -> shared
-template <class R> __device__ __forceinline__ void cp_async(R *dst, const R *src) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  if (sizeof(R) == 8)
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() {
-  asm volatile("cp.async.commit_group;\n" ::: "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() {
-  asm volatile("cp.async.wait_all;\n" ::: "memory");
-}
-
 }  // namespace sw
 
 // One strip (columns X0 .. X0+TX-1) over rows [ya, yb) of the grid of `a`,
@@ -91,12 +76,12 @@ __device__ __forceinline__ void sweep_segment(const HydroStepArgs &a, int X0, in
       const int gx = near ? hk::wrap_near(X0 + px - 3, n0) : hk::wrap<R>(X0 + px - 3, n0);
       const size_t gi = (size_t)gy * n0 + gx;
       const int sy = (k % 3) * TY + ry;
-      sw::cp_async(&s.P[0][sy][px], rho + gi);
-      sw::cp_async(&s.P[1][sy][px], vx + gi);
-      sw::cp_async(&s.P[2][sy][px], vy + gi);
-      sw::cp_async(&s.P[3][sy][px], pr + gi);
+      hk::cp_async(&s.P[0][sy][px], rho + gi);
+      hk::cp_async(&s.P[1][sy][px], vx + gi);
+      hk::cp_async(&s.P[2][sy][px], vy + gi);
+      hk::cp_async(&s.P[3][sy][px], pr + gi);
     }
-    sw::cp_async_commit();
+    hk::cp_async_commit();
   };
   auto sound_block = [&](int k) {
     for (int i = tid; i < TY * S::PX; i += NT) {
@@ -115,7 +100,7 @@ __device__ __forceinline__ void sweep_segment(const HydroStepArgs &a, int X0, in
       load_block(0);
       load_block(1);
     }
-    sw::cp_async_wait_all();
+    hk::cp_async_wait_all();
     __syncthreads();
     if (first) sound_block(0);
     sound_block(c + 1);

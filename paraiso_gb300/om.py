@@ -620,6 +620,37 @@ class Ensemble:
         return v.value
 
 
+def measure_rate(kind: str, size, config: Config, steps: int) -> float:
+    """Cell-updates/s of one configuration measured as the tuner measures a
+    candidate: a settling run, then the best of two timed runs of `steps`
+    steps on the Bernoulli(0.3) / Kelvin-Helmholtz start of seed 1."""
+    cls = {"life": Life, "hydro": Hydro}[kind]
+    m = cls(size, config=config)
+    try:
+        if kind == "life":
+            m.fill_random(1, 0.3)
+        else:
+            m.init_kh(1)
+        m.time_run("proceed", steps)
+        best = min(m.time_run("proceed", steps) for _ in range(2))
+    finally:
+        m.close()
+    return size[0] * size[1] * steps / (best * 1e-3)
+
+
+def ensemble_rate(sizes, config: Config, steps: int = 4) -> float:
+    """Cell-updates/s of an ensemble configuration measured as
+    om_autotune_ensemble measures a candidate."""
+    e = Ensemble(sizes, config=config)
+    try:
+        e.init_kh(1)
+        e.time_step(steps)
+        best = min(e.time_step(steps) for _ in range(2))
+    finally:
+        e.close()
+    return sum(a * b for a, b in sizes) * steps / (best * 1e-3)
+
+
 def autotune(kind: str, size, **base) -> tuple[Config, float]:
     """Fastest launch configuration for a Life or Hydro mesh of this size
     (om_autotune): returns (config, cell-updates/s)."""

@@ -48,14 +48,19 @@ def test_ensemble_bit_exact_per_instance(om_lib, oracle, precision, variant):
     e.close()
 
 
-def test_ensemble_fast_matches_single_grids(om_lib):
+@pytest.mark.parametrize("tile", [(0, 0), (0, 16)])
+def test_ensemble_fast_matches_single_grids(om_lib, tile):
+    # (0, 16): 32 x 16 tiles, each item's primitive box copied while the
+    # block computes the item before; small instances: every block walks
+    # several instances
     sizes = om_lib.ensemble_sizes(5, 42, lo=64, hi=320)
-    e = om_lib.Ensemble(sizes, precision=32, gamma=GAMMA)
+    e = om_lib.Ensemble(sizes, precision=32, gamma=GAMMA, tile_x=tile[0], tile_y=tile[1],
+                        grid_limit=7)
     e.init_kh(7)
     e.step(3)       # graph captured
     e.step(3)       # replayed
     for k, s in enumerate(sizes):
-        h = om_lib.Hydro(s, precision=32, gamma=GAMMA)
+        h = om_lib.Hydro(s, precision=32, gamma=GAMMA, tile_x=tile[0], tile_y=tile[1])
         h.init_kh(7 + k)
         h.set_scalar("cfl", CFL)
         h.proceed(6)
