@@ -1,12 +1,12 @@
 // hydro_ref.cpp -- C entry points around the reference's pre-generated Hydro
 // class (examples-old/Hydro-exampled/dist/Hydro.{hpp,cpp}: 1024x1024, float,
-// open boundary, gamma 5/3).  Compiled together with that Hydro.cpp by
+// open boundary, gamma 5/3; or a copy resized by oracle/resize_ref.py).  Compiled together with that Hydro.cpp by
 // oracle/Makefile into oracle/_ref/libref_hydro.so.  Test infrastructure only.
 #include <cstdint>
 #include "Hydro.hpp"
 
-extern "C" int ref_hydro_size0(void) { return 1024; }
-extern "C" int ref_hydro_memory_size(void) { return 1030 * 1030; }
+extern "C" int ref_hydro_size0(void) { Hydro s; return s.size0(); }
+extern "C" int ref_hydro_memory_size(void) { Hydro s; return s.memorySize(); }
 
 // Scalars as in examples-old/Hydro-exampled/main-kh.cpp: time 0, extent 1,
 // dR = extent / size.  init(); optionally replace the four memory arrays

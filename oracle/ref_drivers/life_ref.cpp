@@ -1,7 +1,8 @@
 // life_ref.cpp -- C entry points around the reference's pre-generated Life
 // class (examples-old/Life-exampled/dist/Life.{hpp,cpp}: 128x128, open
-// boundary, old accessor API).  Compiled together with that Life.cpp by
-// oracle/Makefile into oracle/_ref/libref_life.so.  Test infrastructure only.
+// boundary, old accessor API; or a copy resized by oracle/resize_ref.py).
+// Compiled together with that Life.cpp by oracle/Makefile into
+// oracle/_ref/libref_life.so.  Test infrastructure only.
 #include <cstdint>
 #include <cstring>
 #include "Life.hpp"

@@ -172,3 +172,38 @@ def test_reference_arm_reports_our_config():
     assert bench.life_config(16384, 100, 1)["workload"].startswith("life 16384x16384 cyclic")
     assert bench.life_config(16384, 100, 1) == bench.life_config(16384, 100, 1)
     assert bench.hydro_config(4096, 1)["n0"] == 4096
+
+
+def _reference_present():
+    from oracle import resize_ref
+    return os.path.isdir(os.path.join(resize_ref.reference_tree(),
+                                      "examples-old/Life-exampled/dist"))
+
+
+@pytest.mark.skipif(not _reference_present(), reason="reference tree not present")
+def test_resized_reference_classes(oracle):
+    """oracle/resize_ref.py: resizing the generated classes to their own size
+    and back through another size reproduces them byte for byte, and the
+    resized classes compute what the oracle computes at the new size (Life
+    96^2 open, 50 generations with populations; Hydro 192^2 float open jet,
+    3 steps, gamma 5/3)."""
+    import ctypes as C
+    from oracle import resize_ref as RR
+    for kind, via in (("life", 96), ("life", 16384), ("hydro", 192), ("hydro", 4096)):
+        assert RR.check_identity(kind, via), (kind, via)
+    L = C.CDLL(RR.build("life", 96))
+    L.ref_life_run.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    init = oracle.life_bernoulli(96, 96, 3, 0.3, cyclic=False)
+    out = np.zeros((98, 98), np.int32)
+    pops = np.zeros(50, np.int32)
+    L.ref_life_run(init.ctypes.data, 50, out.ctypes.data, pops.ctypes.data)
+    rc, rp = oracle.life_run(init, 50, cyclic=False)
+    assert np.array_equal(out, rc) and np.array_equal(pops, rp)
+    H = C.CDLL(RR.build("hydro", 192))
+    H.ref_hydro_run.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_void_p, C.c_void_p]
+    out = np.zeros((4, 198, 198), np.float32)
+    H.ref_hydro_run(None, 3, C.c_float(0.5), out.ctypes.data, None)
+    st = oracle.hydro_init_jet(192, 192, cyclic=False, gamma=5 / 3, dtype=np.float32)
+    ref, _, _ = oracle.hydro_run(st, 3, cyclic=False, gamma=5 / 3, cfl=0.5, dtype=np.float32)
+    for a, b in zip(out, ref):
+        assert np.array_equal(a, b)
