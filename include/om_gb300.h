@@ -309,6 +309,12 @@ om_status om_graph_check(const char *text, int major, int minor, const char **so
 
 /* ---- caller-owned buffers, no allocation -------------------------------- */
 
+/* No counterpart in the reference.  Checks the bounded wait of the TMA
+ * kernels on `device`: a one-block kernel arms an mbarrier for bytes that no
+ * copy delivers (none is issued), waits with a short bound (about 4 ms) and
+ * must report the time-out through its error word.  OM_OK when it did. */
+om_status om_selftest_wait_bound(int device);
+
 /* Largest `generations` one om_life_proceed_noalloc call accepts. */
 #define OM_LIFE_NOALLOC_MAX_GENERATIONS 32
 

@@ -2,7 +2,9 @@
 // entry point (the runtime hands out the driver's cuTensorMapEncodeTiled, so
 // the library needs no link against the driver library).
 #include <mutex>
+#include <string>
 
+#include "om_internal.cuh"
 #include "tma.cuh"
 
 namespace om {
@@ -51,5 +53,51 @@ bool encode_tiled(CUtensorMap *map, CUtensorMapDataType type, int rank, void *ba
   return true;
 }
 
+// An mbarrier armed for 128 bytes that no copy delivers (none is issued, so
+// nothing is in flight): the bounded wait must give up and raise *err.
+__global__ void wait_bound_selftest_kernel(uint32_t *err, uint32_t polls) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    mbar_arrive_expect_tx(&bar, 128);
+    mbar_wait(&bar, 0, err, polls);
+  }
+}
+
 }  // namespace tma
 }  // namespace om
+
+using namespace om;
+
+// See include/om_gb300.h.
+extern "C" om_status om_selftest_wait_bound(int device) {
+  OM_CUDA_CHECK(cudaSetDevice(device));
+  uint32_t *err = nullptr;
+  if (cudaMalloc(&err, sizeof(uint32_t)) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("om_selftest_wait_bound: cannot allocate the error word");
+    return OM_ERR_NOMEM;
+  }
+  uint32_t h = 0;
+  cudaError_t e = cudaMemset(err, 0, sizeof(uint32_t));
+  // 200 polls of at most 20 us each: the wait gives up within about 4 ms
+  if (e == cudaSuccess) {
+    tma::wait_bound_selftest_kernel<<<1, 32>>>(err, 200);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(&h, err, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(err);
+  if (e != cudaSuccess) {
+    set_error(std::string("om_selftest_wait_bound: ") + cudaGetErrorString(e));
+    return OM_ERR_CUDA;
+  }
+  if (h != 1) {
+    set_error("om_selftest_wait_bound: the bounded wait did not report its time-out");
+    return OM_ERR_STATE;
+  }
+  return OM_OK;
+}

@@ -61,10 +61,11 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t by
 }
 
 // wait until the phase with parity `parity` of *bar has completed; false
-// (and *err raised) when the bound ran out
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t *err) {
+// (and *err raised) when `polls` polls ran out
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t *err,
+                                          uint32_t polls = kWaitPolls) {
   const uint32_t a = smem_addr(bar);
-  for (uint32_t i = 0; i < kWaitPolls; ++i) {
+  for (uint32_t i = 0; i < polls; ++i) {
     uint32_t done;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"

@@ -44,6 +44,7 @@ EXPORTS = [
     "om_autotune_ensemble", "om_hydro_vjp", "om_hydro_adjoint_run", "om_hydro_time_vjp",
     "om_hydro_time_tape", "om_hydro_forward", "om_hydro_backward", "om_hydro_tape_free", "om_create_graph",
     "om_graph_source", "om_graph_check", "om_save", "om_load", "om_hydro_write_snapshot",
+    "om_selftest_wait_bound",
 ]
 
 
@@ -130,6 +131,7 @@ def load_library(path: str | None = None) -> C.CDLL:
         "om_save": (i, [vp, C.c_char_p]),
         "om_load": (i, [vp, C.c_char_p]),
         "om_hydro_write_snapshot": (i, [vp, C.c_char_p]),
+        "om_selftest_wait_bound": (i, [i]),
         "om_profile_query": (i, [vp, C.c_char_p, C.POINTER(C.c_long), C.POINTER(C.c_double),
                                  C.POINTER(C.c_double)]),
     }

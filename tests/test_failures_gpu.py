@@ -1,7 +1,8 @@
 """Failure handling on the host side (no GPU fault is ever provoked): an
 allocation failure injected through OM_FAIL_ALLOC_AFTER surfaces as
 OM_ERR_NOMEM from every kind's constructor and leaves the device usable;
-non-finite states are reported by the totals."""
+non-finite states are reported by the totals; a bounded mbarrier wait that
+nothing completes gives up and reports through its error word."""
 import numpy as np
 import pytest
 
@@ -49,3 +50,16 @@ def test_nonfinite_state_is_reported(om_lib):
         h.totals()
     assert "non-finite" in str(e.value)
     h.close()
+
+
+def test_bounded_wait_reports_its_time_out(om_lib):
+    # an mbarrier armed for bytes that no copy delivers (no copy is issued):
+    # the wait the TMA kernels use gives up after its bound and raises the
+    # error word; the device stays usable
+    lib = om_lib.load_library()
+    assert lib.om_selftest_wait_bound(0) == 0, lib.om_last_error()
+    life = om_lib.Life((64, 64))
+    life.fill_random(2, 0.3)
+    life.proceed(3)
+    assert life.generation == 3
+    life.close()
