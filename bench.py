@@ -682,8 +682,7 @@ def adjoint_workload(args, dist: Dist) -> dict:
     T = args.adj_steps
     cells = n * n
     target = adjoint_target(n)
-    h = pg.Hydro((n, n), precision=args.adj_precision, gamma=1.4, device=dist.local_rank,
-                 **({"adj_fp64": 1} if args.adj_fp64 else {}))
+    h = pg.Hydro((n, n), precision=args.adj_precision, gamma=1.4, device=dist.local_rank)
     h.init_kh(1)
     h.set_scalar("cfl", 0.4)
     st0 = h.state()
@@ -761,7 +760,7 @@ def adjoint_workload(args, dist: Dist) -> dict:
     out = {
         "metric": ADJOINT_METRIC,
         "adjoint_precision": args.adj_precision,
-        "cotangent_accumulation": "fp64" if args.adj_fp64 else f"fp{args.adj_precision}",
+        "cotangent_accumulation": f"fp{args.adj_precision}",
         "tie_noise": args.tie_noise,
         "value": round(vjp_ms / fwd_ms, 3), "unit": "adjoint_step/forward_step",
         "higher_is_better": False, "n_gpus": dist.world, "steps": T, "warmup": args.warmup,
@@ -1146,8 +1145,6 @@ def main() -> int:
                              "ensemble", "adjoint"])
     ap.add_argument("--adj-steps", type=int, default=200)
     ap.add_argument("--adj-precision", type=int, default=32)
-    ap.add_argument("--adj-fp64", action="store_true",
-                    help="FP32 adjoint: accumulate cotangents in FP64 over the FP32 tape")
     ap.add_argument("--tie-noise", type=float, default=0.0)
     ap.add_argument("--fd-dirs", type=int, default=32)
     ap.add_argument("--fd-eps", type=float, nargs="+", default=[1e-3, 1e-5, 1e-7])
