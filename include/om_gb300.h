@@ -61,9 +61,12 @@ typedef struct {
   int device;       /* CUDA device ordinal */
   int depth;        /* Life: generations per temporally blocked launch (0 = tuned) */
   int tile_x;       /* Life: tile width in 32-cell words; Hydro: tile width in cells (0 = tuned) */
-  int tile_y;       /* tile height in cells (0 = tuned; Hydro FP32: 0 = 32 x 32, 8 and 16
-                       with tile_x 0 or 32, 8 and 16 with tile_x 64; a negative -k
-                       selects the column sweep of k rows per chunk, 8 or 16) */
+  int tile_y;       /* tile height in cells (0 = tuned; Hydro FP32: 0 = the persistent
+                       32 x 32 kernel on grids whose sides are multiples of 32 and
+                       at least 64, else the 32 x 32 tile kernel; 8, 16 and 32
+                       with tile_x 0 or 32, 8 and 16 with tile_x 64 are tile
+                       kernels; a negative -k selects the column sweep of k rows
+                       per chunk, 8 or 16) */
   int use_graph;    /* capture om_run_n in a CUDA graph (default 1) */
   int variant;      /* 0 = fastest path.  Life 1: integer one-cell-per-thread kernel only.
                        Hydro 1: plain unfused FP64-structured grid-stride kernels */
@@ -73,9 +76,9 @@ typedef struct {
                        TMA and need rows of at least 1024 cells); 0 = automatic:
                        with tile_y 0, that kernel on grids of at least 1.5 of its
                        tiles per SM, else register-resident blocks */
-  int grid_limit;   /* persistent kernels (Life warp-specialised, Hydro ensemble):
-                       at most this many CTAs (0 = as many as the GPU keeps
-                       resident) */
+  int grid_limit;   /* persistent kernels (Life warp-specialised, the persistent
+                       Hydro FP32 step, Hydro ensembles): at most this many
+                       CTAs (0 = as many as the GPU keeps resident) */
   int reserved[4];
 } om_config;
 

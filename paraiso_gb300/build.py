@@ -25,6 +25,7 @@ FILE_FLAGS = {
     "hydro_exact.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"],
     # the production FP32 step: approximate division/sqrt, flush-to-zero
     "hydro_fast.cu": ["-use_fast_math"],
+    "hydro_persist.cu": ["-use_fast_math"],
     # single-precision fast math only: the FP64 adjoint stays IEEE
     "adjoint.cu": ["-use_fast_math"],
 }

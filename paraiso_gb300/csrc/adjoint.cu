@@ -872,6 +872,7 @@ static om_status launch_tape(Handle *h, AdjointScratch *s, void *const *in, void
   a.lm = 0;
   a.ms0 = h->size[0];
   a.margin_min = nullptr;
+  a.grid_limit = h->cfg.grid_limit;
   OM_CUDA_CHECK(cudaMemsetAsync(&s->sc->tsmin[1 - read_slot], 0xFF, sizeof(unsigned long long),
                                 h->stream));
   const cudaError_t e = hydro_fused_tape(s->fp64, h->cfg.variant == 2, a, t, h->stream,

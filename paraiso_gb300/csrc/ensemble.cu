@@ -47,6 +47,9 @@ struct om_ensemble_s {
   HydroStepArgs *d_args[2] = {nullptr, nullptr};
   std::vector<int> prefix;
   int *d_prefix = nullptr;
+  // persistent kernel: 4 tensor maps per instance and buffer parity,
+  // [parity][instance][field]
+  CUtensorMap *d_maps = nullptr;
   bool ts_valid = false;
   int grid = 0;
   double *d_partials = nullptr, *d_totals = nullptr, *h_totals = nullptr;
@@ -107,7 +110,9 @@ static om_status ens_issue(om_ensemble E, int n) {
     cudaError_t e = E->fp64 ? hydro_ensemble_f64(E->d_args[E->cur], E->d_prefix, E->count,
                                                  E->tile, E->grid, E->stream)
                             : hydro_ensemble_f32(E->d_args[E->cur], E->d_prefix, E->count,
-                                                 E->tile, E->exact, E->grid, E->stream);
+                                                 E->tile, E->exact, E->grid, E->stream,
+                                                 E->d_maps ? E->d_maps + (size_t)E->cur * E->count * 4
+                                                           : nullptr);
     if (e != cudaSuccess) {
       set_error(std::string("ensemble step: ") + cudaGetErrorString(e));
       return OM_ERR_CUDA;
@@ -151,6 +156,9 @@ om_status om_ensemble_create(int count, const int *sizes, const om_config *cfg,
   E->exact = c.variant == 2 || E->fp64;
   E->tile = hydro_tile_of(c.tile_x, c.tile_y, !E->exact && !E->fp64);
   if (hydro_tile_is_sweep(E->tile)) E->tile = kTile32x32;  // items are tiles
+  if (E->tile == kPersist32x32)
+    for (int k = 0; k < count; ++k)
+      if (!hydro_persist_fits(sizes[2 * k], sizes[2 * k + 1])) E->tile = kTile32x32;
   hydro_tile_dims(E->tile, &E->tx, &E->ty);
   E->gamma = c.gamma;
   E->device = c.device;
@@ -224,6 +232,37 @@ om_status om_ensemble_create(int count, const int *sizes, const om_config *cfg,
     set_error("om_ensemble_create: upload failed");
     return OM_ERR_CUDA;
   }
+  if (E->tile == kPersist32x32) {
+    std::vector<CUtensorMap> maps((size_t)2 * count * 4);
+    for (int p = 0; p < 2 && st == OM_OK; ++p)
+      for (int k = 0; k < count && st == OM_OK; ++k) {
+        HydroStepArgs x{};
+        const size_t off = E->offset[k] * E->es;
+        x.rho = (char *)E->field[0][p] + off;
+        x.v0 = (char *)E->field[1][p] + off;
+        x.v1 = (char *)E->field[2][p] + off;
+        x.p = (char *)E->field[3][p] + off;
+        x.n0 = E->n0[k];
+        x.n1 = E->n1[k];
+        if (!hydro_persist_encode(&maps[((size_t)p * count + k) * 4], x)) {
+          set_error("om_ensemble_create: tensor map encoding failed");
+          st = OM_ERR_CUDA;
+        }
+      }
+    alloc((void **)&E->d_maps, sizeof(CUtensorMap) * maps.size());
+    if (st == OM_OK && cudaMemcpy(E->d_maps, maps.data(), sizeof(CUtensorMap) * maps.size(),
+                                  cudaMemcpyHostToDevice) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("om_ensemble_create: tensor map upload failed");
+      st = OM_ERR_CUDA;
+    }
+    if (st != OM_OK) {
+      std::string keep = om_last_error();
+      om_ensemble_destroy(E);
+      set_error(keep);
+      return st;
+    }
+  }
   const int occ = hydro_ensemble_occupancy(E->fp64, E->tile, E->exact);
   E->grid = std::max(1, std::min(occ * sm_count(E->device), E->prefix[count]));
   if (c.grid_limit > 0) E->grid = std::min(E->grid, c.grid_limit);
@@ -247,6 +286,7 @@ om_status om_ensemble_destroy(om_ensemble E) {
   cudaFree(E->d_args[0]);
   cudaFree(E->d_args[1]);
   cudaFree(E->d_prefix);
+  cudaFree(E->d_maps);
   cudaFree(E->d_partials);
   cudaFree(E->d_totals);
   if (E->h_sc) cudaFreeHost(E->h_sc);
@@ -310,6 +350,22 @@ static om_status ens_tsmin_all(om_ensemble E) {
   return OM_OK;
 }
 
+// after a run's scalar blocks came back: a kernel whose bounded wait for
+// its tensor copies ran out has raised wait_error (cleared here; the next
+// upload clears it on the device)
+static om_status ens_check_waits(om_ensemble E) {
+  bool raised = false;
+  for (int k = 0; k < E->count; ++k)
+    if (E->h_sc[k].wait_error) {
+      raised = true;
+      E->h_sc[k].wait_error = 0;
+    }
+  if (!raised) return OM_OK;
+  set_error("ensemble step: a kernel's bounded wait for its tensor copies ran out; the states "
+            "of this run are unspecified");
+  return OM_ERR_CUDA;
+}
+
 static om_status ens_run(om_ensemble E, int n, bool use_graph) {
   OM_CUDA_CHECK(cudaSetDevice(E->device));
   for (int k = 0; k < E->count; ++k) hydro_scalars_refresh(&E->h_sc[k]);
@@ -349,7 +405,7 @@ static om_status ens_run(om_ensemble E, int n, bool use_graph) {
   OM_CUDA_CHECK(cudaMemcpyAsync(E->h_sc, E->d_sc, sizeof(HydroScalars) * E->count,
                                 cudaMemcpyDeviceToHost, E->stream));
   OM_CUDA_CHECK(cudaStreamSynchronize(E->stream));
-  return OM_OK;
+  return ens_check_waits(E);
 }
 
 om_status om_ensemble_step(om_ensemble E, int n) {
@@ -380,7 +436,7 @@ om_status om_ensemble_time_step(om_ensemble E, int n, float *ms) {
   OM_CUDA_CHECK(cudaMemcpyAsync(E->h_sc, E->d_sc, sizeof(HydroScalars) * E->count,
                                 cudaMemcpyDeviceToHost, E->stream));
   OM_CUDA_CHECK(cudaStreamSynchronize(E->stream));
-  return OM_OK;
+  return ens_check_waits(E);
 }
 
 om_status om_ensemble_read(om_ensemble E, int k, const char *name, void *dst, size_t bytes) {

@@ -127,9 +127,12 @@ static om_status proceed_fused(Handle *h, int n) {
   HydroState *st = hst(h);
   OM_TRY(ensure_tsmin(h));
   const double cells = (double)h->size[0] * h->size[1];
+  const bool persist = !st->fp64 && st->variant != 2 && st->lm == 0 &&
+                       st->tile == kPersist32x32 && hydro_persist_fits(h->size[0], h->size[1]);
   const char *kname = st->fp64 ? "hydro_fused_kernel_f64"
-                               : (st->variant == 2 ? "hydro_fused_kernel_f32_exact"
-                                                   : "hydro_fused_kernel_f32");
+                      : st->variant == 2 ? "hydro_fused_kernel_f32_exact"
+                      : persist          ? "hydro_persist_kernel"
+                                         : "hydro_fused_kernel_f32";
   for (int k = 0; k < n; ++k) {
     OM_CUDA_CHECK(cudaMemsetAsync(&hsc_dev(h)->tsmin[1 - st->slot], 0xFF,
                                   sizeof(unsigned long long), h->stream));
@@ -148,6 +151,7 @@ static om_status proceed_fused(Handle *h, int n) {
     a.lm = st->lm;
     a.ms0 = (int)h->memory_size(0);
     a.margin_min = st->d_margin;
+    a.grid_limit = h->cfg.grid_limit;
     cudaEvent_t ev = prof_begin(h);
     cudaError_t e = st->fp64 ? hydro_fused_f64(a, st->tile, h->stream, nullptr)
                              : hydro_fused_f32(a, st->tile, st->variant == 2, h->stream, nullptr);
@@ -413,6 +417,14 @@ om_status hydro_setup(Handle *h) {
   h->ops.save_state = hydro_save_state;
   h->ops.load_state = hydro_load_state;
   h->ops.before_upload = [](Handle *hh) { hydro_scalars_refresh(hsc_host(hh)); };
+  h->ops.after_run = [](Handle *hh) -> om_status {
+    HydroScalars *sc = hsc_host(hh);
+    if (!sc->wait_error) return OM_OK;
+    sc->wait_error = 0;  // cleared on the device by the next upload
+    set_error("Hydro: a kernel's bounded wait for its tensor copies ran out; the state of this "
+              "run is unspecified");
+    return OM_ERR_CUDA;
+  };
   const int es = st->fp64 ? 8 : 4;
   OM_TRY(alloc_array(h, "density", es));
   OM_TRY(alloc_array(h, "velocity0", es));

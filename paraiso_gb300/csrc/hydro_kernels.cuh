@@ -25,6 +25,8 @@ struct HydroScalars {
   // per-thread conversion from double; (float)x is the same rounding either
   // side
   float cfl_f, dR0_f, dR1_f, ext1_f;
+  // raised by a kernel whose bounded wait for its tensor copies ran out
+  uint32_t wait_error;
 };
 
 // the float copies of a scalar block (host side, before every upload)
@@ -49,6 +51,9 @@ struct HydroStepArgs {
   // (n0 + 2 lm) and the CFL timescale minimum of the margin cells
   int lm, ms0;
   const unsigned long long *margin_min;
+  // persistent kernels: at most this many CTAs (0 = as many as stay
+  // resident); read by the host launcher only
+  int grid_limit;
 };
 
 // What a taped step keeps for the reverse sweep (periodic grids; arrays of

@@ -1,0 +1,96 @@
+// hydro_persist.cu -- launchers of the persistent production FP32 step
+// (hydro_persist.cuh): single grids (plain and taped) and ensembles.
+// Compiled with the production build's fast single-precision math, like
+// hydro_fast.cu, so the two tile codes give the same bits.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "hydro_launch.cuh"
+#include "hydro_persist.cuh"
+#include "om_internal.cuh"
+
+namespace om {
+
+bool hydro_persist_fits(int n0, int n1) {
+  return n0 % hp::TX == 0 && n1 % hp::TY == 0 && n0 >= 2 * hp::TX && n1 >= 2 * hp::TY;
+}
+
+// one field of an n0 x n1 FP32 grid as a 2-D tensor of 40 x 38 boxes
+static bool encode_field(CUtensorMap *m, const void *base, int n0, int n1) {
+  const uint64_t dims[2] = {(uint64_t)n0, (uint64_t)n1};
+  const uint64_t strides[1] = {(uint64_t)n0 * sizeof(float)};
+  const uint32_t box[2] = {(uint32_t)hp::BW, (uint32_t)hp::BH};
+  return tma::encode_tiled(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void *>(base), dims,
+                           strides, box, CU_TENSOR_MAP_SWIZZLE_NONE);
+}
+
+bool hydro_persist_encode(CUtensorMap *maps4, const HydroStepArgs &a) {
+  const void *f[4] = {a.rho, a.v0, a.v1, a.p};
+  for (int k = 0; k < 4; ++k)
+    if (!encode_field(&maps4[k], f[k], a.n0, a.n1)) return false;
+  return true;
+}
+
+template <class K> static int resident_per_sm(K kernel) {
+  const int smem = (int)sizeof(hp::Smem);
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, hp::NT, smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+int hydro_persist_occupancy() {
+  static int n = -1;
+  if (n < 0) n = resident_per_sm(hp::hydro_persist_ensemble_kernel);
+  return n > 0 ? n : 1;
+}
+
+template <bool TAPE>
+static cudaError_t persist_launch(const HydroStepArgs &a0, const HydroTapeOut *tape,
+                                  cudaStream_t s, int *grid_out) {
+  static int occ = -1;
+  if (occ < 0) occ = resident_per_sm(hp::hydro_persist_kernel<TAPE>);
+  if (occ <= 0) return cudaErrorInvalidConfiguration;
+  HydroStepArgs a = a0;
+  a.nt0 = a.n0 / hp::TX;
+  CUtensorMap m[4];
+  if (!hydro_persist_encode(m, a)) return cudaErrorInvalidValue;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const int tiles = a.nt0 * (a.n1 / hp::TY);
+  int grid = std::min(tiles, occ * sm_count(dev));
+  if (a.grid_limit > 0) grid = std::min(grid, a.grid_limit);
+  HydroTapeOut t{};
+  if (tape) t = *tape;
+  hp::hydro_persist_kernel<TAPE><<<grid, hp::NT, sizeof(hp::Smem), s>>>(a, m[0], m[1], m[2], m[3],
+                                                                        t);
+  if (grid_out) *grid_out = grid;
+  return cudaGetLastError();
+}
+
+cudaError_t hydro_persist_step(const HydroStepArgs &a, cudaStream_t s, int *grid_out) {
+  return persist_launch<false>(a, nullptr, s, grid_out);
+}
+
+cudaError_t hydro_persist_tape(const HydroStepArgs &a, const HydroTapeOut &t, cudaStream_t s) {
+  return persist_launch<true>(a, &t, s, nullptr);
+}
+
+cudaError_t hydro_persist_ensemble(const HydroStepArgs *args, const int *prefix, int count,
+                                   const CUtensorMap *table, int grid, cudaStream_t s) {
+  if (hydro_persist_occupancy() < 1) return cudaErrorInvalidConfiguration;
+  hp::hydro_persist_ensemble_kernel<<<grid, hp::NT, sizeof(hp::Smem), s>>>(args, prefix, count,
+                                                                          table);
+  return cudaGetLastError();
+}
+
+}  // namespace om

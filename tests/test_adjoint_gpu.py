@@ -168,14 +168,14 @@ def test_backward_rejects_foreign_tape(om_lib, oracle):
     b.close()
 
 
-@pytest.mark.parametrize("precision", [32, 64])
-def test_segment_tapes_match_retaping(om_lib, oracle, monkeypatch, precision):
+@pytest.mark.parametrize("precision,size", [(32, (64, 48)), (64, (64, 48)), (32, (128, 96))])
+def test_segment_tapes_match_retaping(om_lib, oracle, monkeypatch, precision, size):
     # The backward pass recomputes each segment with the taped step, keeping
     # one tape per step; when those tapes cannot be allocated it recomputes
     # with the plain step and tapes each step again before its reverse.  The
     # taped step writes the same states as the plain one, so both paths give
-    # the same gradient bit for bit.
-    size = (64, 48)
+    # the same gradient bit for bit.  128 x 96 FP32 runs the persistent
+    # 32 x 32 kernel (plain and taped), 64 x 48 the tile kernels.
     steps = 9
     st = noisy_kh(oracle, size, 21)
     if precision == 32:
