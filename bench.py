@@ -418,11 +418,10 @@ def hydro_workload(args, dist: Dist) -> dict:
     # dominant kernel per launch
     h.profile(True)
     h.time_run("proceed", min(args.steps, 10))
-    kname = "hydro_persist_kernel"
-    nl, kms, _ = h.profile_query(kname)
-    if nl == 0:
-        kname = "hydro_fused_kernel_f32"
+    for kname in ("hydro_pair_kernel", "hydro_persist_kernel", "hydro_fused_kernel_f32"):
         nl, kms, _ = h.profile_query(kname)
+        if nl > 0:
+            break
     h.profile(False)
     peak, peak_kind = peaks()
     per_launch_ms = kms / max(nl, 1)

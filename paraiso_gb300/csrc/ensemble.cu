@@ -156,7 +156,7 @@ om_status om_ensemble_create(int count, const int *sizes, const om_config *cfg,
   E->exact = c.variant == 2 || E->fp64;
   E->tile = hydro_tile_of(c.tile_x, c.tile_y, !E->exact && !E->fp64);
   if (hydro_tile_is_sweep(E->tile)) E->tile = kTile32x32;  // items are tiles
-  if (E->tile == kPersist32x32)
+  if (hydro_tile_is_persistent(E->tile))
     for (int k = 0; k < count; ++k)
       if (!hydro_persist_fits(sizes[2 * k], sizes[2 * k + 1])) E->tile = kTile32x32;
   hydro_tile_dims(E->tile, &E->tx, &E->ty);
@@ -232,7 +232,7 @@ om_status om_ensemble_create(int count, const int *sizes, const om_config *cfg,
     set_error("om_ensemble_create: upload failed");
     return OM_ERR_CUDA;
   }
-  if (E->tile == kPersist32x32) {
+  if (hydro_tile_is_persistent(E->tile)) {
     std::vector<CUtensorMap> maps((size_t)2 * count * 4);
     for (int p = 0; p < 2 && st == OM_OK; ++p)
       for (int k = 0; k < count && st == OM_OK; ++k) {

@@ -128,10 +128,12 @@ static om_status proceed_fused(Handle *h, int n) {
   OM_TRY(ensure_tsmin(h));
   const double cells = (double)h->size[0] * h->size[1];
   const bool persist = !st->fp64 && st->variant != 2 && st->lm == 0 &&
-                       st->tile == kPersist32x32 && hydro_persist_fits(h->size[0], h->size[1]);
+                       hydro_tile_is_persistent(st->tile) &&
+                       hydro_persist_fits(h->size[0], h->size[1]);
   const char *kname = st->fp64 ? "hydro_fused_kernel_f64"
                       : st->variant == 2 ? "hydro_fused_kernel_f32_exact"
-                      : persist          ? "hydro_persist_kernel"
+                      : persist          ? (st->tile == kPair32x32 ? "hydro_pair_kernel"
+                                                                       : "hydro_persist_kernel")
                                          : "hydro_fused_kernel_f32";
   for (int k = 0; k < n; ++k) {
     OM_CUDA_CHECK(cudaMemsetAsync(&hsc_dev(h)->tsmin[1 - st->slot], 0xFF,

@@ -197,8 +197,22 @@ template <bool FA, int AX, class R>
 __device__ __forceinline__ hs::Flux<R> wall_flux(R g, const hf::Consts<R> &k,
                                                  const hs::Prim<R> &L, R cl,
                                                  const hs::Prim<R> &Rt, R cr) {
-  if (FA) return hf::hllc<AX>(k, L, cl, Rt, cr);
-  return hs::hllc<AX>(g, L, cl, Rt, cr);
+  if constexpr (FA) return hf::hllc<AX>(k, L, cl, Rt, cr);
+  else return hs::hllc<AX>(g, L, cl, Rt, cr);
+}
+
+// MUSCL face values in the exact or the production algebra
+template <bool FA, class R>
+__device__ __forceinline__ void muscl(R x0, R x1, R x2, R x3, R &l, R &r) {
+  if constexpr (FA) hf::muscl(x0, x1, x2, x3, l, r);
+  else hs::muscl(x0, x1, x2, x3, l, r);
+}
+
+// sound speed of a state in the exact or the production algebra
+template <bool FA, class R>
+__device__ __forceinline__ R face_sound(R g, const hf::Consts<R> &k, R rho, R p) {
+  if constexpr (FA) return hf::sound(k, rho, p);
+  else return hs::sound(g, rho, p);
 }
 
 template <bool FA, class R>
@@ -207,8 +221,8 @@ __device__ __forceinline__ hs::Prim<R> cell_update(R g, const hf::Consts<R> &k,
                                                    const hs::Flux<R> &l0, const hs::Flux<R> &r0,
                                                    const hs::Flux<R> &l1, const hs::Flux<R> &r1,
                                                    R *cons = nullptr) {
-  if (FA) return hf::update(k, b, dtdx0, dtdx1, l0, r0, l1, r1, cons);
-  return hs::update(g, b, dtdx0, dtdx1, l0, r0, l1, r1, cons);
+  if constexpr (FA) return hf::update(k, b, dtdx0, dtdx1, l0, r0, l1, r1, cons);
+  else return hs::update(g, b, dtdx0, dtdx1, l0, r0, l1, r1, cons);
 }
 
 }  // namespace hk
@@ -301,7 +315,7 @@ __device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
     s.P[1][py][px] = u;
     s.P[2][py][px] = v;
     s.P[3][py][px] = q;
-    s.C[py][px] = hs::sound(g, r, q);
+    s.C[py][px] = hk::face_sound<FA>(g, K, r, q);
   }
   __syncthreads();
 
@@ -370,13 +384,13 @@ __device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
 #pragma unroll
         for (int f = 0; f < 4; ++f) {
           R l, r;
-          hs::muscl(s.Q[f][qy][sx], s.Q[f][qy][sx + 1], s.Q[f][qy][sx + 2], s.Q[f][qy][sx + 3],
+          hk::muscl<FA>(s.Q[f][qy][sx], s.Q[f][qy][sx + 1], s.Q[f][qy][sx + 2], s.Q[f][qy][sx + 3],
                     l, r);
           (&L.rho)[f] = l;
           (&Rt.rho)[f] = r;
         }
-        s.fx[i] = hk::wall_flux<FA, 0>(g, K, L, hs::sound(g, L.rho, L.p), Rt,
-                                       hs::sound(g, Rt.rho, Rt.p));
+        s.fx[i] = hk::wall_flux<FA, 0>(g, K, L, hk::face_sound<FA>(g, K, L.rho, L.p), Rt,
+                                       hk::face_sound<FA>(g, K, Rt.rho, Rt.p));
       } else {
         const int j = i - NX;
         const int sy = j / TX, sx = j - sy * TX;
@@ -384,13 +398,13 @@ __device__ __forceinline__ void fused_tile(const HydroStepArgs &a, int tile,
 #pragma unroll
         for (int f = 0; f < 4; ++f) {
           R l, r;
-          hs::muscl(s.Q[f][sy][qx], s.Q[f][sy + 1][qx], s.Q[f][sy + 2][qx], s.Q[f][sy + 3][qx],
+          hk::muscl<FA>(s.Q[f][sy][qx], s.Q[f][sy + 1][qx], s.Q[f][sy + 2][qx], s.Q[f][sy + 3][qx],
                     l, r);
           (&L.rho)[f] = l;
           (&Rt.rho)[f] = r;
         }
-        s.fy[j] = hk::wall_flux<FA, 1>(g, K, L, hs::sound(g, L.rho, L.p), Rt,
-                                       hs::sound(g, Rt.rho, Rt.p));
+        s.fy[j] = hk::wall_flux<FA, 1>(g, K, L, hk::face_sound<FA>(g, K, L.rho, L.p), Rt,
+                                       hk::face_sound<FA>(g, K, Rt.rho, Rt.p));
       }
     }
   }

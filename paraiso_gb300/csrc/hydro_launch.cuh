@@ -14,19 +14,26 @@ namespace om {
 // Tile shapes of the fused kernel available to the tuner (FP32 production
 // build; FP64 and the exact FP32 variant run 32x16).
 // The sweep shapes (kSweep*) walk strips of TX columns down the grid in
-// chunks of TY rows (hydro_sweep.cuh).  kPersist32x32 is the persistent
-// 32 x 32 kernel with prefetched boxes (hydro_persist.cuh) on grids whose
-// sides are multiples of 32 and at least 64, else the 32 x 32 tile kernel.
+// chunks of TY rows (hydro_sweep.cuh).  kPersist32x32 and kPair32x32 are
+// the persistent 32 x 32 kernel with prefetched boxes (hydro_persist.cuh),
+// one wall or cell per thread or two with packed f32x2 instructions, on
+// grids whose sides are multiples of 32 and at least 64, else the 32 x 32
+// tile kernel.
 enum HydroTile {
   kTile32x8 = 0, kTile32x16 = 1, kTile64x16 = 2, kTile32x32 = 3, kTile64x8 = 4,
-  kSweep32x8 = 5, kSweep32x16 = 6, kSweep64x8 = 7, kPersist32x32 = 8, kTileCount = 9
+  kSweep32x8 = 5, kSweep32x16 = 6, kSweep64x8 = 7, kPersist32x32 = 8, kPair32x32 = 9,
+  kTileCount = 10
 };
+inline bool hydro_tile_is_persistent(int tile) {
+  return tile == kPersist32x32 || tile == kPair32x32;
+}
 inline bool hydro_tile_is_sweep(int tile) { return tile >= kSweep32x8 && tile <= kSweep64x8; }
 void hydro_tile_dims(int tile, int *tx, int *ty);
 // the tile a configuration's tile_x / tile_y select (0 = default): x 64
 // with y 8 is 64x8, else 64x16; x 0 or 32 with y 8, 16 or 32 is 32x8,
-// 32x16 or the 32x32 tile kernel, with y 0 (the production default) the
-// persistent 32 x 32 kernel.
+// 32x16 or the 32x32 tile kernel; with y 0 the persistent 32 x 32 kernel,
+// x 0 (the production default) in the paired form, x 32 one wall or cell
+// per thread.
 // A negative tile_y selects a sweep of -tile_y rows per chunk (x 32 or 64).
 inline int hydro_tile_of(int tile_x, int tile_y, bool production) {
   if (!production) return kTile32x16;
@@ -38,7 +45,7 @@ inline int hydro_tile_of(int tile_x, int tile_y, bool production) {
   if (tile_y == 8) return kTile32x8;
   if (tile_y == 16) return kTile32x16;
   if (tile_y == 32) return kTile32x32;
-  return kPersist32x32;
+  return tile_x == 32 ? kPersist32x32 : kPair32x32;
 }
 
 // fused two-stage step; `exact` selects the no-contraction build
@@ -51,9 +58,9 @@ cudaError_t hydro_fused_tape(int fp64, bool exact, const HydroStepArgs &a, const
                              cudaStream_t s, int tile);
 
 // ensemble step over every instance (persistent grid of `grid` blocks, 0 =
-// resident blocks x SMs); args/prefix in device memory.  kPersist32x32
-// takes `table` (4 tensor maps per instance, hydro_persist_encode of the
-// instance's args) and falls back to the 32 x 32 tile kernel without one.
+// resident blocks x SMs); args/prefix in device memory.  The persistent
+// tiles take `table` (4 tensor maps per instance, hydro_persist_encode of
+// the instance's args) and fall back to the 32 x 32 tile kernel without one.
 cudaError_t hydro_ensemble_f32(const HydroStepArgs *args, const int *prefix, int count, int tile,
                                bool exact, int grid, cudaStream_t s,
                                const CUtensorMap *table = nullptr);
@@ -63,11 +70,13 @@ cudaError_t hydro_ensemble_f32(const HydroStepArgs *args, const int *prefix, int
 bool hydro_persist_fits(int n0, int n1);
 // the four field tensor maps of a's current state
 bool hydro_persist_encode(CUtensorMap *maps4, const HydroStepArgs &a);
-int hydro_persist_occupancy();
-cudaError_t hydro_persist_step(const HydroStepArgs &a, cudaStream_t s, int *grid_out);
-cudaError_t hydro_persist_tape(const HydroStepArgs &a, const HydroTapeOut &t, cudaStream_t s);
+int hydro_persist_occupancy(bool pair);
+cudaError_t hydro_persist_step(const HydroStepArgs &a, bool pair, cudaStream_t s, int *grid_out);
+cudaError_t hydro_persist_tape(const HydroStepArgs &a, bool pair, const HydroTapeOut &t,
+                               cudaStream_t s);
 cudaError_t hydro_persist_ensemble(const HydroStepArgs *args, const int *prefix, int count,
-                                   const CUtensorMap *table, int grid, cudaStream_t s);
+                                   const CUtensorMap *table, bool pair, int grid,
+                                   cudaStream_t s);
 cudaError_t hydro_ensemble_f64(const HydroStepArgs *args, const int *prefix, int count, int tile,
                                int grid, cudaStream_t s);
 // resident blocks per SM of the ensemble kernel for (fp64, tile, exact)

@@ -33,7 +33,7 @@ bool hydro_persist_encode(CUtensorMap *maps4, const HydroStepArgs &a) {
   return true;
 }
 
-template <class K> static int resident_per_sm(K kernel) {
+template <class K> static int resident_per_sm(K kernel, int threads) {
   const int smem = (int)sizeof(hp::Smem);
   if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
       cudaSuccess) {
@@ -41,24 +41,29 @@ template <class K> static int resident_per_sm(K kernel) {
     return 0;
   }
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, hp::NT, smem) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
   return n;
 }
 
-int hydro_persist_occupancy() {
-  static int n = -1;
-  if (n < 0) n = resident_per_sm(hp::hydro_persist_ensemble_kernel);
-  return n > 0 ? n : 1;
+int hydro_persist_occupancy(bool pair) {
+  static int n[2] = {-1, -1};
+  int &v = n[pair ? 1 : 0];
+  if (v < 0)
+    v = pair ? resident_per_sm(hp::hydro_persist_ensemble_kernel<true>, hp::NT2)
+             : resident_per_sm(hp::hydro_persist_ensemble_kernel<false>, hp::NT);
+  return v > 0 ? v : 1;
 }
 
-template <bool TAPE>
+template <bool TAPE, bool PAIR>
 static cudaError_t persist_launch(const HydroStepArgs &a0, const HydroTapeOut *tape,
                                   cudaStream_t s, int *grid_out) {
+  auto kernel = PAIR ? hp::hydro_pair_kernel<TAPE> : hp::hydro_persist_kernel<TAPE>;
+  const int threads = PAIR ? hp::NT2 : hp::NT;
   static int occ = -1;
-  if (occ < 0) occ = resident_per_sm(hp::hydro_persist_kernel<TAPE>);
+  if (occ < 0) occ = resident_per_sm(kernel, threads);
   if (occ <= 0) return cudaErrorInvalidConfiguration;
   HydroStepArgs a = a0;
   a.nt0 = a.n0 / hp::TX;
@@ -71,25 +76,32 @@ static cudaError_t persist_launch(const HydroStepArgs &a0, const HydroTapeOut *t
   if (a.grid_limit > 0) grid = std::min(grid, a.grid_limit);
   HydroTapeOut t{};
   if (tape) t = *tape;
-  hp::hydro_persist_kernel<TAPE><<<grid, hp::NT, sizeof(hp::Smem), s>>>(a, m[0], m[1], m[2], m[3],
-                                                                        t);
+  kernel<<<grid, threads, sizeof(hp::Smem), s>>>(a, m[0], m[1], m[2], m[3], t);
   if (grid_out) *grid_out = grid;
   return cudaGetLastError();
 }
 
-cudaError_t hydro_persist_step(const HydroStepArgs &a, cudaStream_t s, int *grid_out) {
-  return persist_launch<false>(a, nullptr, s, grid_out);
+cudaError_t hydro_persist_step(const HydroStepArgs &a, bool pair, cudaStream_t s, int *grid_out) {
+  return pair ? persist_launch<false, true>(a, nullptr, s, grid_out)
+              : persist_launch<false, false>(a, nullptr, s, grid_out);
 }
 
-cudaError_t hydro_persist_tape(const HydroStepArgs &a, const HydroTapeOut &t, cudaStream_t s) {
-  return persist_launch<true>(a, &t, s, nullptr);
+cudaError_t hydro_persist_tape(const HydroStepArgs &a, bool pair, const HydroTapeOut &t,
+                               cudaStream_t s) {
+  return pair ? persist_launch<true, true>(a, &t, s, nullptr)
+              : persist_launch<true, false>(a, &t, s, nullptr);
 }
 
 cudaError_t hydro_persist_ensemble(const HydroStepArgs *args, const int *prefix, int count,
-                                   const CUtensorMap *table, int grid, cudaStream_t s) {
-  if (hydro_persist_occupancy() < 1) return cudaErrorInvalidConfiguration;
-  hp::hydro_persist_ensemble_kernel<<<grid, hp::NT, sizeof(hp::Smem), s>>>(args, prefix, count,
-                                                                          table);
+                                   const CUtensorMap *table, bool pair, int grid,
+                                   cudaStream_t s) {
+  if (hydro_persist_occupancy(pair) < 1) return cudaErrorInvalidConfiguration;
+  if (pair)
+    hp::hydro_persist_ensemble_kernel<true><<<grid, hp::NT2, sizeof(hp::Smem), s>>>(
+        args, prefix, count, table);
+  else
+    hp::hydro_persist_ensemble_kernel<false><<<grid, hp::NT, sizeof(hp::Smem), s>>>(
+        args, prefix, count, table);
   return cudaGetLastError();
 }
 

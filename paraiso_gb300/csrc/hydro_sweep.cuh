@@ -87,7 +87,7 @@ __device__ __forceinline__ void sweep_segment(const HydroStepArgs &a, int X0, in
     for (int i = tid; i < TY * S::PX; i += NT) {
       const int ry = i / S::PX, px = i - ry * S::PX;
       const int sy = (k % 3) * TY + ry;
-      s.C[sy][px] = hs::sound(g, s.P[0][sy][px], s.P[3][sy][px]);
+      s.C[sy][px] = hk::face_sound<FA>(g, K, s.P[0][sy][px], s.P[3][sy][px]);
     }
   };
   auto pslot = [&](int y) { return (y - ya + 3) % S::RP; };
@@ -179,13 +179,14 @@ __device__ __forceinline__ void sweep_segment(const HydroStepArgs &a, int X0, in
 #pragma unroll
           for (int f = 0; f < 4; ++f) {
             R l, r;
-            hs::muscl(s.Q[f][sq][sx], s.Q[f][sq][sx + 1], s.Q[f][sq][sx + 2], s.Q[f][sq][sx + 3],
+            hk::muscl<FA>(s.Q[f][sq][sx], s.Q[f][sq][sx + 1], s.Q[f][sq][sx + 2],
+                          s.Q[f][sq][sx + 3],
                       l, r);
             (&L.rho)[f] = l;
             (&Rt.rho)[f] = r;
           }
-          s.s2x[ry][sx] = hk::wall_flux<FA, 0>(g, K, L, hs::sound(g, L.rho, L.p), Rt,
-                                               hs::sound(g, Rt.rho, Rt.p));
+          s.s2x[ry][sx] = hk::wall_flux<FA, 0>(g, K, L, hk::face_sound<FA>(g, K, L.rho, L.p),
+                                               Rt, hk::face_sound<FA>(g, K, Rt.rho, Rt.p));
         } else {
           const int j = i - NX;
           const int ry = j / W2, cx = j - ry * W2;
@@ -195,12 +196,13 @@ __device__ __forceinline__ void sweep_segment(const HydroStepArgs &a, int X0, in
 #pragma unroll
           for (int f = 0; f < 4; ++f) {
             R l, r;
-            hs::muscl(s.Q[f][a0][qx], s.Q[f][a1][qx], s.Q[f][a2][qx], s.Q[f][a3][qx], l, r);
+            hk::muscl<FA>(s.Q[f][a0][qx], s.Q[f][a1][qx], s.Q[f][a2][qx], s.Q[f][a3][qx], l, r);
             (&L.rho)[f] = l;
             (&Rt.rho)[f] = r;
           }
           s.s2y[sw::slot<S::RY2>(y)][cx] = hk::wall_flux<FA, 1>(
-              g, K, L, hs::sound(g, L.rho, L.p), Rt, hs::sound(g, Rt.rho, Rt.p));
+              g, K, L, hk::face_sound<FA>(g, K, L.rho, L.p), Rt,
+              hk::face_sound<FA>(g, K, Rt.rho, Rt.p));
         }
       }
     }

@@ -17,8 +17,8 @@ def noisy_kh(oracle, size, seed, amp=1e-3):
                  for a in oracle.hydro_init_kh(size[0], size[1], seed))
 
 
-def make(pg, size, precision):
-    h = pg.Hydro(size, precision=precision, gamma=GAMMA)
+def make(pg, size, precision, **kw):
+    h = pg.Hydro(size, precision=precision, gamma=GAMMA, **kw)
     h.set_scalar("cfl", CFL)
     h.set_scalar("dR0", 1.0 / size[0])
     h.set_scalar("dR1", 1.0 / size[1])
@@ -168,14 +168,16 @@ def test_backward_rejects_foreign_tape(om_lib, oracle):
     b.close()
 
 
-@pytest.mark.parametrize("precision,size", [(32, (64, 48)), (64, (64, 48)), (32, (128, 96))])
-def test_segment_tapes_match_retaping(om_lib, oracle, monkeypatch, precision, size):
+@pytest.mark.parametrize("precision,size,tile", [(32, (64, 48), 0), (64, (64, 48), 0),
+                                                 (32, (128, 96), 0), (32, (128, 96), 32)])
+def test_segment_tapes_match_retaping(om_lib, oracle, monkeypatch, precision, size, tile):
     # The backward pass recomputes each segment with the taped step, keeping
     # one tape per step; when those tapes cannot be allocated it recomputes
     # with the plain step and tapes each step again before its reverse.  The
     # taped step writes the same states as the plain one, so both paths give
     # the same gradient bit for bit.  128 x 96 FP32 runs the persistent
-    # 32 x 32 kernel (plain and taped), 64 x 48 the tile kernels.
+    # 32 x 32 kernel (plain and taped; paired with tile_x 0, one wall per
+    # thread with tile_x 32), 64 x 48 the tile kernels.
     steps = 9
     st = noisy_kh(oracle, size, 21)
     if precision == 32:
@@ -184,7 +186,7 @@ def test_segment_tapes_match_retaping(om_lib, oracle, monkeypatch, precision, si
     cot = tuple(rng.standard_normal(a.shape).astype(st[0].dtype) for a in st)
     grads = []
     for retape in (False, True):
-        h = make(om_lib, size, precision)
+        h = make(om_lib, size, precision, tile_x=tile)
         h.set_state(st)
         if retape:
             monkeypatch.setenv("OM_FAIL_ALLOC_AFTER", "0")

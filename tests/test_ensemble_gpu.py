@@ -48,12 +48,13 @@ def test_ensemble_bit_exact_per_instance(om_lib, oracle, precision, variant):
     e.close()
 
 
-@pytest.mark.parametrize("tile", [(0, 0), (0, 32), (0, 16)])
+@pytest.mark.parametrize("tile", [(0, 0), (32, 0), (0, 32), (0, 16)])
 def test_ensemble_fast_matches_single_grids(om_lib, tile):
-    # (0, 0): the persistent 32 x 32 kernel, each item's box prefetched
-    # (TMA inside an instance, wrapped copies at its edges) while the block
-    # computes the item before; (0, 32) and (0, 16): tile kernels; small
-    # instances: every block walks several instances
+    # (0, 0) and (32, 0): the persistent 32 x 32 kernel, paired and one wall
+    # per thread, each item's box prefetched (TMA inside an instance,
+    # wrapped copies at its edges) while the block computes the item before;
+    # (0, 32) and (0, 16): tile kernels; small instances: every block walks
+    # several instances
     sizes = om_lib.ensemble_sizes(5, 42, lo=64, hi=320)
     e = om_lib.Ensemble(sizes, precision=32, gamma=GAMMA, tile_x=tile[0], tile_y=tile[1],
                         grid_limit=7)

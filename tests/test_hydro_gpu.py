@@ -67,8 +67,8 @@ def test_fp32_exact_variants_bit_exact(om_lib, oracle, size, variant):
     h.close()
 
 
-@pytest.mark.parametrize("tile", [(0, 0), (0, 32), (0, 8), (0, 16), (64, 0), (64, 8), (0, -8),
-                                  (0, -16), (64, -8)])
+@pytest.mark.parametrize("tile", [(0, 0), (32, 0), (0, 32), (0, 8), (0, 16), (64, 0), (64, 8),
+                                  (0, -8), (0, -16), (64, -8)])
 def test_fp32_fast_against_fp64(om_lib, oracle, tile):
     size = (128, 96)
     st64 = kh_state(oracle, size, 5, np.float64)
@@ -231,18 +231,21 @@ def test_sweep_matches_tile_kernel(om_lib, oracle, size, sweep):
 def test_persistent_matches_tile_kernel(om_lib, oracle, size, limit):
     """The persistent 32 x 32 kernel (each CTA walks several tiles; the next
     tile's box is prefetched by TMA inside the grid and by wrapped 16-byte
-    copies at its edges; stage-2 walls in runs of three) forms every value
-    with the tile kernel's operations: the two production FP32 paths agree
-    bit for bit.  grid_limit forces several tiles per CTA on small grids;
-    100 x 96 (not a multiple of 32) runs the tile kernel under both."""
+    copies at its edges; stage-2 walls in runs of three), in its paired form
+    (0, 0: two walls or cells per thread with packed f32x2 instructions) and
+    with one wall per thread (32, 0), forms every value with the tile
+    kernel's operations: the production FP32 paths agree bit for bit.
+    grid_limit forces several tiles per CTA on small grids; 100 x 96 (not a
+    multiple of 32) runs the tile kernel under all three."""
     st = kh_state(oracle, size, 13, np.float32)
     out = []
-    for tx, ty in ((0, 0), (0, 32)):
+    for tx, ty in ((0, 0), (32, 0), (0, 32)):
         h = make(om_lib, size, 32, 0, tile_x=tx, tile_y=ty, grid_limit=limit)
         h.set_state(st)
         h.proceed(7)
         out.append((h.state(), h.dt_history(7), h.get_scalar("time")))
         h.close()
-    for a, b in zip(out[0][0], out[1][0]):
-        assert np.array_equal(a, b)
-    assert np.array_equal(out[0][1], out[1][1]) and out[0][2] == out[1][2]
+    for o in out[1:]:
+        for a, b in zip(out[0][0], o[0]):
+            assert np.array_equal(a, b)
+        assert np.array_equal(out[0][1], o[1]) and out[0][2] == o[2]
