@@ -102,6 +102,48 @@ def peak_source(kind: str) -> str:
             else "fallback 6.8 TB/s (MEASURED_PEAKS.json absent)")
 
 
+class NearGpu:
+    """Within the block, this process runs on the host CPUs local to GPU `dev`
+    (its PCI function's sysfs local_cpulist, intersected with the allowed
+    CPUs), so that pinned host buffers allocated there sit in the memory the
+    GPU reaches directly; the affinity is restored on exit.  `info` says what
+    was done (None when the topology could not be read)."""
+
+    def __init__(self, dev: int):
+        self.dev = dev
+        self.saved = None
+        self.info = None
+
+    def __enter__(self):
+        try:
+            import torch
+            p = torch.cuda.get_device_properties(self.dev)
+            addr = f"{p.pci_domain_id:04x}:{p.pci_bus_id:02x}:{p.pci_device_id:02x}.0"
+            with open(f"/sys/bus/pci/devices/{addr}/local_cpulist") as f:
+                text = f.read().strip()
+            cpus = set()
+            for part in text.split(","):
+                if "-" in part:
+                    a, b = part.split("-")
+                    cpus.update(range(int(a), int(b) + 1))
+                elif part:
+                    cpus.add(int(part))
+            allowed = os.sched_getaffinity(0)
+            use = cpus & allowed
+            self.info = {"pci": addr, "local_cpus": len(use), "allowed_cpus": len(allowed)}
+            if use and use != allowed:
+                self.saved = allowed
+                os.sched_setaffinity(0, use)
+        except Exception:
+            self.info = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.saved:
+            os.sched_setaffinity(0, self.saved)
+        return False
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -229,27 +271,29 @@ def life_workload(args, dist: Dist) -> dict:
     # the cells from pinned host memory, run `gens` generations, read the
     # cells and the population back
     import torch
-    host_in = torch.empty(cells, dtype=torch.int32).pin_memory()
-    host_out = torch.empty(cells, dtype=torch.int32).pin_memory()
-    life.read_to_pointer("cell", host_in.data_ptr(), cells * 4)
-    e2e_steps = max(1, min(args.steps, args.e2e_steps))
-    dist.barrier()
-    t0 = time.perf_counter()
-    pops = []
-    for _ in range(e2e_steps):
-        life.write_from_pointer("cell", host_in.data_ptr(), cells * 4)
-        life.run("proceed", gens)
-        life.read_to_pointer("cell", host_out.data_ptr(), cells * 4)
-        pops.append(life.population)
-    t1 = time.perf_counter()
-    dist.barrier()
+    with NearGpu(dist.local_rank) as near:
+        host_in = torch.empty(cells, dtype=torch.int32).pin_memory()
+        host_out = torch.empty(cells, dtype=torch.int32).pin_memory()
+        life.read_to_pointer("cell", host_in.data_ptr(), cells * 4)
+        e2e_steps = max(1, min(args.steps, args.e2e_steps))
+        dist.barrier()
+        t0 = time.perf_counter()
+        pops = []
+        for _ in range(e2e_steps):
+            life.write_from_pointer("cell", host_in.data_ptr(), cells * 4)
+            life.run("proceed", gens)
+            life.read_to_pointer("cell", host_out.data_ptr(), cells * 4)
+            pops.append(life.population)
+        t1 = time.perf_counter()
+        dist.barrier()
+        del host_in, host_out
     e2e_s = dist.max(t1 - t0)
     e2e = {"value": round(cells * gens * e2e_steps * dist.world / e2e_s / 1e9, 3),
            "unit": "Gcell-updates/s", "h2d_bytes_per_step": cells * 4,
            "d2h_bytes_per_step": cells * 4 + 4, "steps": e2e_steps,
-           "api": "om_array_write + om_run_n(proceed) + om_array_read + population scalar"}
+           "api": "om_array_write + om_run_n(proceed) + om_array_read + population scalar",
+           "host_cpus": near.info}
     life.close()
-    del host_in, host_out
 
     out = {
         "metric": LIFE_METRIC,
@@ -440,25 +484,27 @@ def hydro_workload(args, dist: Dist) -> dict:
     # end to end: per step upload the four fields from pinned host memory, one
     # step, read the four fields back
     import torch
-    hosts = [torch.empty(cells, dtype=torch.float32).pin_memory() for _ in range(4)]
     names = ("density", "velocity0", "velocity1", "pressure")
-    for t, nm in zip(hosts, names):
-        h.read_to_pointer(nm, t.data_ptr(), cells * 4)
-    e2e_steps = max(1, min(args.steps, args.e2e_steps))
-    dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        for t, nm in zip(hosts, names):
-            h.write_from_pointer(nm, t.data_ptr(), cells * 4)
-        h.proceed(1)
+    with NearGpu(dist.local_rank) as near:
+        hosts = [torch.empty(cells, dtype=torch.float32).pin_memory() for _ in range(4)]
         for t, nm in zip(hosts, names):
             h.read_to_pointer(nm, t.data_ptr(), cells * 4)
-    e2e_s = dist.max(time.perf_counter() - t0)
+        e2e_steps = max(1, min(args.steps, args.e2e_steps))
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            for t, nm in zip(hosts, names):
+                h.write_from_pointer(nm, t.data_ptr(), cells * 4)
+            h.proceed(1)
+            for t, nm in zip(hosts, names):
+                h.read_to_pointer(nm, t.data_ptr(), cells * 4)
+        e2e_s = dist.max(time.perf_counter() - t0)
+        del hosts
     e2e = {"value": round(cells * e2e_steps * dist.world / e2e_s / 1e9, 3),
            "unit": "Gcell-updates/s", "h2d_bytes_per_step": 4 * cells * 4,
            "d2h_bytes_per_step": 4 * cells * 4, "steps": e2e_steps,
-           "api": "om_array_write x4 + om_run(proceed) + om_array_read x4"}
-    del hosts
+           "api": "om_array_write x4 + om_run(proceed) + om_array_read x4",
+           "host_cpus": near.info}
     h.close()
     # FP64 comparators: the fused FP64 kernel (the same tile code in double)
     # and the plain FP64 GPU path (the generated structure)
@@ -523,13 +569,15 @@ def ensemble_workload(args, dist: Dist) -> dict:
     pgbuild.build()
     count = args.count
     sizes = pg.ensemble_sizes(count, 1 + dist.rank)
-    tile_x, tile_y, tiles_by = args.tile_x, args.tile_y, "command line"
-    if tile_x == 0 and tile_y == 0:
-        # tile shape picked by the autotuner on these very instance sizes
+    tile_x, tile_y, grid_limit, tiles_by = args.tile_x, args.tile_y, 0, "command line"
+    if tile_x == 0 and tile_y == 0 and args.tune:
+        # tile shape and persistent grid size picked by the autotuner on these
+        # very instance sizes
         best, _ = pg.autotune_ensemble(sizes, precision=32, gamma=1.4, device=dist.local_rank)
-        tile_x, tile_y, tiles_by = best.tile_x, best.tile_y, "om_autotune_ensemble"
+        tile_x, tile_y, grid_limit = best.tile_x, best.tile_y, best.grid_limit
+        tiles_by = "om_autotune_ensemble"
     e = pg.Ensemble(sizes, precision=32, gamma=1.4, device=dist.local_rank,
-                    tile_x=tile_x, tile_y=tile_y)
+                    tile_x=tile_x, tile_y=tile_y, grid_limit=grid_limit)
     e.init_kh(1000 * (1 + dist.rank))
     info = e.info()
     cells = info["cells"]
@@ -548,34 +596,36 @@ def ensemble_workload(args, dist: Dist) -> dict:
     # instance's four fields up from pinned host memory, one step, the four
     # fields and the instance time back
     import torch
-    hosts = []
-    for k, (a, b) in enumerate(sizes):
-        row = []
-        for f in pg.Ensemble.FIELDS:
-            t = torch.empty(a * b, dtype=torch.float32).pin_memory()
-            e.read_to_pointer(k, f, t.data_ptr(), a * b * 4)
-            row.append(t)
-        hosts.append(row)
-    e2e_steps = max(1, min(args.steps, args.e2e_steps))
-    dist.barrier()
-    t0 = time.perf_counter()
-    times = []
-    for _ in range(e2e_steps):
+    with NearGpu(dist.local_rank) as near:
+        hosts = []
         for k, (a, b) in enumerate(sizes):
-            for f, t in zip(pg.Ensemble.FIELDS, hosts[k]):
-                e.write_from_pointer(k, f, t.data_ptr(), a * b * 4)
-        e.step(1)
-        for k, (a, b) in enumerate(sizes):
-            for f, t in zip(pg.Ensemble.FIELDS, hosts[k]):
+            row = []
+            for f in pg.Ensemble.FIELDS:
+                t = torch.empty(a * b, dtype=torch.float32).pin_memory()
                 e.read_to_pointer(k, f, t.data_ptr(), a * b * 4)
-        times.append(e.scalar(0, "time"))
-    e2e_s = dist.max(time.perf_counter() - t0)
-    del hosts
+                row.append(t)
+            hosts.append(row)
+        e2e_steps = max(1, min(args.steps, args.e2e_steps))
+        dist.barrier()
+        t0 = time.perf_counter()
+        times = []
+        for _ in range(e2e_steps):
+            for k, (a, b) in enumerate(sizes):
+                for f, t in zip(pg.Ensemble.FIELDS, hosts[k]):
+                    e.write_from_pointer(k, f, t.data_ptr(), a * b * 4)
+            e.step(1)
+            for k, (a, b) in enumerate(sizes):
+                for f, t in zip(pg.Ensemble.FIELDS, hosts[k]):
+                    e.read_to_pointer(k, f, t.data_ptr(), a * b * 4)
+            times.append(e.scalar(0, "time"))
+        e2e_s = dist.max(time.perf_counter() - t0)
+        del hosts
     e2e = {"value": round(cells * e2e_steps * dist.world / e2e_s / 1e9, 3),
            "unit": "Gcell-updates/s", "h2d_bytes_per_step": 16 * cells,
            "d2h_bytes_per_step": 16 * cells + 8, "steps": e2e_steps,
            "api": "om_ensemble_write x4 per instance + om_ensemble_step(1) + "
-                  "om_ensemble_read x4 per instance + om_ensemble_scalar(time)"}
+                  "om_ensemble_read x4 per instance + om_ensemble_scalar(time)",
+           "host_cpus": near.info}
     # the same instances advanced one grid at a time through the single-grid API
     seq_ms = 0.0
     nseq = min(count, args.seq_instances)
@@ -589,10 +639,37 @@ def ensemble_workload(args, dist: Dist) -> dict:
         seq_cells += sizes[k][0] * sizes[k][1]
         h.close()
     seq_gcell = seq_cells * 10 / (seq_ms * 1e-3) / 1e9
+    # one 4096^2 instance through the ensemble kernel against the single-grid
+    # fused step on the same grid (the same tile shape)
+    one = None
+    if args.one_instance:
+        n1 = 4096
+        e1 = pg.Ensemble([(n1, n1)], precision=32, gamma=1.4, device=dist.local_rank,
+                         tile_x=tile_x, tile_y=tile_y)
+        e1.init_kh(7)
+        e1.step(3)
+        e1_ms = min(e1.time_step(20) for _ in range(2))
+        e1.close()
+        h1 = pg.Hydro((n1, n1), precision=32, gamma=1.4, device=dist.local_rank,
+                      tile_x=tile_x, tile_y=tile_y)
+        h1.init_kh(7)
+        h1.set_scalar("cfl", 0.4)
+        h1.proceed(3)
+        h1_ms = min(h1.time_run("proceed", 20) for _ in range(2))
+        h1.close()
+        ens1 = n1 * n1 * 20 / (e1_ms * 1e-3) / 1e9
+        fus1 = n1 * n1 * 20 / (h1_ms * 1e-3) / 1e9
+        one = {"instance": [n1, n1], "ensemble": round(ens1, 3), "single_grid": round(fus1, 3),
+               "ensemble_over_single": round(ens1 / fus1, 3), "unit": "Gcell-updates/s",
+               "note": "one instance through om_ensemble_step against om_run_n(proceed) on the "
+                       "same grid, 20 steps each, best of two"}
     peak, peak_kind = peaks()
     launch_ms = ms / args.steps
     achieved = 32.0 * cells / (launch_ms * 1e-3) / 1e9
-    traffic = profile_traffic_cells("hydro_ensemble_kernel", cells)
+    # the persistent 32 x 32 kernel (tile_y 0 with tile_x 0 or 32) or the tile kernel
+    ens_kernel = ("hydro_persist_ensemble_kernel" if tile_y == 0 and tile_x in (0, 32)
+                  else "hydro_ensemble_kernel")
+    traffic = profile_traffic_cells(ens_kernel, cells)
     out_times = [e.scalar(k, "time") for k in range(count)]
     e.close()
     acc = None
@@ -630,8 +707,9 @@ def ensemble_workload(args, dist: Dist) -> dict:
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic", "config": ensemble_config(count, cells, dist.world),
         "launch": {"work_items": info["work_items"], "grid": info["grid"],
-                   "tile": {"tile_x": tile_x, "tile_y": tile_y, "picked_by": tiles_by}},
-        "roofline": {"bound": "hbm", "kernel": "hydro_ensemble_kernel", "achieved": round(achieved, 1),
+                   "tile": {"tile_x": tile_x, "tile_y": tile_y, "grid_limit": grid_limit,
+                            "picked_by": tiles_by}},
+        "roofline": {"bound": "hbm", "kernel": ens_kernel, "achieved": round(achieved, 1),
                      "peak": peak, "peak_source": peak_source(peak_kind),
                      "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "traffic": traffic["bytes_per_launch"] if traffic else None,
@@ -647,6 +725,7 @@ def ensemble_workload(args, dist: Dist) -> dict:
                                  "persistent_over_single": round(value / dist.world / seq_gcell, 3),
                                  "note": "the first instances, one grid at a time (om_run_n per grid)"},
         "instance_time_range": [min(out_times), max(out_times)],
+        "one_instance": one,
         "accuracy": acc,
     }
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
@@ -1153,6 +1232,10 @@ def main() -> int:
     ap.add_argument("--fd-eps", type=float, nargs="+", default=[1e-3, 1e-5, 1e-7])
     ap.add_argument("--count", type=int, default=64)
     ap.add_argument("--seq-instances", type=int, default=16)
+    ap.add_argument("--no-tune", dest="tune", action="store_false",
+                    help="ensemble line: run the command line's tile shape without tuning")
+    ap.add_argument("--no-one-instance", dest="one_instance", action="store_false",
+                    help="ensemble line: skip the one-4096^2-instance comparison")
     ap.add_argument("--accuracy-steps", type=int, default=1000)
     ap.add_argument("--size", type=int, default=0)
     ap.add_argument("--generations", type=int, default=0)

@@ -72,8 +72,10 @@ typedef struct {
                        Hydro 1: plain unfused FP64-structured grid-stride kernels */
   int life_io;      /* Life cell I/O of the packed kernels: 0 = 128-bit, 1 = 32-bit */
   int life_kernel;  /* Life packed kernel: k >= 1 = warp-specialised persistent
-                       kernel, variant k-1 (variants 4-10 and 13 take their rows by
-                       TMA and need rows of at least 1024 cells); 0 = automatic:
+                       kernel, variant k-1 (variants 4-10 and 13-15 take their rows
+                       by TMA and need rows of at least 1024 cells; in 14 and 15
+                       each consumer warp synchronises with its two neighbours
+                       only); 0 = automatic:
                        with tile_y 0, that kernel on grids of at least 1.5 of its
                        tiles per SM, else register-resident blocks */
   int grid_limit;   /* persistent kernels (Life warp-specialised, the persistent

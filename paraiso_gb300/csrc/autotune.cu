@@ -106,7 +106,7 @@ extern "C" om_status om_autotune(int kind, int ndim, const int *sizes, const om_
           c.life_kernel = 0;
           cands.push_back(c);
         }
-      for (int k = 1; k <= (sizes[0] >= 1024 ? 14 : 4); ++k) {
+      for (int k = 1; k <= (sizes[0] >= 1024 ? 16 : 4); ++k) {
         om_config c = b;
         c.depth = 32;
         c.tile_x = 0;
@@ -189,15 +189,17 @@ extern "C" om_status om_autotune_ensemble(int count, const int *sizes, const om_
     if ((s & 1) && sms == 0) continue;
     om_ensemble e = nullptr;
     if (om_ensemble_create(count, sizes, &c, &e) != OM_OK) continue;
+    // 8 steps per timing, best of three after a settling run: candidates
+    // within a few per cent of each other are told apart
     float ms = 0, bestms = 1e30f;
-    bool ok = om_ensemble_init_kh(e, 1) == OM_OK && om_ensemble_time_step(e, 4, &ms) == OM_OK;
-    for (int r = 0; ok && r < 2; ++r) {
-      ok = om_ensemble_time_step(e, 4, &ms) == OM_OK;
+    bool ok = om_ensemble_init_kh(e, 1) == OM_OK && om_ensemble_time_step(e, 8, &ms) == OM_OK;
+    for (int r = 0; ok && r < 3; ++r) {
+      ok = om_ensemble_time_step(e, 8, &ms) == OM_OK;
       if (ok && ms < bestms) bestms = ms;
     }
     om_ensemble_destroy(e);
     if (!ok) continue;
-    const double rate = (double)cells * 4 / (bestms * 1e-3);
+    const double rate = (double)cells * 8 / (bestms * 1e-3);
     if (rate > best_r) {
       best_r = rate;
       best_c = c;

@@ -24,9 +24,11 @@
 //    exactly one per thread of the 704-thread CTA.
 //  * The paired form (PAIR, 352 threads) evaluates two walls or two cells
 //    per thread with packed f32x2 instructions (hf::f2): a wall and the
-//    wall 1332 items later, a cell and the cell 648 (stage 1) or 512
-//    (stage 2) later, a row's x-wall run with a column's y-wall run.  Walls
-//    of either axis share the arithmetic in the frame of the wall.
+//    wall 1344 items later, a cell and the cell 672 (stage 1) or 512
+//    (stage 2) later (whole warps, so both halves of a warp run along
+//    rows), a row's x-wall run with a column's y-wall run.  Walls of either
+//    axis share the arithmetic in the frame of the wall; an item without a
+//    partner is paired with itself and stored once.
 //  * The tile's CFL minimum is folded in registers over all the tiles of a
 //    CTA (of one instance) and published once.
 // Every value is formed by the same expressions as the production tile
@@ -57,6 +59,11 @@ constexpr uint32_t kBoxBytes = 4u * BH * BW * 4u;  // bytes the four TMA boxes d
 constexpr int kS1XMain = 36 * 32, kS1YMain = 37 * 32, kS1XRem = 36 * 5, kS1YRem = 37 * 4;
 constexpr int kS1Items = kS1XMain + kS1YMain + kS1XRem + kS1YRem;  // 2664
 constexpr int kQMain = 36 * 32, kQItems = 36 * 36;                  // stage-1 cells
+// the paired form's second items start a whole number of warps later, so a
+// warp's second items begin a row as its first ones do: wall i pairs with
+// wall i + kS1Half (when that exists), cell i with cell i + kQHalf
+constexpr int kS1Half = (kS1Items / 2 + 31) / 32 * 32;  // 1344
+constexpr int kQHalf = (kQItems / 2 + 31) / 32 * 32;    // 672
 
 using Flux = hs::Flux<float>;
 using Prim = hs::Prim<float>;
@@ -96,16 +103,24 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
 // describes field k of this grid).  Else every thread copies 16-byte
 // chunks with wrapped coordinates (grid sizes are multiples of 32, so a
 // wrapped chunk stays 16-byte aligned).
+// The four fields of a grid: their tensor maps (m, for boxes inside the
+// grid) and base pointers (f).
+struct FieldRefs {
+  const CUtensorMap *m0, *m1, *m2, *m3;
+  const float *f0, *f1, *f2, *f3;
+};
+
 template <int NTH = NT>
-__device__ __forceinline__ void issue_box(float *dst, bool inside, const CUtensorMap *const *maps,
-                                          const float *const *f, int n0, int n1, int X0, int Y0,
-                                          uint64_t *bar) {
+__device__ __forceinline__ void issue_box(float *dst, bool inside, const FieldRefs &r, int n0,
+                                          int n1, int X0, int Y0, uint64_t *bar) {
   if (inside) {
     if (threadIdx.x == 0) {
       tma::fence_proxy_async();
       tma::mbar_arrive_expect_tx(bar, kBoxBytes);
-#pragma unroll
-      for (int k = 0; k < 4; ++k) tma::load_2d(dst + k * PLANE, maps[k], X0 - 4, Y0 - 3, bar);
+      tma::load_2d(dst, r.m0, X0 - 4, Y0 - 3, bar);
+      tma::load_2d(dst + PLANE, r.m1, X0 - 4, Y0 - 3, bar);
+      tma::load_2d(dst + 2 * PLANE, r.m2, X0 - 4, Y0 - 3, bar);
+      tma::load_2d(dst + 3 * PLANE, r.m3, X0 - 4, Y0 - 3, bar);
     }
   } else {
     for (int i = threadIdx.x; i < BH * 10; i += NTH) {
@@ -113,8 +128,10 @@ __device__ __forceinline__ void issue_box(float *dst, bool inside, const CUtenso
       const int gy = hk::wrap_near(Y0 - 3 + py, n1), gx = hk::wrap_near(X0 - 4 + 4 * j, n0);
       const size_t gi = (size_t)gy * n0 + gx;
       float *d = dst + py * BW + 4 * j;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) cp_async16(d + k * PLANE, f[k] + gi);
+      cp_async16(d, r.f0 + gi);
+      cp_async16(d + PLANE, r.f1 + gi);
+      cp_async16(d + 2 * PLANE, r.f2 + gi);
+      cp_async16(d + 3 * PLANE, r.f3 + gi);
     }
     hk::cp_async_commit();
   }
@@ -319,23 +336,20 @@ __device__ __forceinline__ void persist_run(const HydroStepArgs *__restrict__ ar
   }
   __syncthreads();
 
-  auto instance_maps = [&](int k, const CUtensorMap **mp) {
-    if (ENS) {
-#pragma unroll
-      for (int f = 0; f < 4; ++f) mp[f] = table + (size_t)k * 4 + f;
-    } else {
-      mp[0] = m0; mp[1] = m1; mp[2] = m2; mp[3] = m3;
-    }
-  };
   auto issue = [&](int it, int k, float *dst, uint64_t *bar) {
     const HydroStepArgs &A = args[k];
     const int tile = it - (ENS ? pf[k] : 0);
     const int t1 = tile / A.nt0, t0 = tile - t1 * A.nt0;
-    const float *f[4] = {(const float *)A.rho, (const float *)A.v0, (const float *)A.v1,
-                         (const float *)A.p};
-    const CUtensorMap *mp[4];
-    instance_maps(k, mp);
-    issue_box<NTH>(dst, box_inside(t0 * TX, t1 * TY, A.n0, A.n1), mp, f, A.n0, A.n1, t0 * TX,
+    const CUtensorMap *tk = ENS ? table + (size_t)k * 4 : nullptr;
+    const FieldRefs r{ENS ? tk : m0,
+                      ENS ? tk + 1 : m1,
+                      ENS ? tk + 2 : m2,
+                      ENS ? tk + 3 : m3,
+                      (const float *)A.rho,
+                      (const float *)A.v0,
+                      (const float *)A.v1,
+                      (const float *)A.p};
+    issue_box<NTH>(dst, box_inside(t0 * TX, t1 * TY, A.n0, A.n1), r, A.n0, A.n1, t0 * TX,
                    t1 * TY, bar);
   };
 
@@ -416,18 +430,20 @@ __device__ __forceinline__ void persist_run(const HydroStepArgs *__restrict__ ar
     // stage-1 walls, order-1 reconstruction
     if (PAIR) {
       const hf::K<f2> k2 = hf::kconsts<f2>(K);
-      for (int i = tid; i < kS1Items / 2; i += NTH) {
+      for (int i = tid; i < kS1Half; i += NTH) {
         int axa, ca, wa, axb, cb, wb;
         s1_item(i, axa, ca, wa);
-        s1_item(i + kS1Items / 2, axb, cb, wb);
+        const bool two = i + kS1Half < kS1Items;
+        s1_item(two ? i + kS1Half : i, axb, cb, wb);
         const int da = axa == 0 ? 1 : BW, db = axb == 0 ? 1 : BW;
         const hf::NS<f2> L = pair_state(B, ca, axa, cb, axb);
         const hf::NS<f2> R = pair_state(B, ca + da, axa, cb + db, axb);
         const f2 cl = hf::pack(s.cq.c[ca], s.cq.c[cb]);
         const f2 cr = hf::pack(s.cq.c[ca + da], s.cq.c[cb + db]);
-        store_pair(hf::hllc_ns<f2>(k2, L, cl, R, cr),
-                   axa == 0 ? &s.fl.s1.x[wa] : &s.fl.s1.y[wa], axa,
-                   axb == 0 ? &s.fl.s1.x[wb] : &s.fl.s1.y[wb], axb);
+        Flux fa, fb;
+        store_pair(hf::hllc_ns<f2>(k2, L, cl, R, cr), &fa, axa, &fb, axb);
+        (axa == 0 ? s.fl.s1.x[wa] : s.fl.s1.y[wa]) = fa;
+        if (two) (axb == 0 ? s.fl.s1.x[wb] : s.fl.s1.y[wb]) = fb;
       }
     } else {
       for (int i = tid; i < kS1Items; i += NTH) {
@@ -459,10 +475,11 @@ __device__ __forceinline__ void persist_run(const HydroStepArgs *__restrict__ ar
       if (PAIR) {
         const hf::K<f2> k2 = hf::kconsts<f2>(K);
         const f2 t0 = hf::splat<f2>(dtdx0), t1 = hf::splat<f2>(dtdx1);
-        for (int i = tid; i < kQItems / 2; i += NTH) {
+        for (int i = tid; i < kQHalf; i += NTH) {
           int qya, qxa, qyb, qxb;
           q_item(i, qya, qxa);
-          q_item(i + kQItems / 2, qyb, qxb);
+          const bool two = i + kQHalf < kQItems;
+          q_item(two ? i + kQHalf : i, qyb, qxb);
           const int ca = (qya + 1) * BW + qxa + 2, cb = (qyb + 1) * BW + qxb + 2;
           const Flux &l0a = s.fl.s1.x[qya * F1X + qxa], &r0a = s.fl.s1.x[qya * F1X + qxa + 1];
           const Flux &l1a = s.fl.s1.y[qya * F1Y + qxa], &r1a = s.fl.s1.y[(qya + 1) * F1Y + qxa];
@@ -479,10 +496,10 @@ __device__ __forceinline__ void persist_run(const HydroStepArgs *__restrict__ ar
           for (int f = 0; f < 4; ++f) hf::unpack(q[f], qa[f], qb[f]);
           if (TAPE) {
             tape_cell(qya, qxa, qa, l0a, r0a, l1a, r1a);
-            tape_cell(qyb, qxb, qb, l0b, r0b, l1b, r1b);
+            if (two) tape_cell(qyb, qxb, qb, l0b, r0b, l1b, r1b);
           }
           s.cq.q[qya * QP + qxa] = make_float4(qa[0], qa[1], qa[2], qa[3]);
-          s.cq.q[qyb * QP + qxb] = make_float4(qb[0], qb[1], qb[2], qb[3]);
+          if (two) s.cq.q[qyb * QP + qxb] = make_float4(qb[0], qb[1], qb[2], qb[3]);
         }
       } else {
         for (int i = tid; i < kQItems; i += NTH) {

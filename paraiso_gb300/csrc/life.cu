@@ -817,7 +817,10 @@ __host__ __device__ constexpr bool kStagedPack() {
 // on the same mbarrier.  Words further out stay zero: with at most 32
 // generations per launch their error front never reaches an owned word.
 // Waits are bounded (tma::mbar_wait raises *err).
-template <int R, int NWC, int NWP, int NWS, bool TMA = false, int NS = 2>
+// PS: consumer warps synchronise each generation with their two neighbours
+// only (an mbarrier per warp and buffer parity, signalled once the warp's
+// boundary rows are written), instead of a barrier over all consumers
+template <int R, int NWC, int NWP, int NWS, bool TMA = false, int NS = 2, bool PS = false>
 __global__ void __launch_bounds__((NWC + NWP + NWS) * 32, 1)
 life_ws_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbParams p,
                uint32_t *__restrict__ pop, const __grid_constant__ CUtensorMap tmap,
@@ -828,6 +831,7 @@ life_ws_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbPa
   __shared__ uint32_t spop[32];
   __shared__ int4 nib[16];  // nibble -> its four cells
   __shared__ uint64_t bars[NWP][NS];
+  __shared__ uint64_t cbar[PS ? NWC : 1][2];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid < 16) nib[tid] = make_int4(tid & 1, (tid >> 1) & 1, (tid >> 2) & 1, (tid >> 3) & 1);
   const int kk = p.kk;
@@ -838,6 +842,10 @@ life_ws_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbPa
     tma::mbar_init(&bars[tid / NS][tid % NS], 1);
     tma::fence_mbar_init();
   }
+  if (PS && tid < 2 * NWC) tma::mbar_init(&cbar[tid >> 1][tid & 1], 1);
+  // consumer generations so far (all tiles): generation G exchanges through
+  // buffer G & 1, and is use G >> 1 of that buffer's mbarriers
+  uint32_t G = 0;
   __syncthreads();
   constexpr int NWT = NWC + NWP + NWS;
   // write back the owned words of tile t from shared-memory buffer A, by
@@ -957,10 +965,23 @@ life_ws_kernel(const int32_t *__restrict__ cur, int32_t *__restrict__ next, TbPa
         }
         const uint32_t colmask = (lane >= 1 && lane <= tw_own) ? ~0u : 0u;
         for (int g = 0; g < kk; ++g) {
-          const int b = g & 1;
+          const int b = PS ? (int)(G & 1u) : (g & 1);
           ex[b][warp][0][lane] = rows[0];
           ex[b][warp][1][lane] = rows[R - 1];
-          asm volatile("bar.sync 1, %0;" ::"r"(NWC * 32) : "memory");
+          if (PS) {
+            // A neighbour is at most one use ahead on a buffer: to arrive
+            // again it must first see this warp's next generation.  It
+            // reads a buffer before it signals the next generation, so
+            // this warp's rewrite two generations on cannot overtake it.
+            __syncwarp();
+            if (lane == 0) tma::mbar_arrive(&cbar[warp][b]);
+            const uint32_t par = (G >> 1) & 1u;
+            if (warp > 0) tma::mbar_wait(&cbar[warp - 1][b], par, err);
+            if (warp < NWC - 1) tma::mbar_wait(&cbar[warp + 1][b], par, err);
+            ++G;
+          } else {
+            asm volatile("bar.sync 1, %0;" ::"r"(NWC * 32) : "memory");
+          }
           const uint32_t up = warp > 0 ? ex[b][warp - 1][1][lane] : 0u;
           const uint32_t down = warp < NWC - 1 ? ex[b][warp + 1][0][lane] : 0u;
           RowSums ra = row_sums(__shfl_up_sync(0xffffffffu, up, 1), up,
@@ -1136,14 +1157,16 @@ struct WsVariant {
   int R, NWC, NWP, NWS;
   bool tma;  // producers take their rows by TMA
   int ns;    // TMA slots per producer warp
+  bool ps;   // consumers synchronise with their neighbours only
 };
 static const WsVariant kWsVariants[] = {
     {24, 16, 8, 8, false, 0}, {16, 16, 8, 8, false, 0}, {24, 16, 12, 4, false, 0},
     {20, 16, 8, 8, false, 0}, {20, 16, 8, 8, true, 2},  {24, 16, 8, 8, true, 2},
     {20, 16, 4, 12, true, 4}, {20, 16, 6, 10, true, 3}, {24, 16, 4, 12, true, 4},
     {21, 16, 8, 8, true, 2},  {22, 16, 8, 8, true, 2},  {21, 16, 8, 8, false, 0},
-    {22, 16, 8, 8, false, 0}, {23, 16, 8, 8, true, 2}};
-static const int kNumWsVariants = 14;
+    {22, 16, 8, 8, false, 0}, {23, 16, 8, 8, true, 2},  {22, 16, 8, 8, true, 2, true},
+    {20, 16, 8, 8, true, 2, true}};
+static const int kNumWsVariants = 16;
 // the variant the automatic choice takes when TMA serves the grid (rows of
 // at least 32 words; fastest on GB300 at 16384^2: 22 rows per consumer warp
 // give 990 tiles, at most 7 per SM, where 20 rows give 1098, at most 8),
@@ -1182,7 +1205,9 @@ static cudaError_t launch_ws(int v, const int32_t *cur, int32_t *next, const TbP
     case 10: k = life_ws_kernel<22, 16, 8, 8, true, 2>; break;
     case 11: k = life_ws_kernel<21, 16, 8, 8>; break;
     case 12: k = life_ws_kernel<22, 16, 8, 8>; break;
-    default: k = life_ws_kernel<23, 16, 8, 8, true, 2>; break;
+    case 13: k = life_ws_kernel<23, 16, 8, 8, true, 2>; break;
+    case 14: k = life_ws_kernel<22, 16, 8, 8, true, 2, true>; break;
+    default: k = life_ws_kernel<20, 16, 8, 8, true, 2, true>; break;
   }
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;

@@ -60,6 +60,13 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t by
                : "memory");
 }
 
+// one arrival on *bar (release: this thread's earlier shared-memory writes,
+// and those ordered before them, are visible to a thread whose wait sees
+// the phase complete)
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
 // wait until the phase with parity `parity` of *bar has completed; false
 // (and *err raised) when `polls` polls ran out
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t *err,

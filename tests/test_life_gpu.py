@@ -73,7 +73,7 @@ def test_life_temporal_blocking_tiles(om_lib, oracle, depth, tw, th, io):
     assert launches >= 2
 
 
-@pytest.mark.parametrize("kernel", list(range(1, 15)))
+@pytest.mark.parametrize("kernel", list(range(1, 17)))
 @pytest.mark.parametrize("depth", [32, 13])
 def test_life_warp_specialised(om_lib, oracle, kernel, depth):
     size = (2048, 1500)   # several tiles per CTA on a small grid, partial tiles
@@ -207,7 +207,7 @@ def test_life_full_size_properties(om_lib, oracle):
     gen.close()
 
 
-@pytest.mark.parametrize("kernel", [5, 8, 11, 14])
+@pytest.mark.parametrize("kernel", [5, 8, 11, 14, 15, 16])
 @pytest.mark.parametrize("size", [(1024, 700), (3072, 333), (1984, 1111)])
 def test_life_tma_rows_edge_tiles(om_lib, oracle, kernel, size):
     """The TMA variants on grids whose first and last tile columns wrap (the
