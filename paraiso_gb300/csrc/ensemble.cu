@@ -366,6 +366,45 @@ static om_status ens_check_waits(om_ensemble E) {
   return OM_ERR_CUDA;
 }
 
+// the CUDA graph of n steps from buffer parity E->cur (captured on first use)
+static om_status ens_graph(om_ensemble E, int n, cudaGraphExec_t *out) {
+  auto key = std::make_tuple(n, E->cur);
+  auto it = E->graphs.find(key);
+  if (it == E->graphs.end()) {
+    const int cur0 = E->cur;
+    cudaGraph_t g = nullptr;
+    OM_CUDA_CHECK(cudaStreamBeginCapture(E->stream, cudaStreamCaptureModeThreadLocal));
+    om_status s = ens_issue(E, n);
+    cudaError_t ce = cudaStreamEndCapture(E->stream, &g);
+    E->cur = cur0;
+    if (s != OM_OK) { if (g) cudaGraphDestroy(g); return s; }
+    if (ce != cudaSuccess) {
+      set_error(std::string("ensemble graph capture: ") + cudaGetErrorString(ce));
+      return OM_ERR_CUDA;
+    }
+    cudaGraphExec_t ex = nullptr;
+    ce = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) {
+      set_error(std::string("ensemble graph instantiate: ") + cudaGetErrorString(ce));
+      return OM_ERR_CUDA;
+    }
+    it = E->graphs.emplace(key, ex).first;
+  }
+  *out = it->second;
+  return OM_OK;
+}
+
+// replay the graph of n steps (n > 1)
+static om_status ens_replay(om_ensemble E, int n) {
+  cudaGraphExec_t ex = nullptr;
+  OM_TRY(ens_graph(E, n, &ex));
+  OM_CUDA_CHECK(cudaGraphLaunch(ex, E->stream));
+  if (n & 1) E->cur = 1 - E->cur;
+  E->last_launches = 2 * n;
+  return OM_OK;
+}
+
 static om_status ens_run(om_ensemble E, int n, bool use_graph) {
   OM_CUDA_CHECK(cudaSetDevice(E->device));
   for (int k = 0; k < E->count; ++k) hydro_scalars_refresh(&E->h_sc[k]);
@@ -373,32 +412,7 @@ static om_status ens_run(om_ensemble E, int n, bool use_graph) {
                                 cudaMemcpyHostToDevice, E->stream));
   OM_TRY(ens_tsmin_all(E));
   if (use_graph && n > 1) {
-    auto key = std::make_tuple(n, E->cur);
-    auto it = E->graphs.find(key);
-    if (it == E->graphs.end()) {
-      const int cur0 = E->cur;
-      cudaGraph_t g = nullptr;
-      OM_CUDA_CHECK(cudaStreamBeginCapture(E->stream, cudaStreamCaptureModeThreadLocal));
-      om_status s = ens_issue(E, n);
-      cudaError_t ce = cudaStreamEndCapture(E->stream, &g);
-      E->cur = cur0;
-      if (s != OM_OK) { if (g) cudaGraphDestroy(g); return s; }
-      if (ce != cudaSuccess) {
-        set_error(std::string("ensemble graph capture: ") + cudaGetErrorString(ce));
-        return OM_ERR_CUDA;
-      }
-      cudaGraphExec_t ex = nullptr;
-      ce = cudaGraphInstantiate(&ex, g, 0);
-      cudaGraphDestroy(g);
-      if (ce != cudaSuccess) {
-        set_error(std::string("ensemble graph instantiate: ") + cudaGetErrorString(ce));
-        return OM_ERR_CUDA;
-      }
-      it = E->graphs.emplace(key, ex).first;
-    }
-    OM_CUDA_CHECK(cudaGraphLaunch(it->second, E->stream));
-    if (n & 1) E->cur = 1 - E->cur;
-    E->last_launches = 2 * n;
+    OM_TRY(ens_replay(E, n));
   } else {
     OM_TRY(ens_issue(E, n));
   }
@@ -422,12 +436,20 @@ om_status om_ensemble_time_step(om_ensemble E, int n, float *ms) {
   OM_CUDA_CHECK(cudaMemcpyAsync(E->d_sc, E->h_sc, sizeof(HydroScalars) * E->count,
                                 cudaMemcpyHostToDevice, E->stream));
   OM_TRY(ens_tsmin_all(E));
+  cudaGraphExec_t ex = nullptr;
+  if (n > 1) OM_TRY(ens_graph(E, n, &ex));
   cudaEvent_t e0, e1;
   OM_CUDA_CHECK(cudaEventCreate(&e0));
   OM_CUDA_CHECK(cudaEventCreate(&e1));
   OM_CUDA_CHECK(cudaStreamSynchronize(E->stream));
   OM_CUDA_CHECK(cudaEventRecord(e0, E->stream));
-  OM_TRY(ens_issue(E, n));
+  if (ex) {
+    OM_CUDA_CHECK(cudaGraphLaunch(ex, E->stream));
+    if (n & 1) E->cur = 1 - E->cur;
+    E->last_launches = 2 * n;
+  } else {
+    OM_TRY(ens_issue(E, n));
+  }
   OM_CUDA_CHECK(cudaEventRecord(e1, E->stream));
   OM_CUDA_CHECK(cudaEventSynchronize(e1));
   cudaEventElapsedTime(ms, e0, e1);

@@ -86,7 +86,19 @@ struct alignas(128) Smem {
   } fl;
   uint64_t bar[2];
   unsigned long long red[32];
+  // ensembles: the arguments of the current and the next item's instance
+  // (read from shared memory rather than held in registers across phases)
+  HydroStepArgs args[2];
 };
+
+// a warp copies an argument block into shared memory
+__device__ __forceinline__ void copy_args(HydroStepArgs *dst, const HydroStepArgs *src,
+                                          int lane) {
+  static_assert(sizeof(HydroStepArgs) % 4 == 0, "argument block of whole words");
+  const uint32_t *s = reinterpret_cast<const uint32_t *>(src);
+  uint32_t *d = reinterpret_cast<uint32_t *>(dst);
+  for (int i = lane; i < (int)(sizeof(HydroStepArgs) / 4); i += 32) d[i] = s[i];
+}
 
 // a box lies inside the grid (no periodic image needed)
 __device__ __forceinline__ bool box_inside(int X0, int Y0, int n0, int n1) {
@@ -392,6 +404,7 @@ __device__ __forceinline__ void persist_run(const HydroStepArgs *__restrict__ ar
   if (ENS)
     while (lo < count - 1 && pf[lo + 1] <= item) ++lo;
   issue(item, lo, s.box[0], &s.bar[0]);
+  if (ENS && warp == 0) copy_args(&s.args[0], &args[lo], lane);
   {
     int X0, Y0;
     tile_origin(item, lo, X0, Y0);
@@ -404,7 +417,7 @@ __device__ __forceinline__ void persist_run(const HydroStepArgs *__restrict__ ar
   unsigned long long m = ~0ull;
 
   for (;;) {
-    const HydroStepArgs &A = args[lo];
+    const HydroStepArgs &A = ENS ? s.args[b] : args[lo];
     const int n0 = A.n0, n1 = A.n1;
     const int tile = item - (ENS ? pf[lo] : 0);
     int X0, Y0;
@@ -609,6 +622,9 @@ __device__ __forceinline__ void persist_run(const HydroStepArgs *__restrict__ ar
       A.sc->dt_last = (double)dtG;
       A.sc->time = A.sc->time + (double)dtG;
     }
+    // the next item's arguments into the other slot (its last reader, the
+    // previous item, is behind the last barrier)
+    if (ENS && next < total && warp == NTH / 32 - 1) copy_args(&s.args[b ^ 1], &args[lo_n], lane);
     // publish the CFL minimum when this CTA leaves the instance (the
     // reduction ends with a barrier); else one barrier before the next tile
     if (next >= total || lo_n != lo) {
