@@ -886,6 +886,20 @@ static om_status launch_tape(Handle *h, AdjointScratch *s, void *const *in, void
   return OM_OK;
 }
 
+// After a pass: a taped step whose bounded wait for its tensor copies ran
+// out raised wait_error in the adjoint's scalar block (cleared here).
+static om_status adjoint_waits(Handle *h, AdjointScratch *s) {
+  uint32_t w = 0;
+  OM_CUDA_CHECK(cudaMemcpyAsync(&w, &s->sc->wait_error, sizeof(w), cudaMemcpyDeviceToHost,
+                                h->stream));
+  OM_CUDA_CHECK(cudaStreamSynchronize(h->stream));
+  if (!w) return OM_OK;
+  OM_CUDA_CHECK(cudaMemsetAsync(&s->sc->wait_error, 0, sizeof(w), h->stream));
+  set_error("Hydro adjoint: a taped step's bounded wait for its tensor copies ran out; the "
+            "gradient of this pass is unspecified");
+  return OM_ERR_CUDA;
+}
+
 // s->sc becomes a copy of the handle's scalar block with the CFL minimum of
 // the handle's current state in tsmin[0].
 static om_status load_scalars(Handle *h, AdjointScratch *s) {
@@ -1138,7 +1152,7 @@ extern "C" om_status om_hydro_backward(om_handle H, om_hydro_tape t, const void 
     set_error(std::string("om_hydro_backward: ") + cudaGetErrorString(cudaGetLastError()));
     return OM_ERR_CUDA;
   }
-  return OM_OK;
+  return adjoint_waits(h, s);
 }
 
 extern "C" om_status om_hydro_adjoint_run(om_handle H, int steps, const void *target,
@@ -1210,7 +1224,7 @@ extern "C" om_status om_hydro_adjoint_run(om_handle H, int steps, const void *ta
     set_error(std::string("om_hydro_adjoint_run: ") + cudaGetErrorString(cudaGetLastError()));
     return done(OM_ERR_CUDA);
   }
-  return done(OM_OK);
+  return done(adjoint_waits(h, sc));
 }
 
 // Device time (ms) of one adjoint step at the handle's current state, for
