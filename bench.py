@@ -462,7 +462,8 @@ def hydro_workload(args, dist: Dist) -> dict:
     # dominant kernel per launch
     h.profile(True)
     h.time_run("proceed", min(args.steps, 10))
-    for kname in ("hydro_pair_kernel", "hydro_persist_kernel", "hydro_fused_kernel_f32"):
+    for kname in ("hydro_pair_kernel", "hydro_pair2_kernel", "hydro_persist_kernel",
+                  "hydro_fused_kernel_f32"):
         nl, kms, _ = h.profile_query(kname)
         if nl > 0:
             break
@@ -666,10 +667,14 @@ def ensemble_workload(args, dist: Dist) -> dict:
     peak, peak_kind = peaks()
     launch_ms = ms / args.steps
     achieved = 32.0 * cells / (launch_ms * 1e-3) / 1e9
-    # the persistent 32 x 32 kernel (tile_y 0 with tile_x 0 or 32) or the tile kernel
-    ens_kernel = ("hydro_persist_ensemble_kernel" if tile_y == 0 and tile_x in (0, 32)
-                  else "hydro_ensemble_kernel")
-    traffic = profile_traffic_cells(ens_kernel, cells)
+    # the persistent 32 x 32 kernel (tile_y 0: tile_x 0 two groups per CTA,
+    # 16 or 32 one group) or the tile kernel; the persistent forms move the
+    # same data (one traffic capture)
+    persistent = tile_y == 0 and tile_x in (0, 16, 32)
+    ens_kernel = ("hydro_pair2_ensemble_kernel" if persistent and tile_x == 0
+                  else "hydro_persist_ensemble_kernel" if persistent else "hydro_ensemble_kernel")
+    traffic = profile_traffic_cells("hydro_persist_ensemble_kernel" if persistent else ens_kernel,
+                                    cells)
     out_times = [e.scalar(k, "time") for k in range(count)]
     e.close()
     acc = None

@@ -125,12 +125,12 @@ extern "C" om_status om_autotune(int kind, int ndim, const int *sizes, const om_
     }
   } else {
     steps = 8;
-    // the persistent 32 x 32 kernel, paired (0, 0) and one wall per thread
-    // (32, 0), tile kernels, then column sweeps (a negative tile_y: rows
-    // per chunk)
-    const int shapes[10][2] = {{0, 0}, {32, 0}, {0, 32}, {0, 8}, {64, 0}, {0, 16}, {64, 8},
-                               {0, -8}, {0, -16}, {64, -8}};
-    const int nshapes = (b.precision == 64 || b.variant != 0) ? 1 : 10;
+    // the persistent 32 x 32 kernel, paired with two groups per CTA (0, 0),
+    // paired with two CTAs per SM (16, 0) and one wall per thread (32, 0),
+    // tile kernels, then column sweeps (a negative tile_y: rows per chunk)
+    const int shapes[11][2] = {{0, 0}, {16, 0}, {32, 0}, {0, 32}, {0, 8}, {64, 0}, {0, 16},
+                               {64, 8}, {0, -8}, {0, -16}, {64, -8}};
+    const int nshapes = (b.precision == 64 || b.variant != 0) ? 1 : 11;
     for (int s = 0; s < nshapes; ++s) {
       om_config c = b;
       c.tile_x = shapes[s][0];
@@ -168,8 +168,8 @@ extern "C" om_status om_autotune_ensemble(int count, const int *sizes, const om_
   }
   om_config b;
   if (base) b = *base; else om_config_default(&b);
-  const int shapes[7][2] = {{0, 0}, {32, 0}, {0, 32}, {0, 8}, {64, 0}, {0, 16}, {64, 8}};
-  const int nshapes = (b.precision == 64 || b.variant != 0) ? 1 : 7;
+  const int shapes[8][2] = {{0, 0}, {16, 0}, {32, 0}, {0, 32}, {0, 8}, {64, 0}, {0, 16}, {64, 8}};
+  const int nshapes = (b.precision == 64 || b.variant != 0) ? 1 : 8;
   long long cells = 0;
   for (int k = 0; k < count; ++k) cells += (long long)sizes[2 * k] * sizes[2 * k + 1];
   int dev = b.device;

@@ -159,6 +159,11 @@ om_status om_ensemble_create(int count, const int *sizes, const om_config *cfg,
   if (hydro_tile_is_persistent(E->tile))
     for (int k = 0; k < count; ++k)
       if (!hydro_persist_fits(sizes[2 * k], sizes[2 * k + 1])) E->tile = kTile32x32;
+  if (E->tile == kPairGroups32x32) {
+    long long items = 0;
+    for (int k = 0; k < count; ++k) items += (long long)(sizes[2 * k] / 32) * (sizes[2 * k + 1] / 32);
+    if (hydro_persist_form_for(2, items, c.device, c.grid_limit) != 2) E->tile = kPair32x32;
+  }
   hydro_tile_dims(E->tile, &E->tx, &E->ty);
   E->gamma = c.gamma;
   E->device = c.device;

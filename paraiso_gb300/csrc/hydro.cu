@@ -130,10 +130,16 @@ static om_status proceed_fused(Handle *h, int n) {
   const bool persist = !st->fp64 && st->variant != 2 && st->lm == 0 &&
                        hydro_tile_is_persistent(st->tile) &&
                        hydro_persist_fits(h->size[0], h->size[1]);
+  // the persistent kernel's form that runs (the profile name follows it)
+  const int form = persist ? hydro_persist_form_for(hydro_persist_form(st->tile),
+                                                    (long long)(h->size[0] / 32) * (h->size[1] / 32),
+                                                    h->device, h->cfg.grid_limit)
+                           : -1;
   const char *kname = st->fp64 ? "hydro_fused_kernel_f64"
                       : st->variant == 2 ? "hydro_fused_kernel_f32_exact"
-                      : persist          ? (st->tile == kPair32x32 ? "hydro_pair_kernel"
-                                                                       : "hydro_persist_kernel")
+                      : persist          ? (form == 2   ? "hydro_pair2_kernel"
+                                            : form == 1 ? "hydro_pair_kernel"
+                                                        : "hydro_persist_kernel")
                                          : "hydro_fused_kernel_f32";
   for (int k = 0; k < n; ++k) {
     OM_CUDA_CHECK(cudaMemsetAsync(&hsc_dev(h)->tsmin[1 - st->slot], 0xFF,

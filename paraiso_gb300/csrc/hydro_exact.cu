@@ -17,6 +17,7 @@ void hydro_tile_dims(int tile, int *tx, int *ty) {
     case kTile32x32: *tx = 32; *ty = 32; break;
     case kPersist32x32: *tx = 32; *ty = 32; break;
     case kPair32x32: *tx = 32; *ty = 32; break;
+    case kPairGroups32x32: *tx = 32; *ty = 32; break;
     case kTile64x8: *tx = 64; *ty = 8; break;
     case kSweep32x8: *tx = 32; *ty = 8; break;
     case kSweep32x16: *tx = 32; *ty = 16; break;

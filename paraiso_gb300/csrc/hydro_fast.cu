@@ -92,7 +92,7 @@ cudaError_t hydro_ensemble_f32(const HydroStepArgs *args, const int *prefix, int
                                bool exact, int grid, cudaStream_t s, const CUtensorMap *table) {
   if (exact) return hydro_ensemble_f32_exact(args, prefix, count, grid, s);
   if (hydro_tile_is_persistent(tile) && table)
-    return hydro_persist_ensemble(args, prefix, count, table, tile == kPair32x32, grid, s);
+    return hydro_persist_ensemble(args, prefix, count, table, hydro_persist_form(tile), grid, s);
   switch (tile) {
     case kTile32x8: return launch_ens<32, 8, 256>(args, prefix, count, grid, s);
     case kTile64x16: return launch_ens<64, 16, 512>(args, prefix, count, grid, s);
@@ -106,8 +106,9 @@ cudaError_t hydro_ensemble_f32(const HydroStepArgs *args, const int *prefix, int
 int hydro_ensemble_occupancy(int fp64, int tile, bool exact) {
   if (fp64 || exact) return hydro_ensemble_occupancy_exact(fp64);
   switch (tile) {
-    case kPersist32x32: return hydro_persist_occupancy(false);
-    case kPair32x32: return hydro_persist_occupancy(true);
+    case kPersist32x32:
+    case kPair32x32:
+    case kPairGroups32x32: return hydro_persist_occupancy(hydro_persist_form(tile));
     case kTile32x8: return occ_fast<32, 8, 256>();
     case kTile64x16: return occ_fast<64, 16, 512>();
     case kTile32x32: return occ_fast<32, 32, 512>();
@@ -143,8 +144,9 @@ cudaError_t hydro_fused_tape(int fp64, bool exact, const HydroStepArgs &a0, cons
   switch (tile) {
     case kPersist32x32:
     case kPair32x32:
+    case kPairGroups32x32:
       if (hydro_persist_fits(a0.n0, a0.n1))
-        return hydro_persist_tape(a0, tile == kPair32x32, t, s);
+        return hydro_persist_tape(a0, hydro_persist_form(tile), t, s);
       return launch_tape_fast<32, 32, 512>(a0, t, s);
     case kTile32x8: return launch_tape_fast<32, 8, 256>(a0, t, s);
     case kTile64x16: return launch_tape_fast<64, 16, 512>(a0, t, s);
@@ -165,8 +167,9 @@ cudaError_t hydro_fused_f32(const HydroStepArgs &a, int tile, bool exact, cudaSt
   switch (tile) {
     case kPersist32x32:
     case kPair32x32:
+    case kPairGroups32x32:
       if (hydro_persist_fits(a.n0, a.n1))
-        return hydro_persist_step(a, tile == kPair32x32, s, grid_out);
+        return hydro_persist_step(a, hydro_persist_form(tile), s, grid_out);
       return launch_fast<32, 32, 512>(a, s, grid_out);
     case kTile32x8: return launch_fast<32, 8, 256>(a, s, grid_out);
     case kTile64x16: return launch_fast<64, 16, 512>(a, s, grid_out);

@@ -14,26 +14,33 @@ namespace om {
 // Tile shapes of the fused kernel available to the tuner (FP32 production
 // build; FP64 and the exact FP32 variant run 32x16).
 // The sweep shapes (kSweep*) walk strips of TX columns down the grid in
-// chunks of TY rows (hydro_sweep.cuh).  kPersist32x32 and kPair32x32 are
-// the persistent 32 x 32 kernel with prefetched boxes (hydro_persist.cuh),
-// one wall or cell per thread or two with packed f32x2 instructions, on
-// grids whose sides are multiples of 32 and at least 64, else the 32 x 32
-// tile kernel.
+// chunks of TY rows (hydro_sweep.cuh).  kPersist32x32, kPair32x32 and
+// kPairGroups32x32 are the persistent 32 x 32 kernel with prefetched boxes
+// (hydro_persist.cuh): one wall or cell per thread, two with packed f32x2
+// instructions, and the latter as one CTA of two groups half a tile apart;
+// on grids whose sides are multiples of 32 and at least 64, else the
+// 32 x 32 tile kernel.
 enum HydroTile {
   kTile32x8 = 0, kTile32x16 = 1, kTile64x16 = 2, kTile32x32 = 3, kTile64x8 = 4,
   kSweep32x8 = 5, kSweep32x16 = 6, kSweep64x8 = 7, kPersist32x32 = 8, kPair32x32 = 9,
-  kTileCount = 10
+  kPairGroups32x32 = 10, kTileCount = 11
 };
 inline bool hydro_tile_is_persistent(int tile) {
-  return tile == kPersist32x32 || tile == kPair32x32;
+  return tile == kPersist32x32 || tile == kPair32x32 || tile == kPairGroups32x32;
+}
+// the persistent kernel's form: 0 one wall per thread, 1 paired, 2 paired
+// with two groups per CTA
+inline int hydro_persist_form(int tile) {
+  return tile == kPairGroups32x32 ? 2 : tile == kPair32x32 ? 1 : 0;
 }
 inline bool hydro_tile_is_sweep(int tile) { return tile >= kSweep32x8 && tile <= kSweep64x8; }
 void hydro_tile_dims(int tile, int *tx, int *ty);
 // the tile a configuration's tile_x / tile_y select (0 = default): x 64
 // with y 8 is 64x8, else 64x16; x 0 or 32 with y 8, 16 or 32 is 32x8,
-// 32x16 or the 32x32 tile kernel; with y 0 the persistent 32 x 32 kernel,
-// x 0 (the production default) in the paired form, x 32 one wall or cell
-// per thread.
+// 32x16 or the 32x32 tile kernel; with y 0 the persistent 32 x 32 kernel:
+// x 0 (the production default) paired, as one CTA per SM of two groups half
+// a tile apart; x 16 paired, two CTAs per SM; x 32 one wall or cell per
+// thread.
 // A negative tile_y selects a sweep of -tile_y rows per chunk (x 32 or 64).
 inline int hydro_tile_of(int tile_x, int tile_y, bool production) {
   if (!production) return kTile32x16;
@@ -45,7 +52,8 @@ inline int hydro_tile_of(int tile_x, int tile_y, bool production) {
   if (tile_y == 8) return kTile32x8;
   if (tile_y == 16) return kTile32x16;
   if (tile_y == 32) return kTile32x32;
-  return tile_x == 32 ? kPersist32x32 : kPair32x32;
+  if (tile_x == 16) return kPair32x32;
+  return tile_x == 32 ? kPersist32x32 : kPairGroups32x32;
 }
 
 // fused two-stage step; `exact` selects the no-contraction build
@@ -70,12 +78,18 @@ cudaError_t hydro_ensemble_f32(const HydroStepArgs *args, const int *prefix, int
 bool hydro_persist_fits(int n0, int n1);
 // the four field tensor maps of a's current state
 bool hydro_persist_encode(CUtensorMap *maps4, const HydroStepArgs &a);
-int hydro_persist_occupancy(bool pair);
-cudaError_t hydro_persist_step(const HydroStepArgs &a, bool pair, cudaStream_t s, int *grid_out);
-cudaError_t hydro_persist_tape(const HydroStepArgs &a, bool pair, const HydroTapeOut &t,
+// the form that runs for `tiles` tiles: two groups per CTA only when every
+// group has at least 16 tiles (grid_limit > 0: that many CTAs at most),
+// else the paired form
+int hydro_persist_form_for(int form, long long tiles, int device, int grid_limit);
+// resident CTAs per SM of the persistent ensemble kernel of a form
+// (hydro_persist_form; a CTA of form 2 holds two groups)
+int hydro_persist_occupancy(int form);
+cudaError_t hydro_persist_step(const HydroStepArgs &a, int form, cudaStream_t s, int *grid_out);
+cudaError_t hydro_persist_tape(const HydroStepArgs &a, int form, const HydroTapeOut &t,
                                cudaStream_t s);
 cudaError_t hydro_persist_ensemble(const HydroStepArgs *args, const int *prefix, int count,
-                                   const CUtensorMap *table, bool pair, int grid,
+                                   const CUtensorMap *table, int form, int grid,
                                    cudaStream_t s);
 cudaError_t hydro_ensemble_f64(const HydroStepArgs *args, const int *prefix, int count, int tile,
                                int grid, cudaStream_t s);

@@ -13,6 +13,16 @@
 
 namespace om {
 
+// The two-group form pays half a tile per group for its start; it runs when
+// each of its groups (two per CTA, one CTA per SM or grid_limit CTAs) has at
+// least 16 tiles, else the paired form with two CTAs per SM does.
+int hydro_persist_form_for(int form, long long tiles, int device, int grid_limit) {
+  if (form != 2) return form;
+  int ctas = sm_count(device);
+  if (grid_limit > 0 && grid_limit < ctas) ctas = grid_limit;
+  return tiles >= 16LL * 2 * ctas ? 2 : 1;
+}
+
 bool hydro_persist_fits(int n0, int n1) {
   return n0 % hp::TX == 0 && n1 % hp::TY == 0 && n0 >= 2 * hp::TX && n1 >= 2 * hp::TY;
 }
@@ -33,8 +43,8 @@ bool hydro_persist_encode(CUtensorMap *maps4, const HydroStepArgs &a) {
   return true;
 }
 
-template <class K> static int resident_per_sm(K kernel, int threads) {
-  const int smem = (int)sizeof(hp::Smem);
+template <class K> static int resident_per_sm(K kernel, int threads, int groups = 1) {
+  const int smem = (int)sizeof(hp::Smem) * groups;
   if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
       cudaSuccess) {
     cudaGetLastError();
@@ -48,22 +58,27 @@ template <class K> static int resident_per_sm(K kernel, int threads) {
   return n;
 }
 
-int hydro_persist_occupancy(bool pair) {
-  static int n[2] = {-1, -1};
-  int &v = n[pair ? 1 : 0];
+int hydro_persist_occupancy(int form) {
+  static int n[3] = {-1, -1, -1};
+  int &v = n[form];
   if (v < 0)
-    v = pair ? resident_per_sm(hp::hydro_persist_ensemble_kernel<true>, hp::NT2)
-             : resident_per_sm(hp::hydro_persist_ensemble_kernel<false>, hp::NT);
+    v = form == 2 ? resident_per_sm(hp::hydro_pair2_ensemble_kernel, 2 * hp::NT2, 2)
+        : form == 1 ? resident_per_sm(hp::hydro_persist_ensemble_kernel<true>, hp::NT2)
+                    : resident_per_sm(hp::hydro_persist_ensemble_kernel<false>, hp::NT);
   return v > 0 ? v : 1;
 }
 
-template <bool TAPE, bool PAIR>
+// FORM 0: one wall or cell per thread; 1: paired; 2: paired, two groups per CTA
+template <bool TAPE, int FORM>
 static cudaError_t persist_launch(const HydroStepArgs &a0, const HydroTapeOut *tape,
                                   cudaStream_t s, int *grid_out) {
-  auto kernel = PAIR ? hp::hydro_pair_kernel<TAPE> : hp::hydro_persist_kernel<TAPE>;
-  const int threads = PAIR ? hp::NT2 : hp::NT;
+  auto kernel = FORM == 2 ? hp::hydro_pair2_kernel<TAPE>
+                : FORM == 1 ? hp::hydro_pair_kernel<TAPE> : hp::hydro_persist_kernel<TAPE>;
+  const int groups = FORM == 2 ? 2 : 1;
+  const int threads = (FORM == 0 ? hp::NT : hp::NT2) * groups;
+  const size_t smem = sizeof(hp::Smem) * groups;
   static int occ = -1;
-  if (occ < 0) occ = resident_per_sm(kernel, threads);
+  if (occ < 0) occ = resident_per_sm(kernel, threads, groups);
   if (occ <= 0) return cudaErrorInvalidConfiguration;
   HydroStepArgs a = a0;
   a.nt0 = a.n0 / hp::TX;
@@ -72,31 +87,45 @@ static cudaError_t persist_launch(const HydroStepArgs &a0, const HydroTapeOut *t
   int dev = 0;
   cudaGetDevice(&dev);
   const int tiles = a.nt0 * (a.n1 / hp::TY);
-  int grid = std::min(tiles, occ * sm_count(dev));
+  // every group of a CTA takes at least one tile
+  int grid = std::min((tiles + groups - 1) / groups, occ * sm_count(dev));
   if (a.grid_limit > 0) grid = std::min(grid, a.grid_limit);
   HydroTapeOut t{};
   if (tape) t = *tape;
-  kernel<<<grid, threads, sizeof(hp::Smem), s>>>(a, m[0], m[1], m[2], m[3], t);
+  kernel<<<grid, threads, smem, s>>>(a, m[0], m[1], m[2], m[3], t);
   if (grid_out) *grid_out = grid;
   return cudaGetLastError();
 }
 
-cudaError_t hydro_persist_step(const HydroStepArgs &a, bool pair, cudaStream_t s, int *grid_out) {
-  return pair ? persist_launch<false, true>(a, nullptr, s, grid_out)
-              : persist_launch<false, false>(a, nullptr, s, grid_out);
+cudaError_t hydro_persist_step(const HydroStepArgs &a, int form, cudaStream_t s, int *grid_out) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  form = hydro_persist_form_for(form, (long long)(a.n0 / hp::TX) * (a.n1 / hp::TY), dev,
+                                a.grid_limit);
+  return form == 2 ? persist_launch<false, 2>(a, nullptr, s, grid_out)
+         : form == 1 ? persist_launch<false, 1>(a, nullptr, s, grid_out)
+                     : persist_launch<false, 0>(a, nullptr, s, grid_out);
 }
 
-cudaError_t hydro_persist_tape(const HydroStepArgs &a, bool pair, const HydroTapeOut &t,
+cudaError_t hydro_persist_tape(const HydroStepArgs &a, int form, const HydroTapeOut &t,
                                cudaStream_t s) {
-  return pair ? persist_launch<true, true>(a, &t, s, nullptr)
-              : persist_launch<true, false>(a, &t, s, nullptr);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  form = hydro_persist_form_for(form, (long long)(a.n0 / hp::TX) * (a.n1 / hp::TY), dev,
+                                a.grid_limit);
+  return form == 2 ? persist_launch<true, 2>(a, &t, s, nullptr)
+         : form == 1 ? persist_launch<true, 1>(a, &t, s, nullptr)
+                     : persist_launch<true, 0>(a, &t, s, nullptr);
 }
 
 cudaError_t hydro_persist_ensemble(const HydroStepArgs *args, const int *prefix, int count,
-                                   const CUtensorMap *table, bool pair, int grid,
+                                   const CUtensorMap *table, int form, int grid,
                                    cudaStream_t s) {
-  if (hydro_persist_occupancy(pair) < 1) return cudaErrorInvalidConfiguration;
-  if (pair)
+  if (hydro_persist_occupancy(form) < 1) return cudaErrorInvalidConfiguration;
+  if (form == 2)
+    hp::hydro_pair2_ensemble_kernel<<<grid, 2 * hp::NT2, 2 * sizeof(hp::Smem), s>>>(
+        args, prefix, count, table);
+  else if (form == 1)
     hp::hydro_persist_ensemble_kernel<true><<<grid, hp::NT2, sizeof(hp::Smem), s>>>(
         args, prefix, count, table);
   else

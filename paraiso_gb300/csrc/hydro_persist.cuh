@@ -85,11 +85,16 @@ struct alignas(128) Smem {
     } s2;
   } fl;
   uint64_t bar[2];
+  uint64_t go;  // two groups per CTA: group 0 releases group 1 (in group 0's block)
   unsigned long long red[32];
   // ensembles: the arguments of the current and the next item's instance
   // (read from shared memory rather than held in registers across phases)
   HydroStepArgs args[2];
 };
+
+// two CTAs per SM, or one CTA of two groups, within the SM's shared memory
+// (227 KB per CTA at most)
+static_assert(2 * sizeof(Smem) <= 232448, "two shared-memory blocks per SM");
 
 // a warp copies an argument block into shared memory
 __device__ __forceinline__ void copy_args(HydroStepArgs *dst, const HydroStepArgs *src,
@@ -124,9 +129,9 @@ struct FieldRefs {
 
 template <int NTH = NT>
 __device__ __forceinline__ void issue_box(float *dst, bool inside, const FieldRefs &r, int n0,
-                                          int n1, int X0, int Y0, uint64_t *bar) {
+                                          int n1, int X0, int Y0, uint64_t *bar, int tid) {
   if (inside) {
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
       tma::fence_proxy_async();
       tma::mbar_arrive_expect_tx(bar, kBoxBytes);
       tma::load_2d(dst, r.m0, X0 - 4, Y0 - 3, bar);
@@ -135,7 +140,7 @@ __device__ __forceinline__ void issue_box(float *dst, bool inside, const FieldRe
       tma::load_2d(dst + 3 * PLANE, r.m3, X0 - 4, Y0 - 3, bar);
     }
   } else {
-    for (int i = threadIdx.x; i < BH * 10; i += NTH) {
+    for (int i = tid; i < BH * 10; i += NTH) {
       const int py = i / 10, j = i - py * 10;
       const int gy = hk::wrap_near(Y0 - 3 + py, n1), gx = hk::wrap_near(X0 - 4 + 4 * j, n0);
       const size_t gi = (size_t)gy * n0 + gx;
@@ -328,25 +333,60 @@ __device__ __forceinline__ void wall_run2(const float4 *q, int xb, int yb, Flux 
 // and items pf[k] .. pf[k+1]-1).  TAPE: the taped step (single grid).
 // PAIR: the paired form (NT2 threads), else one wall or cell per thread
 // (NT threads).
-template <bool TAPE, bool ENS, bool PAIR>
+// GROUPS 2: the CTA holds two independent groups of NTH threads, each with
+// its own shared-memory block (sm[0], sm[1]) and named barrier, working on
+// alternate items; group 1 starts once group 0 has passed the second phase
+// of its first tile, so the two groups' phases run about half a tile apart
+// and one group's barrier tails overlap the other's arithmetic.
+template <bool TAPE, bool ENS, bool PAIR, int GROUPS = 1>
 __device__ __forceinline__ void persist_run(const HydroStepArgs *__restrict__ args,
                                             const int *__restrict__ pf, int count,
                                             const CUtensorMap *table, const CUtensorMap *m0,
                                             const CUtensorMap *m1, const CUtensorMap *m2,
-                                            const CUtensorMap *m3, Smem &s,
+                                            const CUtensorMap *m3, Smem *sm,
                                             const HydroTapeOut *tape) {
   constexpr int NTH = PAIR ? NT2 : NT;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int grp = GROUPS == 2 ? (int)threadIdx.x / NTH : 0;
+  Smem &s = sm[grp];
+  const int tid = (int)threadIdx.x - grp * NTH, lane = tid & 31, warp = tid >> 5;
+  auto sync = [&]() {
+    if (GROUPS == 1) __syncthreads();
+    else asm volatile("bar.sync %0, %1;" ::"r"(1 + grp), "r"(NTH) : "memory");
+  };
+  // block-wide (group-wide) min of CFL bit patterns folded into *dst
+  auto min_to = [&](unsigned long long v, unsigned long long *dst) {
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+      v = w < v ? w : v;
+    }
+    if (lane == 0) s.red[warp] = v;
+    sync();
+    if (warp == 0) {
+      v = lane < NTH / 32 ? s.red[lane] : ~0ull;
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w < v ? w : v;
+      }
+      if (lane == 0) atomicMin(dst, v);
+    }
+  };
   const int total =
       ENS ? pf[count] : args[0].nt0 * ((args[0].n1 + TY - 1) / TY);
-  int item = blockIdx.x;
-  if (item >= total) return;
+  int item = (int)blockIdx.x * GROUPS + grp;
+  const int stride = (int)gridDim.x * GROUPS;
   if (tid == 0) {
     tma::mbar_init(&s.bar[0], 1);
     tma::mbar_init(&s.bar[1], 1);
+    if (GROUPS == 2 && grp == 0) tma::mbar_init(&s.go, 1);
     tma::fence_mbar_init();
   }
   __syncthreads();
+  bool released = GROUPS == 1 || grp == 1;
+  if (item >= total) {
+    if (!released && tid == 0) tma::mbar_arrive(&sm[0].go);
+    return;
+  }
+  if (GROUPS == 2 && grp == 1) tma::mbar_wait(&sm[0].go, 0, &args[0].sc->wait_error);
 
   auto issue = [&](int it, int k, float *dst, uint64_t *bar) {
     const HydroStepArgs &A = args[k];
@@ -362,7 +402,7 @@ __device__ __forceinline__ void persist_run(const HydroStepArgs *__restrict__ ar
                       (const float *)A.v1,
                       (const float *)A.p};
     issue_box<NTH>(dst, box_inside(t0 * TX, t1 * TY, A.n0, A.n1), r, A.n0, A.n1, t0 * TX,
-                   t1 * TY, bar);
+                   t1 * TY, bar, tid);
   };
 
   // sound speeds of the box cells into s.cq.c: items [i0, BH*BW/ (PAIR ? 2 : 1))
@@ -409,10 +449,10 @@ __device__ __forceinline__ void persist_run(const HydroStepArgs *__restrict__ ar
     int X0, Y0;
     tile_origin(item, lo, X0, Y0);
     await_box(0, X0, Y0, args[lo].n0, args[lo].n1, &args[lo].sc->wait_error);
-    __syncthreads();
+    sync();
     sounds(s.box[0], hf::consts<float>(args[lo].gamma_f), tid, NTH);
   }
-  __syncthreads();
+  sync();
   int b = 0;
   unsigned long long m = ~0ull;
 
@@ -432,7 +472,7 @@ __device__ __forceinline__ void persist_run(const HydroStepArgs *__restrict__ ar
     // the next item's box goes into the other buffer while this one computes
     // (that buffer's last reader, the previous tile's stage 2, is behind the
     // last barrier)
-    const int next = item + gridDim.x;
+    const int next = item + stride;
     int lo_n = lo;
     if (next < total) {
       if (ENS)
@@ -470,7 +510,7 @@ __device__ __forceinline__ void persist_run(const HydroStepArgs *__restrict__ ar
               hf::hllc<1>(K, box_cell(B, c), s.cq.c[c], box_cell(B, c + BW), s.cq.c[c + BW]);
       }
     }
-    __syncthreads();
+    sync();
 
     // stage-1 cells (qy, qx) = box cell (qy+1, qx+2), advanced by dt/2
     {
@@ -530,7 +570,11 @@ __device__ __forceinline__ void persist_run(const HydroStepArgs *__restrict__ ar
         }
       }
     }
-    __syncthreads();
+    sync();
+    if (!released) {  // group 0, first tile: let group 1 start
+      if (tid == 0) tma::mbar_arrive(&sm[0].go);
+      released = true;
+    }
 
     // stage-2 walls, MUSCL-minmod of the stage-1 state: the x walls
     // 3t..3t+2 of row `lane` and the y walls 3t..3t+2 of column `lane`
@@ -551,7 +595,7 @@ __device__ __forceinline__ void persist_run(const HydroStepArgs *__restrict__ ar
       tile_origin(next, lo_n, Xn, Yn);
       await_box(b ^ 1, Xn, Yn, args[lo_n].n0, args[lo_n].n1, &args[lo_n].sc->wait_error);
     }
-    __syncthreads();
+    sync();
 
     // stage-2 cells (oy, ox) = box cell (oy+3, ox+4), advanced by dt and
     // written out, with the CFL minimum of the new state; the threads with
@@ -628,10 +672,10 @@ __device__ __forceinline__ void persist_run(const HydroStepArgs *__restrict__ ar
     // publish the CFL minimum when this CTA leaves the instance (the
     // reduction ends with a barrier); else one barrier before the next tile
     if (next >= total || lo_n != lo) {
-      hk::block_min_to(m, &A.sc->tsmin[1 - A.read_slot], s.red);
+      min_to(m, &A.sc->tsmin[1 - A.read_slot]);
       m = ~0ull;
     } else {
-      __syncthreads();
+      sync();
     }
     if (next >= total) break;
     item = next;
@@ -648,7 +692,7 @@ hydro_persist_kernel(HydroStepArgs a, const __grid_constant__ CUtensorMap m0,
                      const __grid_constant__ CUtensorMap m3, HydroTapeOut tape) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   persist_run<TAPE, false, false>(&a, nullptr, 1, nullptr, &m0, &m1, &m2, &m3,
-                                  *reinterpret_cast<Smem *>(smem_raw), &tape);
+                                  reinterpret_cast<Smem *>(smem_raw), &tape);
 }
 
 template <bool TAPE>
@@ -658,7 +702,30 @@ hydro_pair_kernel(HydroStepArgs a, const __grid_constant__ CUtensorMap m0,
                   const __grid_constant__ CUtensorMap m3, HydroTapeOut tape) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   persist_run<TAPE, false, true>(&a, nullptr, 1, nullptr, &m0, &m1, &m2, &m3,
-                                 *reinterpret_cast<Smem *>(smem_raw), &tape);
+                                 reinterpret_cast<Smem *>(smem_raw), &tape);
+}
+
+// the paired form as one CTA per SM of two groups half a tile apart (two
+// shared-memory blocks); 80 registers keep the 22 warps within the SM
+// sub-partitions' register files
+template <bool TAPE>
+__global__ void __maxnreg__(80)
+hydro_pair2_kernel(HydroStepArgs a, const __grid_constant__ CUtensorMap m0,
+                   const __grid_constant__ CUtensorMap m1, const __grid_constant__ CUtensorMap m2,
+                   const __grid_constant__ CUtensorMap m3, HydroTapeOut tape) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  persist_run<TAPE, false, true, 2>(&a, nullptr, 1, nullptr, &m0, &m1, &m2, &m3,
+                                    reinterpret_cast<Smem *>(smem_raw), &tape);
+}
+
+// the paired ensemble step as one CTA per SM of two groups half an item apart
+__global__ void __maxnreg__(80)
+hydro_pair2_ensemble_kernel(const HydroStepArgs *__restrict__ args,
+                            const int *__restrict__ prefix, int count,
+                            const CUtensorMap *__restrict__ table) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  persist_run<false, true, true, 2>(args, prefix, count, table, nullptr, nullptr, nullptr, nullptr,
+                                    reinterpret_cast<Smem *>(smem_raw), nullptr);
 }
 
 // table: 4 tensor maps per instance for the buffers `args` reads
@@ -669,7 +736,7 @@ hydro_persist_ensemble_kernel(const HydroStepArgs *__restrict__ args,
                               const CUtensorMap *__restrict__ table) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   persist_run<false, true, PAIR>(args, prefix, count, table, nullptr, nullptr, nullptr, nullptr,
-                                 *reinterpret_cast<Smem *>(smem_raw), nullptr);
+                                 reinterpret_cast<Smem *>(smem_raw), nullptr);
 }
 
 }  // namespace hp

@@ -169,7 +169,8 @@ def test_backward_rejects_foreign_tape(om_lib, oracle):
 
 
 @pytest.mark.parametrize("precision,size,tile", [(32, (64, 48), 0), (64, (64, 48), 0),
-                                                 (32, (128, 96), 0), (32, (128, 96), 32)])
+                                                 (32, (128, 96), 0), (32, (128, 96), 16),
+                                                 (32, (128, 96), 32)])
 def test_segment_tapes_match_retaping(om_lib, oracle, monkeypatch, precision, size, tile):
     # The backward pass recomputes each segment with the taped step, keeping
     # one tape per step; when those tapes cannot be allocated it recomputes

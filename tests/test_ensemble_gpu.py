@@ -48,10 +48,11 @@ def test_ensemble_bit_exact_per_instance(om_lib, oracle, precision, variant):
     e.close()
 
 
-@pytest.mark.parametrize("tile", [(0, 0), (32, 0), (0, 32), (0, 16)])
+@pytest.mark.parametrize("tile", [(0, 0), (16, 0), (32, 0), (0, 32), (0, 16)])
 def test_ensemble_fast_matches_single_grids(om_lib, tile):
-    # (0, 0) and (32, 0): the persistent 32 x 32 kernel, paired and one wall
-    # per thread, each item's box prefetched (TMA inside an instance,
+    # (0, 0), (16, 0) and (32, 0): the persistent 32 x 32 kernel, paired as
+    # two groups per CTA, paired, and one wall per thread, each item's box
+    # prefetched (TMA inside an instance,
     # wrapped copies at its edges) while the block computes the item before;
     # (0, 32) and (0, 16): tile kernels; small instances: every block walks
     # several instances
@@ -70,6 +71,26 @@ def test_ensemble_fast_matches_single_grids(om_lib, tile):
             assert np.array_equal(a, b), (k, s)
         assert e.scalar(k, "time") == h.get_scalar("time")
         np.testing.assert_allclose(e.totals(k), h.totals(), rtol=1e-12)
+        h.close()
+    e.close()
+
+
+def test_ensemble_two_groups_matches_single_grids(om_lib):
+    # grid_limit 2: two CTAs of two groups for about 100 items, so the
+    # two-group form of the persistent kernel runs; every instance equals its
+    # single-grid production run (the same arithmetic) bit for bit
+    sizes = om_lib.ensemble_sizes(4, 9, lo=128, hi=256)
+    e = om_lib.Ensemble(sizes, precision=32, gamma=GAMMA, grid_limit=2)
+    e.init_kh(3)
+    e.step(4)
+    for k, s in enumerate(sizes):
+        h = om_lib.Hydro(s, precision=32, gamma=GAMMA)
+        h.init_kh(3 + k)
+        h.set_scalar("cfl", CFL)
+        h.proceed(4)
+        for a, b in zip(e.state(k), h.state()):
+            assert np.array_equal(a, b), (k, s)
+        assert e.scalar(k, "time") == h.get_scalar("time")
         h.close()
     e.close()
 

@@ -67,8 +67,8 @@ def test_fp32_exact_variants_bit_exact(om_lib, oracle, size, variant):
     h.close()
 
 
-@pytest.mark.parametrize("tile", [(0, 0), (32, 0), (0, 32), (0, 8), (0, 16), (64, 0), (64, 8),
-                                  (0, -8), (0, -16), (64, -8)])
+@pytest.mark.parametrize("tile", [(0, 0), (16, 0), (32, 0), (0, 32), (0, 8), (0, 16), (64, 0),
+                                  (64, 8), (0, -8), (0, -16), (64, -8)])
 def test_fp32_fast_against_fp64(om_lib, oracle, tile):
     size = (128, 96)
     st64 = kh_state(oracle, size, 5, np.float64)
@@ -227,19 +227,24 @@ def test_sweep_matches_tile_kernel(om_lib, oracle, size, sweep):
 
 @pytest.mark.parametrize("size,limit", [((128, 96), 0), ((128, 96), 3), ((64, 64), 0),
                                         ((256, 160), 5), ((96, 320), 2), ((1024, 768), 0),
+                                        ((1024, 768), 4), ((512, 512), 2), ((256, 128), 1),
                                         ((100, 96), 0)])
 def test_persistent_matches_tile_kernel(om_lib, oracle, size, limit):
     """The persistent 32 x 32 kernel (each CTA walks several tiles; the next
     tile's box is prefetched by TMA inside the grid and by wrapped 16-byte
     copies at its edges; stage-2 walls in runs of three), in its paired form
-    (0, 0: two walls or cells per thread with packed f32x2 instructions) and
-    with one wall per thread (32, 0), forms every value with the tile
-    kernel's operations: the production FP32 paths agree bit for bit.
+    (two walls or cells per thread with packed f32x2 instructions; 0, 0: as
+    one CTA per SM of two groups running half a tile apart; 16, 0: two CTAs
+    per SM) and with one wall per thread (32, 0), forms every value with
+    the tile kernel's operations: the production FP32 paths agree bit for
+    bit.
     grid_limit forces several tiles per CTA on small grids; 100 x 96 (not a
-    multiple of 32) runs the tile kernel under all three."""
+    multiple of 32) runs the tile kernel under all three.  The two-group
+    form runs where each group gets at least 16 tiles: here with grid_limit
+    4, 2 and 1 (768, 256 and 32 tiles), else (0, 0) runs the paired form."""
     st = kh_state(oracle, size, 13, np.float32)
     out = []
-    for tx, ty in ((0, 0), (32, 0), (0, 32)):
+    for tx, ty in ((0, 0), (16, 0), (32, 0), (0, 32)):
         h = make(om_lib, size, 32, 0, tile_x=tx, tile_y=ty, grid_limit=limit)
         h.set_state(st)
         h.proceed(7)
