@@ -668,13 +668,12 @@ def ensemble_workload(args, dist: Dist) -> dict:
     launch_ms = ms / args.steps
     achieved = 32.0 * cells / (launch_ms * 1e-3) / 1e9
     # the persistent 32 x 32 kernel (tile_y 0: tile_x 0 two groups per CTA,
-    # 16 or 32 one group) or the tile kernel; the persistent forms move the
-    # same data (one traffic capture)
+    # which the library runs on work lists of at least 16 items per group,
+    # as here; 16 or 32 one group) or the tile kernel
     persistent = tile_y == 0 and tile_x in (0, 16, 32)
     ens_kernel = ("hydro_pair2_ensemble_kernel" if persistent and tile_x == 0
                   else "hydro_persist_ensemble_kernel" if persistent else "hydro_ensemble_kernel")
-    traffic = profile_traffic_cells("hydro_persist_ensemble_kernel" if persistent else ens_kernel,
-                                    cells)
+    traffic = profile_traffic_cells(ens_kernel, cells)
     out_times = [e.scalar(k, "time") for k in range(count)]
     e.close()
     acc = None
