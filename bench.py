@@ -276,6 +276,10 @@ def life_workload(args, dist: Dist) -> dict:
         host_out = torch.empty(cells, dtype=torch.int32).pin_memory()
         life.read_to_pointer("cell", host_in.data_ptr(), cells * 4)
         e2e_steps = max(1, min(args.steps, args.e2e_steps))
+        # one untimed round trip first (its first use of this path's graph)
+        life.write_from_pointer("cell", host_in.data_ptr(), cells * 4)
+        life.run("proceed", gens)
+        life.read_to_pointer("cell", host_out.data_ptr(), cells * 4)
         dist.barrier()
         t0 = time.perf_counter()
         pops = []
@@ -491,6 +495,12 @@ def hydro_workload(args, dist: Dist) -> dict:
         for t, nm in zip(hosts, names):
             h.read_to_pointer(nm, t.data_ptr(), cells * 4)
         e2e_steps = max(1, min(args.steps, args.e2e_steps))
+        # one untimed round trip first
+        for t, nm in zip(hosts, names):
+            h.write_from_pointer(nm, t.data_ptr(), cells * 4)
+        h.proceed(1)
+        for t, nm in zip(hosts, names):
+            h.read_to_pointer(nm, t.data_ptr(), cells * 4)
         dist.barrier()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
@@ -607,6 +617,14 @@ def ensemble_workload(args, dist: Dist) -> dict:
                 row.append(t)
             hosts.append(row)
         e2e_steps = max(1, min(args.steps, args.e2e_steps))
+        # one untimed round trip first
+        for k, (a, b) in enumerate(sizes):
+            for f, t in zip(pg.Ensemble.FIELDS, hosts[k]):
+                e.write_from_pointer(k, f, t.data_ptr(), a * b * 4)
+        e.step(1)
+        for k, (a, b) in enumerate(sizes):
+            for f, t in zip(pg.Ensemble.FIELDS, hosts[k]):
+                e.read_to_pointer(k, f, t.data_ptr(), a * b * 4)
         dist.barrier()
         t0 = time.perf_counter()
         times = []
