@@ -29,10 +29,15 @@
 //    rows), a row's x-wall run with a column's y-wall run.  Walls of either
 //    axis share the arithmetic in the frame of the wall; an item without a
 //    partner is paired with itself and stored once.
+//  * On large grids the paired form runs as one CTA per SM of two groups
+//    (persist_run's GROUPS), each with its own shared-memory block and
+//    named barrier, whose phases are offset by about half a tile.
+//  * Stage 2 of a tile shares its pass with the next tile's sound speeds.
 //  * The tile's CFL minimum is folded in registers over all the tiles of a
-//    CTA (of one instance) and published once.
-// Every value is formed by the same expressions as the production tile
-// kernel of hydro_kernels.cuh, so the two give the same bits.
+//    CTA or group (of one instance) and published once.
+// Every value is formed by the production algebra's explicit operations
+// (hf:: in hydro_scheme.cuh), as in the tile kernels of hydro_kernels.cuh,
+// so all of them give the same bits.
 #pragma once
 
 #include <cuda.h>
@@ -47,7 +52,7 @@ namespace hp {
 
 constexpr int TX = 32, TY = 32;
 constexpr int NT = 704;                 // 22 warps; two CTAs per SM
-constexpr int NT2 = 352;                // the paired form: 11 warps; two CTAs per SM
+constexpr int NT2 = 352;                // the paired form: 11 warps; two CTAs (or groups) per SM
 constexpr int BW = 40, BH = 38;         // box columns X0-4 .. X0+35, rows Y0-3 .. Y0+34
 constexpr int PLANE = 1536;             // floats per field plane: 38 x 40 = 1520, padded to 6144 B
 constexpr int QP = 37;                  // stage-1 records per row (36 used)
