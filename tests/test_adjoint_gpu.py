@@ -168,17 +168,20 @@ def test_backward_rejects_foreign_tape(om_lib, oracle):
     b.close()
 
 
-@pytest.mark.parametrize("precision,size,tile", [(32, (64, 48), 0), (64, (64, 48), 0),
-                                                 (32, (128, 96), 0), (32, (128, 96), 16),
-                                                 (32, (128, 96), 32)])
-def test_segment_tapes_match_retaping(om_lib, oracle, monkeypatch, precision, size, tile):
+@pytest.mark.parametrize("precision,size,tile,limit", [(32, (64, 48), 0, 0), (64, (64, 48), 0, 0),
+                                                       (32, (128, 96), 0, 0),
+                                                       (32, (128, 96), 16, 0),
+                                                       (32, (128, 96), 32, 0),
+                                                       (32, (256, 128), 0, 1)])
+def test_segment_tapes_match_retaping(om_lib, oracle, monkeypatch, precision, size, tile, limit):
     # The backward pass recomputes each segment with the taped step, keeping
     # one tape per step; when those tapes cannot be allocated it recomputes
     # with the plain step and tapes each step again before its reverse.  The
     # taped step writes the same states as the plain one, so both paths give
     # the same gradient bit for bit.  128 x 96 FP32 runs the persistent
-    # 32 x 32 kernel (plain and taped; paired with tile_x 0, one wall per
-    # thread with tile_x 32), 64 x 48 the tile kernels.
+    # 32 x 32 kernel (plain and taped; paired with tile_x 0 and 16, one wall
+    # per thread with tile_x 32), 64 x 48 the tile kernels; 256 x 128 with
+    # one CTA (32 tiles, 16 per group) its two-group form.
     steps = 9
     st = noisy_kh(oracle, size, 21)
     if precision == 32:
@@ -187,7 +190,7 @@ def test_segment_tapes_match_retaping(om_lib, oracle, monkeypatch, precision, si
     cot = tuple(rng.standard_normal(a.shape).astype(st[0].dtype) for a in st)
     grads = []
     for retape in (False, True):
-        h = make(om_lib, size, precision, tile_x=tile)
+        h = make(om_lib, size, precision, tile_x=tile, grid_limit=limit)
         h.set_state(st)
         if retape:
             monkeypatch.setenv("OM_FAIL_ALLOC_AFTER", "0")
