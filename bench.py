@@ -875,7 +875,11 @@ def adjoint_workload(args, dist: Dist) -> dict:
                                f"{args.adj_precision} steps, loss mean((rho_T - target)^2), "
                                "target 1.5 + 8 Fourier modes (amplitude 0.1), gradient w.r.t. "
                                "initial rho, vx, vy, p", "n0": n, "n1": n,
-                   "parallelism": f"replicas x{dist.world}"},
+                   "parallelism": f"replicas x{dist.world}",
+                   "l2": (f"no flush: a {n}x{n} state ({4 * n * n * args.adj_precision // 8 >> 20} "
+                          "MiB) fits in L2 and the forward and reverse steps are compute- and "
+                          "latency-bound; a reverse step reads 24 taped arrays of the same "
+                          "size")},
         "forward_step_ms": round(fwd_ms, 4), "adjoint_step_ms": round(vjp_ms, 4),
         "taped_step_ms": round(tape_ms, 4),
         "per_step_cost_over_forward": {
