@@ -63,10 +63,13 @@ typedef struct {
   int tile_x;       /* Life: tile width in 32-cell words; Hydro: tile width in cells (0 = tuned) */
   int tile_y;       /* tile height in cells (0 = tuned; Hydro FP32: 0 = the persistent
                        32 x 32 kernel on grids whose sides are multiples of 32 and
-                       at least 64, else the 32 x 32 tile kernel; 8, 16 and 32
-                       with tile_x 0 or 32, 8 and 16 with tile_x 64 are tile
-                       kernels; a negative -k selects the column sweep of k rows
-                       per chunk, 8 or 16) */
+                       at least 64 (else the 32 x 32 tile kernel): with tile_x 0
+                       paired, as one CTA per SM of two groups half a tile apart
+                       when every group gets at least 16 tiles, else two CTAs per
+                       SM; with tile_x 16 paired, two CTAs per SM; with tile_x 32
+                       one wall per thread.  8, 16 and 32 with tile_x 0 or 32, 8
+                       and 16 with tile_x 64 are tile kernels; a negative -k
+                       selects the column sweep of k rows per chunk, 8 or 16) */
   int use_graph;    /* capture om_run_n in a CUDA graph (default 1) */
   int variant;      /* 0 = fastest path.  Life 1: integer one-cell-per-thread kernel only.
                        Hydro 1: plain unfused FP64-structured grid-stride kernels */
